@@ -1,0 +1,181 @@
+/*
+ * tensorsat_gb300.h -- C ABI of the GB300 (sm_103a) executor for TensorSat's hot path:
+ * contracting the Boolean tensor network a CNF instance compiles to, pairwise, along a
+ * contraction tree, in the OR-AND semiring (SAT bit) or over exact integers (model count).
+ *
+ * Conventions (all entry points):
+ *   - plain C types only; every pointer named `*_dev` or documented as "device" is a
+ *     device pointer owned by the caller; host arrays are read during the call only;
+ *   - tensors are dense and C-ordered (first port = slowest-varying index), exactly like
+ *     the numpy arrays held by tensorsat's FinRel;
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream); every call is
+ *     asynchronous with respect to the host unless stated otherwise;
+ *   - no entry point allocates device memory on the contraction path: the tree executor
+ *     runs inside a caller-provided workspace whose size tsg_plan_workspace_bytes reports;
+ *   - errors are returned as status codes (never as exceptions); tsg_last_error() returns
+ *     a message describing the last failing call on the calling thread.
+ *
+ * Reference interfaces replaced (paths are relative to the tensorsat project root):
+ *   tsg_contract2_or_and     FinRel._contract2            tensorsat/lang/fin_rel.py:255-288
+ *   tsg_contract2_count_u64  the unclamped einsum of the #SAT prototype
+ *                            notebooks/prototypes/2025-02-13-#sat-tensor-contraction.ipynb
+ *                            (cells 11-12); the count semantics FinRel itself never offers
+ *   tsg_rewire_or_and        FinRel._rewire                tensorsat/lang/fin_rel.py:379-393
+ *                            (with misc.rewire_array       tensorsat/_utils/misc.py:104-123)
+ *   tsg_union_or             FinRel._union                 tensorsat/lang/fin_rel.py:345-346
+ *   tsg_spider_fill          FinRel._spider                tensorsat/lang/fin_rel.py:290-298
+ *   tsg_plan_create / tsg_plan_run
+ *                            the per-node loop of a contraction tree:
+ *                            SimpleContraction.contract    tensorsat/contractions/simple.py:251-292
+ *                            and CotengraContraction.contract (tree.contract, one einsum per
+ *                            node through tensorsat/_autoray.py:31-62)
+ *                                                          tensorsat/contractions/cotengra.py:100-128
+ *                            with sliced indices combined by `+` (OR for FinRel,
+ *                            tensorsat/diagrams.py:965-970) or by integer sum (counts).
+ */
+#ifndef TENSORSAT_GB300_H
+#define TENSORSAT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define TSG_API __attribute__((visibility("default")))
+#else
+#define TSG_API
+#endif
+
+typedef int32_t tsg_status;
+
+#define TSG_OK 0
+#define TSG_ERR_INVALID_ARGUMENT 1 /* bad ranks, wires, dims or pointers (ValueError upstream) */
+#define TSG_ERR_UNSUPPORTED 2      /* valid request outside what the kernels implement */
+#define TSG_ERR_TOO_LARGE 3        /* a tensor or index space exceeds the 64-bit / size limits */
+#define TSG_ERR_WORKSPACE 4        /* workspace missing, misaligned or smaller than required */
+#define TSG_ERR_CUDA 5             /* a CUDA runtime call failed (message has the CUDA error) */
+#define TSG_ERR_TIMEOUT 6          /* a bounded device-side wait gave up */
+
+/* Arithmetic of a tree run (tsg_plan_run). */
+#define TSG_RING_OR_AND 0 /* uint8 {0,1}: out = OR_k (L AND R); the SAT-bit semiring */
+#define TSG_RING_MODP 1   /* uint32 residues mod odd primes < 2^31, one plane per prime */
+#define TSG_RING_U64 2    /* uint64 with wrap-around: the count modulo 2^64 */
+
+#define TSG_MAX_PORTS 64  /* ports per operand of a per-step contraction */
+#define TSG_MAX_BITS 62   /* wires of one tree-step index space (out bits + summed bits) */
+#define TSG_MAX_PRIMES 4  /* residue planes per TSG_RING_MODP run */
+
+/* Message of the last failing call on this thread ("" if none). Never NULL. */
+TSG_API const char* tsg_last_error(void);
+
+/* ABI version of this library (incremented on incompatible changes). */
+TSG_API int32_t tsg_abi_version(void);
+
+/* ---------------------------------------------------------------------------------
+ * Per-step (box-level) operations. Wires are arbitrary int64 labels; a label may repeat
+ * inside lhs_wires, rhs_wires or out_wires (einsum diagonal semantics), and every out
+ * wire must occur in lhs or rhs. Dims are given per port; ports carrying the same wire
+ * must have equal dims. Wires of lhs/rhs that are absent from out_wires are summed.
+ * ------------------------------------------------------------------------------- */
+
+/* out = sign(einsum(lhs, lhs_wires, rhs, rhs_wires -> out_wires)) over uint8 {0,1}
+ * tensors; out has shape (dim of out_wires[i])_i. Replaces FinRel._contract2. */
+TSG_API tsg_status tsg_contract2_or_and(const uint8_t* lhs_dev, int32_t lhs_rank,
+                                const int64_t* lhs_wires, const int64_t* lhs_dims,
+                                const uint8_t* rhs_dev, int32_t rhs_rank,
+                                const int64_t* rhs_wires, const int64_t* rhs_dims,
+                                int32_t out_rank, const int64_t* out_wires,
+                                uint8_t* out_dev, void* stream);
+
+/* Same index semantics with uint64 entries and no clamping (counts, wrap mod 2^64). */
+TSG_API tsg_status tsg_contract2_count_u64(const uint64_t* lhs_dev, int32_t lhs_rank,
+                                   const int64_t* lhs_wires, const int64_t* lhs_dims,
+                                   const uint64_t* rhs_dev, int32_t rhs_rank,
+                                   const int64_t* rhs_wires, const int64_t* rhs_dims,
+                                   int32_t out_rank, const int64_t* out_wires,
+                                   uint64_t* out_dev, void* stream);
+
+/* out = sign(rewire(in, out_ports)): permute / duplicate (diagonal) / discard (sum)
+ * ports of a uint8 {0,1} tensor. Replaces FinRel._rewire. */
+TSG_API tsg_status tsg_rewire_or_and(const uint8_t* in_dev, int32_t rank, const int64_t* dims,
+                             int32_t out_rank, const int32_t* out_ports, uint8_t* out_dev,
+                             void* stream);
+
+/* out[i] = a[i] | b[i] for i < n (uint8). Replaces FinRel._union. */
+TSG_API tsg_status tsg_union_or(const uint8_t* a_dev, const uint8_t* b_dev, uint8_t* out_dev,
+                        int64_t n, void* stream);
+
+/* Writes the COPY/spider tensor of `num_ports` ports of dimension `dim`:
+ * out[i,...,i] = 1, every other entry 0. Replaces FinRel._spider. */
+TSG_API tsg_status tsg_spider_fill(uint8_t* out_dev, int64_t dim, int32_t num_ports, void* stream);
+
+/* ---------------------------------------------------------------------------------
+ * Tree executor. A plan is a contraction tree over wires of dimension 2 (bits), with an
+ * optional set of sliced wires. Leaves are uint8 {0,1} tensors, packed into one device
+ * pool; sliced wires stay inside the leaves and are fixed per slice by the executor.
+ *
+ * Leaf l: rank leaf_ranks[l] (bits, sliced bits included), element offset
+ *   leaf_offsets[l] in the pool, and for each sliced wire j < num_sliced the bit position
+ *   leaf_slice_pos[l*num_sliced + j] of that wire inside the leaf index (bit 0 = last,
+ *   fastest port), or -1 if the leaf does not carry it. Slice id bit j = value of sliced
+ *   wire j.
+ * Step s combines operands step_operands[2s] and step_operands[2s+1] (a value v >= 0 is
+ *   leaf v; v < 0 is the result of step -v-1, which must precede s). Its index space has
+ *   step_out_bits[s] output bits and step_sum_bits[s] summed bits. For operand X in
+ *   {lhs, rhs}: step_lhs_pos / step_rhs_pos[s*TSG_MAX_BITS + i] is the bit position inside
+ *   X of output bit i (i < out_bits), then of summed bit i-out_bits, or -1 when X does not
+ *   carry that wire. Output bit i of step s is bit i of its result tensor. Every
+ *   intermediate is consumed exactly once; the last step is the root.
+ * ------------------------------------------------------------------------------- */
+typedef struct tsg_plan tsg_plan;
+
+TSG_API tsg_status tsg_plan_create(int32_t num_leaves, const int32_t* leaf_ranks,
+                           const int64_t* leaf_offsets, int32_t num_sliced,
+                           const int32_t* leaf_slice_pos, int32_t num_steps,
+                           const int32_t* step_operands, const int32_t* step_out_bits,
+                           const int32_t* step_sum_bits, const int32_t* step_lhs_pos,
+                           const int32_t* step_rhs_pos, tsg_plan** plan_out);
+
+TSG_API void tsg_plan_destroy(tsg_plan* plan);
+
+/* Bytes of workspace tsg_plan_run needs for `group_size` slices per launch group. */
+TSG_API tsg_status tsg_plan_workspace_bytes(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                                    int64_t group_size, int64_t* bytes_out);
+
+/* Root output bits of the plan (the result tensor has 2^bits entries per plane). */
+TSG_API tsg_status tsg_plan_root_bits(const tsg_plan* plan, int32_t* bits_out);
+
+/* Number of kernel launches tsg_plan_run issues for the given slice range and group. */
+TSG_API tsg_status tsg_plan_launch_count(const tsg_plan* plan, int64_t slice_begin,
+                                 int64_t slice_end, int64_t group_size, int64_t* count_out);
+
+/* Contracts slices [slice_begin, slice_end) of the plan, `group_size` slices per launch
+ * group (a power of two; slice_begin must be a multiple of it, the last group may be
+ * partial), and combines the per-slice root tensors into result_dev:
+ *   OR_AND: uint8 [2^root_bits], OR over slices;
+ *   MODP:   uint32 [num_primes][2^root_bits], sum mod primes[p];
+ *   U64:    uint64 [2^root_bits], sum mod 2^64.
+ * If accumulate != 0 the result is combined with the existing contents of result_dev,
+ * otherwise it is overwritten. leaf_pool_dev holds the uint8 leaves. workspace_dev must
+ * be 256-byte aligned and at least tsg_plan_workspace_bytes long. Every launch is
+ * bounds-checked on the host first (see tsg_plan_validate). */
+TSG_API tsg_status tsg_plan_run(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                        const uint32_t* primes, const uint8_t* leaf_pool_dev,
+                        int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                        void* workspace_dev, int64_t workspace_bytes, void* result_dev,
+                        int32_t accumulate, void* stream);
+
+/* Builds every launch tsg_plan_run would issue for these arguments and checks, on the
+ * host, that each operand offset stays inside its leaf or workspace buffer. Touches no
+ * device memory and needs no GPU. */
+TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                             const uint32_t* primes, int64_t slice_begin,
+                             int64_t slice_end, int64_t group_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TENSORSAT_GB300_H */

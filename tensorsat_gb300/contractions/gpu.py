@@ -1,0 +1,466 @@
+"""Tree-executor contractions on the GPU: the drop-in for ``CotengraContraction``.
+
+:class:`GpuContraction` plays the role of ``CotengraContraction``
+(``tensorsat/contractions/cotengra.py:51-131``): it is built once for a box class and a
+wiring (planning a contraction tree with the project's own optimiser,
+:mod:`tensorsat_gb300.planner`, in place of ``ctg.array_contract_tree``), exposes the tree
+and its pop/append ``path``, and ``contract(diagram)`` returns the contracted box. Where
+cotengra runs one einsum per tree node through ``tensorsat/_autoray.py:31-62``, this class
+hands the whole tree to the native executor (``tsg_plan_run``): every node is a device
+kernel and sliced wires run as batched groups of slices.
+
+Beyond the reference, :meth:`GpuContraction.count` returns the exact model count: the same
+tree contracted over the integers, either modulo 2^64 (exact when the count bound is below
+2^64) or modulo up to four 31-bit primes recombined by the Chinese remainder theorem.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+from typing import Any, Sequence
+
+import numpy as np
+import torch
+
+from .. import _device, _native, planner
+from ..diagrams import Diagram, TensorLikeType, Wiring
+from ..lang.cuda_rel import CudaRel, leaf_array
+from .abc import Contraction
+
+PRIMES_31 = (2147483647, 2147483629, 2147483587, 2147483579)
+"""Moduli of the residue count ring: the four largest primes below 2^31."""
+
+DEFAULT_TARGET_BITS = 26
+
+
+@dataclass
+class _Leaves:
+    """How the wiring's slots become bit-network leaves."""
+
+    leaf_wires: list[tuple[int, ...]]
+    slot_of_leaf: list[int | None]
+    synthetic: list[np.ndarray | None]
+    diag_slots: frozenset[int]
+    discard_factor: int
+    out_unique: tuple[int, ...]
+    wire_dims: dict[int, int]
+
+
+def _prepare(wiring: Wiring) -> _Leaves:
+    dims = {w: t.tensor_dim for w, t in enumerate(wiring.wire_types)}
+    leaf_wires: list[tuple[int, ...]] = []
+    slot_of_leaf: list[int | None] = []
+    synthetic: list[np.ndarray | None] = []
+    diag = set()
+    for s, ws in enumerate(wiring.slot_wires_list):
+        uniq = tuple(dict.fromkeys(ws))
+        if len(uniq) != len(ws):
+            diag.add(s)
+        leaf_wires.append(uniq)
+        slot_of_leaf.append(s)
+        synthetic.append(None)
+    out_set = set(wiring.out_wires)
+    factor = 1
+    for w in sorted(wiring.dangling_wires):
+        if w in out_set:
+            leaf_wires.append((w,))
+            slot_of_leaf.append(None)
+            synthetic.append(np.ones(dims[w], dtype=np.uint8))
+        else:
+            factor *= dims[w]
+    while len(leaf_wires) < 2:
+        leaf_wires.append(())
+        slot_of_leaf.append(None)
+        synthetic.append(np.ones((), dtype=np.uint8))
+    return _Leaves(leaf_wires, slot_of_leaf, synthetic, frozenset(diag), factor,
+                   tuple(dict.fromkeys(wiring.out_wires)), dims)
+
+
+def _functional_wire(t: np.ndarray) -> int | None:
+    """A port whose value is a function of the other ports (exactly one 1 per assignment
+    of the others), if any."""
+    if t.ndim == 0 or t.size > 1 << 12:
+        return None
+    for p in range(t.ndim):
+        if np.all(t.sum(axis=p) == 1):
+            return p
+    return None
+
+
+def count_bound_bits(wiring: Wiring, arrays: Sequence[np.ndarray]) -> float:
+    """log2 of an upper bound on every entry of the count tensor of a 0/1 network: a
+    wire whose value is a function of the others at one tensor (a gate output, a
+    constant) adds nothing, every other summed wire adds log2(dim)."""
+    determined: set[int] = set()
+    for ws, arr in zip(wiring.slot_wires_list, arrays):
+        if len(set(ws)) != len(ws):
+            continue
+        p = _functional_wire(arr)
+        if p is not None and ws[p] not in determined:
+            determined.add(ws[p])
+    out = set(wiring.out_wires)
+    bits = 0.0
+    for w, t in enumerate(wiring.wire_types):
+        if w in out or w in determined:
+            continue
+        bits += math.log2(t.tensor_dim)
+    return bits
+
+
+def crt(residues: Sequence[np.ndarray], moduli: Sequence[int]) -> np.ndarray:
+    """Chinese remaindering of per-prime residue arrays into Python integers."""
+    M = 1
+    for p in moduli:
+        M *= p
+    shape = residues[0].shape
+    flat = [r.reshape(-1) for r in residues]
+    out = np.empty(flat[0].shape[0], dtype=object)
+    coeffs = []
+    for p in moduli:
+        Mi = M // p
+        coeffs.append(Mi * pow(Mi, -1, p))
+    for i in range(out.shape[0]):
+        out[i] = sum(int(r[i]) * c for r, c in zip(flat, coeffs)) % M
+    return out.reshape(shape)
+
+
+class NativePlan:
+    """Owner of a ``tsg_plan`` handle built from a :class:`planner.SlicedPlan`."""
+
+    def __init__(self, plan: planner.SlicedPlan) -> None:
+        lib = _native.lib()
+        arrs = plan.native_arrays()
+        ranks = arrs["leaf_ranks"]
+        sizes = [1 << int(r) for r in ranks]
+        offsets = np.zeros(len(sizes), dtype=np.int64)
+        off = 0
+        for i, n in enumerate(sizes):
+            offsets[i] = off
+            off += (n + 15) // 16 * 16
+        self.leaf_offsets = offsets
+        self.leaf_sizes = sizes
+        self.pool_bytes = max(off, 16)
+        self.num_sliced = len(plan.sliced)
+        self._arrs = arrs
+        handle = _native.c_void_p()
+        lsp = np.ascontiguousarray(arrs["leaf_slice_pos"], dtype=np.int32)
+        st = lib.tsg_plan_create(
+            len(ranks), _native.ptr_i32(ranks), _native.ptr_i64(offsets), self.num_sliced,
+            _native.ptr_i32(lsp), len(arrs["step_out_bits"]),
+            _native.ptr_i32(np.ascontiguousarray(arrs["step_operands"])),
+            _native.ptr_i32(arrs["step_out_bits"]), _native.ptr_i32(arrs["step_sum_bits"]),
+            _native.ptr_i32(arrs["step_lhs_pos"]), _native.ptr_i32(arrs["step_rhs_pos"]),
+            _native.ctypes.byref(handle),
+        )
+        _native.check(st)
+        self.handle = handle
+        self._lib = lib
+
+    def workspace_bytes(self, ring: int, num_primes: int, group: int) -> int:
+        out = _native.c_int64()
+        _native.check(self._lib.tsg_plan_workspace_bytes(self.handle, ring, num_primes, group,
+                                                         _native.ctypes.byref(out)))
+        return int(out.value)
+
+    def launch_count(self, begin: int, end: int, group: int) -> int:
+        out = _native.c_int64()
+        _native.check(self._lib.tsg_plan_launch_count(self.handle, begin, end, group,
+                                                      _native.ctypes.byref(out)))
+        return int(out.value)
+
+    def validate(self, ring: int, primes: Sequence[int], begin: int, end: int, group: int) -> None:
+        """Host-side bounds check of every launch (no GPU needed)."""
+        parr = (_native.c_uint32 * max(1, len(primes)))(*primes)
+        _native.check(self._lib.tsg_plan_validate(self.handle, ring, len(primes), parr, begin,
+                                                  end, group))
+
+    def run(self, ring: int, primes: Sequence[int], pool: torch.Tensor, begin: int, end: int,
+            group: int, workspace: torch.Tensor, result: torch.Tensor, accumulate: bool,
+            stream: int) -> None:
+        parr = (_native.c_uint32 * max(1, len(primes)))(*primes)
+        st = self._lib.tsg_plan_run(
+            self.handle, ring, len(primes), parr, pool.data_ptr(), begin, end, group,
+            workspace.data_ptr(), workspace.numel(), result.data_ptr(), int(bool(accumulate)),
+            stream,
+        )
+        _native.check(st)
+
+    def __del__(self) -> None:
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._lib.tsg_plan_destroy(h)
+            except Exception:  # pragma: no cover - interpreter shutdown
+                pass
+            self.handle = None
+
+
+class GpuContraction(Contraction):
+    """Contraction of bit networks (all wires of dimension 2) by the GPU tree executor.
+
+    :param optimize: accepted for signature parity with ``CotengraContraction``; every
+        value selects the project's min-fill tree search (``"greedy"``, ``"auto"``, ...).
+    :param target_bits: slice until every intermediate has at most ``2**target_bits``
+        entries (``None``: never slice).
+    :param trials: randomized elimination orders tried; the cheapest tree is kept.
+    :param tree, sliced: use this tree (and sliced wires) instead of searching.
+    """
+
+    def __init__(
+        self,
+        box_class: type,
+        wiring: Wiring,
+        *,
+        optimize: Any = "auto",
+        target_bits: int | None = DEFAULT_TARGET_BITS,
+        trials: int = 8,
+        seed: int = 0,
+        tree: planner.ContractionTree | None = None,
+        sliced: Sequence[int] | None = None,
+        canonicalize: bool = True,
+        sort_contraction_indices: bool = False,
+    ) -> None:
+        super().__init__(box_class, wiring)
+        if wiring.num_wires == 0 and wiring.num_slots == 0:
+            raise ValueError("Cannot define contraction for empty wiring.")
+        for t in wiring.wire_types:
+            if not isinstance(t, TensorLikeType):
+                raise ValueError("Wiring must have tensor-like wire types.")
+        self._optimize = optimize
+        self._leaves = _prepare(wiring)
+        lw = self._leaves
+        if any(d != 2 for w, d in lw.wire_dims.items()
+               if any(w in ws for ws in lw.leaf_wires) or w in lw.out_unique):
+            raise NotImplementedError(
+                "GpuContraction executes bit networks: every connected wire must have"
+                " dimension 2"
+            )
+        net = planner.Network(lw.leaf_wires, {w: 2 for ws in lw.leaf_wires for w in ws},
+                              lw.out_unique)
+        self._network = net
+        if tree is None:
+            tree, sl = planner.optimize(net, target_bits=target_bits, trials=trials, seed=seed)
+        else:
+            sl = frozenset(sliced or ())
+        self._tree = tree
+        self._plan = planner.SlicedPlan(tree, tuple(sorted(sl)), list(lw.leaf_wires))
+        self._native: NativePlan | None = None
+        self._pool_cache: tuple[int, torch.Tensor] | None = None
+
+    # -- plan inspection ------------------------------------------------------------
+
+    @property
+    def tree(self) -> planner.ContractionTree:
+        return self._tree
+
+    @property
+    def path(self) -> tuple[tuple[int, int], ...]:
+        """The tree as a pop/append path over the prepared leaves."""
+        return self._tree.linear_path()
+
+    @property
+    def sliced_wires(self) -> tuple[int, ...]:
+        return self._plan.sliced
+
+    @property
+    def num_slices(self) -> int:
+        return self._plan.num_slices
+
+    @property
+    def sliced_plan(self) -> planner.SlicedPlan:
+        return self._plan
+
+    @property
+    def discard_factor(self) -> int:
+        """Factor of the count contributed by wires connected to nothing (each summed
+        freely); :meth:`run` results exclude it, :meth:`count` includes it."""
+        return self._leaves.discard_factor
+
+    def stats(self) -> dict[str, float]:
+        sl = frozenset(self._plan.sliced)
+        tot, peak, wr = self._tree.cost(sl)
+        return {
+            "steps": len(self._tree.steps),
+            "log2_index_space_per_slice": tot,
+            "peak_bits": peak,
+            "log2_written_per_slice": wr,
+            "num_sliced": len(sl),
+            "log2_total_index_space": tot + len(sl),
+        }
+
+    def native_plan(self) -> NativePlan:
+        if self._native is None:
+            self._native = NativePlan(self._plan)
+        return self._native
+
+    # -- leaves -----------------------------------------------------------------------
+
+    def leaf_pool(self, diagram: Diagram) -> torch.Tensor:
+        """The diagram's leaf tensors packed into one device uint8 buffer (cached for the
+        last diagram)."""
+        if self._pool_cache is not None and self._pool_cache[0] == id(diagram):
+            return self._pool_cache[1]
+        dev = _device.require_cuda()
+        npl = self.native_plan()
+        lw = self._leaves
+        host = np.zeros(npl.pool_bytes, dtype=np.uint8)
+        device_leaves: list[tuple[int, Any]] = []
+        boxes = diagram.blocks
+        for l, (slot, syn) in enumerate(zip(lw.slot_of_leaf, lw.synthetic)):
+            off = int(npl.leaf_offsets[l])
+            if syn is not None:
+                host[off: off + syn.size] = syn.reshape(-1)
+                continue
+            box = boxes[slot]
+            on_device = isinstance(box, CudaRel) and box._tensor.device.type == "cuda"
+            if slot in lw.diag_slots or on_device:
+                device_leaves.append((l, box))
+                continue
+            arr = (box._tensor.numpy() if isinstance(box, CudaRel) else leaf_array(box))
+            arr = arr.reshape(-1)
+            host[off: off + arr.size] = arr
+        pool = torch.from_numpy(host).to(dev, non_blocking=False)
+        stream = _device.stream_handle()
+        for l, box in device_leaves:
+            off = int(npl.leaf_offsets[l])
+            slot = lw.slot_of_leaf[l]
+            t = box.device_tensor() if isinstance(box, CudaRel) else _device.to_device_u8(
+                torch.from_numpy(leaf_array(box)))
+            if slot in lw.diag_slots:
+                ws = list(self._wiring.slot_wires_list[slot])
+                uniq = list(lw.leaf_wires[l])
+                one = torch.ones((), dtype=torch.uint8, device=dev)
+                st = _native.lib().tsg_contract2_or_and(
+                    t.data_ptr(), len(ws), _native.i64_array(ws), _native.i64_array(t.shape),
+                    one.data_ptr(), 0, _native.i64_array([]), _native.i64_array([]),
+                    len(uniq), _native.i64_array(uniq), pool.data_ptr() + off, stream)
+                _native.check(st)
+            else:
+                pool[off: off + t.numel()].copy_(t.reshape(-1))
+        self._pool_cache = (id(diagram), pool)
+        return pool
+
+    # -- execution --------------------------------------------------------------------
+
+    def choose_group(self, ring: int, num_primes: int, budget_bytes: int | None = None,
+                     max_group: int = 4096) -> int:
+        """Largest power-of-two slice group whose workspace fits the budget (default: 40%
+        of free device memory)."""
+        npl = self.native_plan()
+        if npl.num_sliced == 0:
+            return 1
+        if budget_bytes is None:
+            free, _ = torch.cuda.mem_get_info()
+            budget_bytes = int(free * 0.4)
+        g = min(self.num_slices, max_group)
+        while g > 1 and npl.workspace_bytes(ring, num_primes, g) > budget_bytes:
+            g //= 2
+        return g
+
+    def run(self, diagram: Diagram | None, ring: int, primes: Sequence[int] = (),
+            slice_range: tuple[int, int] | None = None, group: int | None = None,
+            pool: torch.Tensor | None = None, workspace: torch.Tensor | None = None,
+            result: torch.Tensor | None = None, accumulate: bool = False) -> torch.Tensor:
+        """Runs the tree executor over a slice range and returns the device result
+        (uint8 / uint64 / uint32[planes] over the root's 2^bits entries)."""
+        dev = _device.require_cuda()
+        npl = self.native_plan()
+        if pool is None:
+            if diagram is None:
+                raise ValueError("run() needs a diagram or a leaf pool")
+            self.validate(diagram)
+            pool = self.leaf_pool(diagram)
+        planes = len(primes) if ring == _native.TSG_RING_MODP else 1
+        b, e = slice_range if slice_range is not None else (0, self.num_slices)
+        if group is None:
+            group = self.choose_group(ring, planes)
+        if workspace is None:
+            workspace = torch.empty(npl.workspace_bytes(ring, planes, group), dtype=torch.uint8,
+                                    device=dev)
+        entries = 1 << len(self._leaves.out_unique)
+        if result is None:
+            if ring == _native.TSG_RING_OR_AND:
+                result = torch.zeros(entries, dtype=torch.uint8, device=dev)
+            elif ring == _native.TSG_RING_U64:
+                result = torch.zeros(entries, dtype=torch.int64, device=dev)
+            else:
+                result = torch.zeros(planes * entries, dtype=torch.int32, device=dev)
+        npl.run(ring, primes, pool, b, e, group, workspace, result, accumulate,
+                _device.stream_handle())
+        return result
+
+    def contract(self, diagram: Diagram, *, progbar: bool = False, order: Any = None,
+                 autojit: Any = "auto", group: int | None = None) -> CudaRel:
+        """Validates and contracts the diagram in the OR-AND semiring; returns the result
+        box (a scalar box for a SAT network: ``bool(box)`` is the SAT bit)."""
+        self.validate(diagram)
+        res = self.run(diagram, _native.TSG_RING_OR_AND, group=group)
+        lw = self._leaves
+        k = len(lw.out_unique)
+        box = CudaRel._new(res.reshape((2,) * k))
+        if tuple(self._wiring.out_wires) != lw.out_unique:
+            box = box._rewire([lw.out_unique.index(w) for w in self._wiring.out_wires])
+        return box
+
+    def count(self, diagram: Diagram, *, ring: str = "auto", num_primes: int | None = None,
+              group: int | None = None) -> Any:
+        """Exact model count (``int``) of a closed network, or a numpy object array of
+        counts indexed by the out wires.
+
+        ``ring="u64"`` counts modulo 2^64, ``"modp"`` modulo ``num_primes`` 31-bit primes
+        with CRT, ``"auto"`` picks u64 when the count bound is below 2^64 and otherwise
+        enough primes for the bound.
+        """
+        self.validate(diagram)
+        arrays = []
+        for blk in diagram.blocks:
+            try:
+                arrays.append(leaf_array(blk))
+            except TypeError:
+                arrays.append(np.zeros((), dtype=np.uint8))
+        bound = count_bound_bits(self._wiring, arrays)
+        if ring == "auto":
+            ring = "u64" if bound < 64 else "modp"
+        if ring == "u64":
+            if bound >= 64:
+                raise OverflowError("count bound exceeds 2^64: use ring='modp'")
+            res = self.run(diagram, _native.TSG_RING_U64, group=group)
+            vals = res.cpu().numpy().view(np.uint64)
+            counts = np.array([int(v) for v in vals], dtype=object)
+        elif ring == "modp":
+            if num_primes is None:
+                num_primes = max(1, min(4, math.ceil((bound + 1) / 30.9)))
+            primes = PRIMES_31[:num_primes]
+            if sum(math.log2(p) for p in primes) <= bound:
+                raise OverflowError(
+                    f"count bound 2^{bound:.0f} needs more than {num_primes} 31-bit primes"
+                )
+            res = self.run(diagram, _native.TSG_RING_MODP, primes=primes, group=group)
+            planes = res.cpu().numpy().view(np.uint32).reshape(num_primes, -1)
+            counts = crt([planes[p] for p in range(num_primes)], primes)
+        else:
+            raise ValueError(f"unknown count ring {ring!r}")
+        lw = self._leaves
+        counts = counts * lw.discard_factor
+        k = len(lw.out_unique)
+        if k == 0:
+            return int(counts[0])
+        arr = counts.reshape((2,) * k)
+        outs = self._wiring.out_wires
+        if tuple(outs) == lw.out_unique:
+            return arr
+        # expand repeated / permuted out wires (diagonal entries, zeros elsewhere)
+        full = np.zeros((2,) * len(outs), dtype=object)
+        for idx in np.ndindex(*full.shape):
+            vals = {}
+            ok = True
+            for w, v in zip(outs, idx):
+                if vals.setdefault(w, v) != v:
+                    ok = False
+                    break
+            full[idx] = arr[tuple(vals[w] for w in lw.out_unique)] if ok else 0
+        return full
+
+    def __repr__(self) -> str:
+        return "<GpuContraction>"

@@ -1,0 +1,813 @@
+// Tree executor of the tensorsat_gb300 C ABI: runs every pairwise contraction of a
+// contraction tree over bit-indexed tensors (all wires of dimension 2) on the device, for
+// a range of slices, and combines the per-slice roots. This replaces the per-node loop of
+// SimpleContraction.contract (tensorsat/contractions/simple.py:251-292) and of cotengra's
+// tree.contract behind CotengraContraction.contract (tensorsat/contractions/cotengra.py:
+// 100-128), each node of which ends in FinRel._contract2 (tensorsat/lang/fin_rel.py:255-288).
+//
+// Data layout in HBM. A tensor over r bit-wires is a dense array of 2^r entries; bit i of
+// the linear index is the value of the tensor's i-th wire counted from the last port
+// (numpy C order). Slice-dependent intermediates hold `group` slices back to back:
+// element (g, x) lives at g * 2^r + x. TSG_RING_MODP tensors keep one uint32 plane per
+// prime, planes back to back. Leaves are uint8 {0,1} in one pool and keep their sliced
+// wires; the executor selects the slice by fixing those bits.
+//
+// Index mapping. A step's thread index t packs (group slot g, output index o) as
+// g * 2^out_bits + o. Each operand offset is a bit scatter of t plus a bit scatter of the
+// summed index k, both encoded as runs (src bit, length, dst bit) so contiguous wires move
+// as one shift-and-mask.
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "tsg_common.cuh"
+
+namespace tsg {
+namespace {
+
+constexpr int kMaxRuns = 64;
+constexpr int kThreads = 256;
+
+struct BitMap {
+  int32_t n;
+  uint8_t src[kMaxRuns];
+  uint8_t len[kMaxRuns];
+  uint8_t dst[kMaxRuns];
+};
+
+struct StepArgs {
+  const uint8_t* lhs;
+  const uint8_t* rhs;
+  uint8_t* out;
+  uint64_t l_base, r_base;             // constant element offsets
+  uint64_t l_plane, r_plane, o_plane;  // residue-plane strides (elements)
+  uint64_t total;                      // output entries of this launch
+  int32_t k_bits;
+  BitMap lt, lk, rt, rk;
+};
+
+struct RingArgs {
+  int32_t np;
+  uint32_t p[TSG_MAX_PRIMES];
+  uint64_t m[TSG_MAX_PRIMES];  // Barrett constants floor((2^64-1)/p)
+};
+
+__device__ __forceinline__ uint64_t scatter_bits(const BitMap& m, uint64_t x) {
+  uint64_t r = 0;
+#pragma unroll 1
+  for (int i = 0; i < m.n; ++i)
+    r |= ((x >> m.src[i]) & ((1ull << m.len[i]) - 1ull)) << m.dst[i];
+  return r;
+}
+
+template <bool kLeaf, typename T>
+__device__ __forceinline__ T load_elem(const uint8_t* base, uint64_t off) {
+  if constexpr (kLeaf) {
+    return (T)base[off];
+  } else {
+    return reinterpret_cast<const T*>(base)[off];
+  }
+}
+
+// One pairwise contraction step: out[t] = sum_k lhs[scatter(t,k)] * rhs[scatter(t,k)] in
+// the ring kRing. kLLeaf / kRLeaf mark uint8 leaf operands (widened on load).
+template <int kRing, bool kLLeaf, bool kRLeaf>
+__global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArgs ring) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t nk = 1ull << a.k_bits;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.total; t += stride) {
+    const uint64_t lo = a.l_base + scatter_bits(a.lt, t);
+    const uint64_t ro = a.r_base + scatter_bits(a.rt, t);
+    if constexpr (kRing == TSG_RING_OR_AND) {
+      uint32_t acc = 0;
+      for (uint64_t kk = 0; kk < nk; ++kk) {
+        acc |= (uint32_t)a.lhs[lo + scatter_bits(a.lk, kk)] &
+               (uint32_t)a.rhs[ro + scatter_bits(a.rk, kk)];
+      }
+      a.out[t] = acc ? 1 : 0;
+    } else if constexpr (kRing == TSG_RING_U64) {
+      uint64_t acc = 0;
+      for (uint64_t kk = 0; kk < nk; ++kk) {
+        acc += load_elem<kLLeaf, uint64_t>(a.lhs, lo + scatter_bits(a.lk, kk)) *
+               load_elem<kRLeaf, uint64_t>(a.rhs, ro + scatter_bits(a.rk, kk));
+      }
+      reinterpret_cast<uint64_t*>(a.out)[t] = acc;
+    } else {
+      uint64_t acc[TSG_MAX_PRIMES] = {0, 0, 0, 0};
+      for (uint64_t kk = 0; kk < nk; ++kk) {
+        const uint64_t lko = lo + scatter_bits(a.lk, kk);
+        const uint64_t rko = ro + scatter_bits(a.rk, kk);
+        if constexpr (kLLeaf && kRLeaf) {
+          const uint64_t v = (uint64_t)(a.lhs[lko] & a.rhs[rko]);
+#pragma unroll
+          for (int p = 0; p < TSG_MAX_PRIMES; ++p) acc[p] += v;
+        } else {
+#pragma unroll
+          for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
+            if (p < ring.np) {
+              const uint64_t l = load_elem<kLLeaf, uint32_t>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane));
+              const uint64_t r = load_elem<kRLeaf, uint32_t>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane));
+              // acc < p < 2^31 and l * r < 2^62, so the sum stays below 2^63
+              acc[p] = barrett_reduce(acc[p] + l * r, ring.p[p], ring.m[p]);
+            }
+          }
+        }
+      }
+      uint32_t* out = reinterpret_cast<uint32_t*>(a.out);
+#pragma unroll
+      for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
+        if (p < ring.np) out[t + p * a.o_plane] = barrett_reduce(acc[p], ring.p[p], ring.m[p]);
+      }
+    }
+  }
+}
+
+// Combines the root tensors of `cnt` slices (layout [plane][cnt][E]) into result[E]
+// (OR for OR_AND, sum mod 2^64 for U64, sum mod p per plane for MODP). One block per root
+// entry; threads stride over slices, then a shared-memory tree reduction.
+template <int kRing>
+__global__ void __launch_bounds__(kThreads)
+    root_reduce_kernel(const uint8_t* root, uint64_t cnt, uint64_t entries, uint64_t plane,
+                       uint8_t* result, int accumulate, RingArgs ring) {
+  __shared__ uint64_t red[kThreads];
+  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
+  for (uint64_t e = blockIdx.x; e < entries; e += gridDim.x) {
+    for (int p = 0; p < np; ++p) {
+      uint64_t part = 0;
+      for (uint64_t g = threadIdx.x; g < cnt; g += blockDim.x) {
+        const uint64_t idx = p * plane + g * entries + e;
+        if constexpr (kRing == TSG_RING_OR_AND) {
+          part |= root[idx];
+        } else if constexpr (kRing == TSG_RING_U64) {
+          part += reinterpret_cast<const uint64_t*>(root)[idx];
+        } else {
+          // residues < 2^31 summed over at most 2^32 slices per thread stay below 2^63
+          part += reinterpret_cast<const uint32_t*>(root)[idx];
+        }
+      }
+      if constexpr (kRing == TSG_RING_MODP) part = barrett_reduce(part, ring.p[p], ring.m[p]);
+      red[threadIdx.x] = part;
+      __syncthreads();
+      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+          if constexpr (kRing == TSG_RING_OR_AND) {
+            red[threadIdx.x] |= red[threadIdx.x + s];
+          } else {
+            red[threadIdx.x] += red[threadIdx.x + s];  // MODP: each term < 2^31, 256 terms
+          }
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        uint64_t v = red[0];
+        if constexpr (kRing == TSG_RING_OR_AND) {
+          if (accumulate) v |= result[e];
+          result[e] = v ? 1 : 0;
+        } else if constexpr (kRing == TSG_RING_U64) {
+          uint64_t* r = reinterpret_cast<uint64_t*>(result);
+          r[e] = accumulate ? r[e] + v : v;
+        } else {
+          uint32_t* r = reinterpret_cast<uint32_t*>(result) + p * entries;
+          if (accumulate) v += r[e];
+          r[e] = barrett_reduce(v, ring.p[p], ring.m[p]);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Host side.
+
+struct LeafInfo {
+  int rank;
+  int64_t offset;
+  std::vector<int> spos;  // bit position of each sliced wire, -1 if absent
+  bool dep;
+};
+
+struct StepInfo {
+  int op[2];
+  int out_bits, k_bits;
+  int pos[2][TSG_MAX_BITS];
+  bool dep;
+};
+
+struct Layout {
+  int64_t group;
+  int64_t elem_bytes;
+  int planes;
+  std::vector<int64_t> offset;  // byte offset of each step's output in the workspace
+  std::vector<int64_t> plane;   // plane stride (elements) of each step's output
+  int64_t bytes;
+};
+
+bool operand_dep(const std::vector<LeafInfo>& leaves, const std::vector<StepInfo>& steps, int v) {
+  return v >= 0 ? leaves[v].dep : steps[-v - 1].dep;
+}
+
+int operand_rank(const std::vector<LeafInfo>& leaves, const std::vector<StepInfo>& steps, int v) {
+  return v >= 0 ? leaves[v].rank : steps[-v - 1].out_bits;
+}
+
+int64_t align256(int64_t x) { return (x + 255) & ~int64_t(255); }
+
+// First-fit allocator over a byte range, used to place intermediates by liveness.
+class Arena {
+ public:
+  int64_t alloc(int64_t bytes) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        const int64_t off = it->first;
+        const int64_t rest = it->second - bytes;
+        free_.erase(it);
+        if (rest > 0) free_[off + bytes] = rest;
+        return off;
+      }
+    }
+    const int64_t off = top_;
+    top_ += bytes;
+    return off;
+  }
+  void release(int64_t off, int64_t bytes) {
+    auto it = free_.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+    // give back a free block that touches the top
+    if (!free_.empty()) {
+      auto last = std::prev(free_.end());
+      if (last->first + last->second == top_) {
+        top_ = last->first;
+        free_.erase(last);
+      }
+    }
+  }
+  int64_t peak() const { return peak_; }
+  void note() { peak_ = std::max(peak_, top_); }
+
+ private:
+  std::map<int64_t, int64_t> free_;
+  int64_t top_ = 0;
+  int64_t peak_ = 0;
+};
+
+}  // namespace
+}  // namespace tsg
+
+struct tsg_plan {
+  std::vector<tsg::LeafInfo> leaves;
+  std::vector<tsg::StepInfo> steps;
+  int num_sliced = 0;
+  int root_bits = 0;
+  int64_t max_entry_bits = 0;
+  std::vector<tsg::Layout> layouts;  // cache keyed by (group, elem_bytes, planes)
+};
+
+namespace tsg {
+namespace {
+
+tsg_status elem_info(int32_t ring, int32_t num_primes, int64_t* elem_bytes, int* planes) {
+  switch (ring) {
+    case TSG_RING_OR_AND:
+      *elem_bytes = 1;
+      *planes = 1;
+      return TSG_OK;
+    case TSG_RING_U64:
+      *elem_bytes = 8;
+      *planes = 1;
+      return TSG_OK;
+    case TSG_RING_MODP:
+      if (num_primes < 1 || num_primes > TSG_MAX_PRIMES)
+        return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: MODP needs 1..4 primes");
+      *elem_bytes = 4;
+      *planes = num_primes;
+      return TSG_OK;
+    default:
+      return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: unknown ring");
+  }
+}
+
+tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int planes,
+                      const Layout** out) {
+  for (const Layout& l : plan->layouts) {
+    if (l.group == group && l.elem_bytes == elem_bytes && l.planes == planes) {
+      *out = &l;
+      return TSG_OK;
+    }
+  }
+  const auto& steps = plan->steps;
+  const int ns = (int)steps.size();
+  Layout lay;
+  lay.group = group;
+  lay.elem_bytes = elem_bytes;
+  lay.planes = planes;
+  lay.offset.assign(ns, -1);
+  lay.plane.assign(ns, 0);
+  std::vector<int64_t> bytes(ns, 0);
+  for (int s = 0; s < ns; ++s) {
+    const int64_t slices = steps[s].dep ? group : 1;
+    if (steps[s].out_bits + 64 - __builtin_clzll((unsigned long long)slices) > 62)
+      return fail(TSG_ERR_TOO_LARGE, "plan_run: group * tensor size exceeds 2^62 entries");
+    const int64_t elems = slices << steps[s].out_bits;
+    lay.plane[s] = elems;
+    const long double b = (long double)elems * elem_bytes * planes;
+    if (b > 9.0e18L) return fail(TSG_ERR_TOO_LARGE, "plan_run: tensor bytes overflow");
+    bytes[s] = align256(elems * elem_bytes * planes);
+  }
+  Arena arena;
+  // prologue: slice-independent steps; then one group of slice-dependent steps.
+  for (int phase = 0; phase < 2; ++phase) {
+    for (int s = 0; s < ns; ++s) {
+      if (steps[s].dep != (phase == 1)) continue;
+      lay.offset[s] = arena.alloc(bytes[s]);
+      arena.note();
+      for (int o = 0; o < 2; ++o) {
+        const int v = steps[s].op[o];
+        if (v >= 0) continue;
+        const int x = -v - 1;
+        // an independent result read by a dependent step is re-read by every group
+        if (!steps[x].dep && steps[s].dep) continue;
+        arena.release(lay.offset[x], bytes[x]);
+      }
+    }
+  }
+  lay.bytes = std::max<int64_t>(arena.peak(), 256);
+  plan->layouts.push_back(lay);
+  *out = &plan->layouts.back();
+  return TSG_OK;
+}
+
+// Encodes (src bit -> dst bit) pairs, sorted by src, as runs.
+tsg_status make_bitmap(std::vector<std::pair<int, int>> pairs, BitMap* m) {
+  std::sort(pairs.begin(), pairs.end());
+  std::memset(m, 0, sizeof(*m));
+  for (const auto& pr : pairs) {
+    if (m->n > 0) {
+      const int i = m->n - 1;
+      if (m->src[i] + m->len[i] == pr.first && m->dst[i] + m->len[i] == pr.second) {
+        m->len[i]++;
+        continue;
+      }
+    }
+    if (m->n >= kMaxRuns) return fail(TSG_ERR_TOO_LARGE, "plan_run: too many bit runs");
+    m->src[m->n] = (uint8_t)pr.first;
+    m->dst[m->n] = (uint8_t)pr.second;
+    m->len[m->n] = 1;
+    m->n++;
+  }
+  return TSG_OK;
+}
+
+struct RunCtx {
+  const tsg_plan* plan;
+  const Layout* lay;
+  int ring;
+  RingArgs ra;
+  const uint8_t* pool;
+  uint8_t* ws;
+  cudaStream_t stream;
+  int g_bits;  // log2(group)
+};
+
+template <int kRing, bool kL, bool kR>
+void launch_step_t(const StepArgs& a, const RingArgs& ra, cudaStream_t st) {
+  tree_step_kernel<kRing, kL, kR><<<grid_for(a.total, kThreads, 8), kThreads, 0, st>>>(a, ra);
+}
+
+template <int kRing>
+void launch_step_ring(bool l_leaf, bool r_leaf, const StepArgs& a, const RingArgs& ra,
+                      cudaStream_t st) {
+  if (l_leaf) {
+    if (r_leaf) launch_step_t<kRing, true, true>(a, ra, st);
+    else launch_step_t<kRing, true, false>(a, ra, st);
+  } else {
+    if (r_leaf) launch_step_t<kRing, false, true>(a, ra, st);
+    else launch_step_t<kRing, false, false>(a, ra, st);
+  }
+}
+
+// Largest value scatter_bits(m, x) takes for any x < 2^bits (the runs are disjoint bit
+// fields, so setting every source bit maximises the result).
+uint64_t scatter_max(const BitMap& m, int bits) {
+  uint64_t r = 0;
+  for (int i = 0; i < m.n; ++i) {
+    for (int b = 0; b < m.len[i]; ++b) {
+      if (m.src[i] + b < bits) r |= 1ull << (m.dst[i] + b);
+    }
+  }
+  return r;
+}
+
+int bit_width(uint64_t x) { return x == 0 ? 0 : 64 - __builtin_clzll((unsigned long long)x); }
+
+// Host-side bounds check of one launch: every element offset the kernel can form for an
+// operand must stay inside that operand (its leaf, or its workspace buffer), and the
+// output index inside the output buffer. Runs before every launch and in
+// tsg_plan_validate, so an inconsistent plan is reported instead of reaching the GPU.
+tsg_status check_step_bounds(const RunCtx& c, int s, const StepArgs& a, const bool is_leaf[2]) {
+  const tsg_plan* plan = c.plan;
+  const StepInfo& st = plan->steps[s];
+  const int tbits = bit_width(a.total - 1);
+  if (a.total > (uint64_t)c.lay->plane[s])
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan bounds: output exceeds its buffer");
+  for (int o = 0; o < 2; ++o) {
+    const BitMap& tm = o == 0 ? a.lt : a.rt;
+    const BitMap& km = o == 0 ? a.lk : a.rk;
+    const uint64_t base = o == 0 ? a.l_base : a.r_base;
+    const uint64_t hi = base + scatter_max(tm, tbits) + scatter_max(km, st.k_bits);
+    const int v = st.op[o];
+    uint64_t lo_ext, hi_ext;
+    if (is_leaf[o]) {
+      const LeafInfo& lf = plan->leaves[v];
+      lo_ext = (uint64_t)lf.offset;
+      hi_ext = lo_ext + (1ull << lf.rank);
+    } else {
+      lo_ext = 0;
+      hi_ext = (uint64_t)c.lay->plane[-v - 1];
+    }
+    if (base < lo_ext || hi >= hi_ext)
+      return fail(TSG_ERR_INVALID_ARGUMENT, "plan bounds: operand offset outside its tensor");
+  }
+  return TSG_OK;
+}
+
+// Fills the kernel arguments of step s for slices [base, base + cnt) (cnt == 1 and base
+// ignored for slice-independent steps).
+tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, StepArgs* out,
+                      bool is_leaf_out[2]) {
+  const tsg_plan* plan = c.plan;
+  const StepInfo& st = plan->steps[s];
+  const int gb = st.dep ? c.g_bits : 0;
+  StepArgs& a = *out;
+  std::memset(&a, 0, sizeof(a));
+  a.total = (uint64_t)(st.dep ? cnt : 1) << st.out_bits;
+  a.k_bits = st.k_bits;
+  a.out = c.ws + c.lay->offset[s];
+  a.o_plane = (uint64_t)c.lay->plane[s];
+  bool is_leaf[2];
+  for (int o = 0; o < 2; ++o) {
+    const int v = st.op[o];
+    std::vector<std::pair<int, int>> tp, kp;
+    for (int i = 0; i < st.out_bits; ++i)
+      if (st.pos[o][i] >= 0) tp.push_back({i, st.pos[o][i]});
+    for (int i = 0; i < st.k_bits; ++i)
+      if (st.pos[o][st.out_bits + i] >= 0) kp.push_back({i, st.pos[o][st.out_bits + i]});
+    uint64_t basec = 0;
+    const uint8_t* ptr;
+    uint64_t plane = 0;
+    if (v >= 0) {
+      const LeafInfo& lf = plan->leaves[v];
+      ptr = c.pool;
+      basec = (uint64_t)lf.offset;
+      for (int j = 0; j < plan->num_sliced; ++j) {
+        if (lf.spos[j] < 0) continue;
+        if (st.dep && j < gb) {
+          tp.push_back({st.out_bits + j, lf.spos[j]});
+        } else if (st.dep) {
+          basec += (uint64_t)((base >> j) & 1) << lf.spos[j];
+        }
+      }
+      is_leaf[o] = true;
+    } else {
+      const int x = -v - 1;
+      const StepInfo& xs = plan->steps[x];
+      ptr = c.ws + c.lay->offset[x];
+      plane = (uint64_t)c.lay->plane[x];
+      if (xs.dep)
+        for (int j = 0; j < gb; ++j) tp.push_back({st.out_bits + j, xs.out_bits + j});
+      is_leaf[o] = false;
+    }
+    BitMap* tm = o == 0 ? &a.lt : &a.rt;
+    BitMap* km = o == 0 ? &a.lk : &a.rk;
+    TSG_TRY(make_bitmap(tp, tm));
+    TSG_TRY(make_bitmap(kp, km));
+    if (o == 0) {
+      a.lhs = ptr;
+      a.l_base = basec;
+      a.l_plane = plane;
+    } else {
+      a.rhs = ptr;
+      a.r_base = basec;
+      a.r_plane = plane;
+    }
+  }
+  is_leaf_out[0] = is_leaf[0];
+  is_leaf_out[1] = is_leaf[1];
+  return check_step_bounds(c, s, a, is_leaf);
+}
+
+tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
+  StepArgs a;
+  bool is_leaf[2];
+  TSG_TRY(build_step(c, s, base, cnt, &a, is_leaf));
+  switch (c.ring) {
+    case TSG_RING_OR_AND:
+      // every OR_AND operand is uint8, leaf or not
+      launch_step_t<TSG_RING_OR_AND, true, true>(a, c.ra, c.stream);
+      break;
+    case TSG_RING_U64:
+      launch_step_ring<TSG_RING_U64>(is_leaf[0], is_leaf[1], a, c.ra, c.stream);
+      break;
+    default:
+      launch_step_ring<TSG_RING_MODP>(is_leaf[0], is_leaf[1], a, c.ra, c.stream);
+      break;
+  }
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status launch_reduce(const RunCtx& c, int64_t cnt, uint8_t* result, int accumulate) {
+  const tsg_plan* plan = c.plan;
+  const int root = (int)plan->steps.size() - 1;
+  const uint64_t entries = 1ull << plan->root_bits;
+  const uint8_t* rp = c.ws + c.lay->offset[root];
+  const uint64_t plane = (uint64_t)c.lay->plane[root];
+  unsigned blocks = (unsigned)std::min<uint64_t>(entries, (uint64_t)device_sm_count() * 8);
+  switch (c.ring) {
+    case TSG_RING_OR_AND:
+      root_reduce_kernel<TSG_RING_OR_AND><<<blocks, kThreads, 0, c.stream>>>(
+          rp, (uint64_t)cnt, entries, plane, result, accumulate, c.ra);
+      break;
+    case TSG_RING_U64:
+      root_reduce_kernel<TSG_RING_U64><<<blocks, kThreads, 0, c.stream>>>(
+          rp, (uint64_t)cnt, entries, plane, result, accumulate, c.ra);
+      break;
+    default:
+      root_reduce_kernel<TSG_RING_MODP><<<blocks, kThreads, 0, c.stream>>>(
+          rp, (uint64_t)cnt, entries, plane, result, accumulate, c.ra);
+      break;
+  }
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
+
+tsg_status check_range(const tsg_plan* plan, int64_t slice_begin, int64_t slice_end,
+                       int64_t group) {
+  const int64_t nslices = int64_t(1) << plan->num_sliced;
+  if (!is_pow2(group)) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: group size must be a power of two");
+  if (slice_begin < 0 || slice_end > nslices || slice_begin >= slice_end)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: empty or out-of-range slice range");
+  if (slice_begin % group != 0)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: slice_begin must be a multiple of the group size");
+  if (plan->num_sliced == 0 && group != 1)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: unsliced plans run with group size 1");
+  if (group > nslices) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: group larger than the slice count");
+  return TSG_OK;
+}
+
+}  // namespace
+}  // namespace tsg
+
+namespace tsg {
+namespace {
+
+// Shared body of tsg_plan_run and tsg_plan_validate. With dry == true no pointer is
+// dereferenced and nothing is launched: every launch's arguments are built and
+// bounds-checked only.
+tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                    const uint32_t* primes, const uint8_t* pool, int64_t slice_begin,
+                    int64_t slice_end, int64_t group_size, void* workspace,
+                    int64_t workspace_bytes, void* result_dev, int32_t accumulate,
+                    cudaStream_t stream, bool dry) {
+  TSG_TRY(check_range(plan, slice_begin, slice_end, group_size));
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  RingArgs ra;
+  std::memset(&ra, 0, sizeof(ra));
+  if (ring == TSG_RING_MODP) {
+    if (!primes) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: MODP needs primes");
+    ra.np = num_primes;
+    for (int p = 0; p < num_primes; ++p) {
+      if (primes[p] < 3 || primes[p] >= (1u << 31) || (primes[p] % 2) == 0)
+        return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: moduli must be odd and in [3, 2^31)");
+      ra.p[p] = primes[p];
+      ra.m[p] = UINT64_MAX / primes[p];
+    }
+  }
+  const Layout* lay;
+  TSG_TRY(get_layout(const_cast<tsg_plan*>(plan), group_size, eb, planes, &lay));
+  if (!dry) {
+    if (!workspace || workspace_bytes < lay->bytes)
+      return fail(TSG_ERR_WORKSPACE, "plan_run: workspace smaller than tsg_plan_workspace_bytes");
+    if (((uintptr_t)workspace & 255) != 0)
+      return fail(TSG_ERR_WORKSPACE, "plan_run: workspace must be 256-byte aligned");
+  }
+  RunCtx c;
+  c.plan = plan;
+  c.lay = lay;
+  c.ring = ring;
+  c.ra = ra;
+  c.pool = pool;
+  c.ws = (uint8_t*)workspace;
+  c.stream = stream;
+  c.g_bits = 0;
+  while ((int64_t(1) << c.g_bits) < group_size) c.g_bits++;
+  const int ns = (int)plan->steps.size();
+  auto step = [&](int s, int64_t base, int64_t cnt) -> tsg_status {
+    if (!dry) return launch_step(c, s, base, cnt);
+    StepArgs a;
+    bool is_leaf[2];
+    return build_step(c, s, base, cnt, &a, is_leaf);
+  };
+  for (int s = 0; s < ns; ++s)
+    if (!plan->steps[s].dep) TSG_TRY(step(s, 0, 1));
+  uint8_t* result = (uint8_t*)result_dev;
+  if (!plan->steps.back().dep) {
+    return dry ? TSG_OK : launch_reduce(c, 1, result, accumulate);
+  }
+  bool first = true;
+  for (int64_t base = slice_begin; base < slice_end; base += group_size) {
+    const int64_t cnt = std::min<int64_t>(group_size, slice_end - base);
+    for (int s = 0; s < ns; ++s)
+      if (plan->steps[s].dep) TSG_TRY(step(s, base, cnt));
+    if (!dry) TSG_TRY(launch_reduce(c, cnt, result, first ? accumulate : 1));
+    first = false;
+  }
+  return TSG_OK;
+}
+
+}  // namespace
+}  // namespace tsg
+
+using namespace tsg;
+
+extern "C" {
+
+tsg_status tsg_plan_create(int32_t num_leaves, const int32_t* leaf_ranks,
+                           const int64_t* leaf_offsets, int32_t num_sliced,
+                           const int32_t* leaf_slice_pos, int32_t num_steps,
+                           const int32_t* step_operands, const int32_t* step_out_bits,
+                           const int32_t* step_sum_bits, const int32_t* step_lhs_pos,
+                           const int32_t* step_rhs_pos, tsg_plan** plan_out) {
+  if (!plan_out) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_create: null output pointer");
+  *plan_out = nullptr;
+  if (num_leaves < 1 || num_steps < 1 || num_steps != num_leaves - 1)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_create: a tree over L leaves has L-1 steps (L >= 2)");
+  if (num_sliced < 0 || num_sliced > 62)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_create: sliced wires must number 0..62");
+  if (!leaf_ranks || !leaf_offsets || (num_sliced > 0 && !leaf_slice_pos) || !step_operands ||
+      !step_out_bits || !step_sum_bits || !step_lhs_pos || !step_rhs_pos)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_create: null array");
+  tsg_plan* plan = new tsg_plan();
+  auto bad = [&](tsg_status code, const std::string& msg) {
+    delete plan;
+    return fail(code, msg);
+  };
+  plan->num_sliced = num_sliced;
+  plan->leaves.resize(num_leaves);
+  std::vector<int> sliced_seen(num_sliced, 0);
+  for (int l = 0; l < num_leaves; ++l) {
+    LeafInfo& lf = plan->leaves[l];
+    lf.rank = leaf_ranks[l];
+    lf.offset = leaf_offsets[l];
+    if (lf.rank < 0 || lf.rank > TSG_MAX_BITS || lf.offset < 0)
+      return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: leaf rank or offset out of range");
+    lf.spos.assign(num_sliced, -1);
+    lf.dep = false;
+    for (int j = 0; j < num_sliced; ++j) {
+      const int p = leaf_slice_pos[(int64_t)l * num_sliced + j];
+      if (p < -1 || p >= lf.rank)
+        return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: sliced bit position outside the leaf");
+      lf.spos[j] = p;
+      if (p >= 0) {
+        lf.dep = true;
+        sliced_seen[j] = 1;
+      }
+    }
+  }
+  for (int j = 0; j < num_sliced; ++j)
+    if (!sliced_seen[j])
+      return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: a sliced wire appears in no leaf");
+  std::vector<int> leaf_uses(num_leaves, 0), step_uses(num_steps, 0);
+  plan->steps.resize(num_steps);
+  for (int s = 0; s < num_steps; ++s) {
+    StepInfo& st = plan->steps[s];
+    st.out_bits = step_out_bits[s];
+    st.k_bits = step_sum_bits[s];
+    if (st.out_bits < 0 || st.k_bits < 0 || st.out_bits + st.k_bits > TSG_MAX_BITS)
+      return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: step index space exceeds 62 bits");
+    for (int o = 0; o < 2; ++o) {
+      const int v = step_operands[2 * s + o];
+      st.op[o] = v;
+      if (v >= 0) {
+        if (v >= num_leaves) return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: leaf id out of range");
+        leaf_uses[v]++;
+      } else {
+        const int x = -v - 1;
+        if (x >= s) return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: step reads a later step");
+        step_uses[x]++;
+      }
+      const int32_t* pos = (o == 0 ? step_lhs_pos : step_rhs_pos) + (int64_t)s * TSG_MAX_BITS;
+      const int rank = operand_rank(plan->leaves, plan->steps, v);
+      // every bit of the operand must be an output bit, a summed bit or a sliced bit
+      std::vector<int> cover(rank, 0);
+      for (int i = 0; i < st.out_bits + st.k_bits; ++i) {
+        const int p = pos[i];
+        st.pos[o][i] = p;
+        if (p < -1 || p >= rank)
+          return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: bit position outside the operand");
+        if (p >= 0) {
+          if (cover[p]) return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: operand bit mapped twice");
+          cover[p] = 1;
+        }
+      }
+      for (int i = st.out_bits + st.k_bits; i < TSG_MAX_BITS; ++i) st.pos[o][i] = -1;
+      if (v >= 0) {
+        for (int j = 0; j < num_sliced; ++j) {
+          const int p = plan->leaves[v].spos[j];
+          if (p < 0) continue;
+          if (cover[p]) return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: sliced bit also indexed");
+          cover[p] = 1;
+        }
+      }
+      for (int b = 0; b < rank; ++b)
+        if (!cover[b]) return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: operand bit not covered");
+    }
+    // every summed bit must be carried by at least one operand, every output bit too
+    for (int i = 0; i < st.out_bits + st.k_bits; ++i)
+      if (st.pos[0][i] < 0 && st.pos[1][i] < 0)
+        return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: index bit carried by neither operand");
+    st.dep = operand_dep(plan->leaves, plan->steps, st.op[0]) ||
+             operand_dep(plan->leaves, plan->steps, st.op[1]);
+  }
+  for (int l = 0; l < num_leaves; ++l)
+    if (leaf_uses[l] != 1) return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: each leaf is used once");
+  for (int s = 0; s + 1 < num_steps; ++s)
+    if (step_uses[s] != 1)
+      return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: each non-root step is consumed once");
+  if (step_uses[num_steps - 1] != 0)
+    return bad(TSG_ERR_INVALID_ARGUMENT, "plan_create: the root step must not be consumed");
+  plan->root_bits = plan->steps.back().out_bits;
+  *plan_out = plan;
+  return TSG_OK;
+}
+
+void tsg_plan_destroy(tsg_plan* plan) { delete plan; }
+
+tsg_status tsg_plan_root_bits(const tsg_plan* plan, int32_t* bits_out) {
+  if (!plan || !bits_out) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_root_bits: null pointer");
+  *bits_out = plan->root_bits;
+  return TSG_OK;
+}
+
+tsg_status tsg_plan_workspace_bytes(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                                    int64_t group_size, int64_t* bytes_out) {
+  if (!plan || !bytes_out) return fail(TSG_ERR_INVALID_ARGUMENT, "workspace_bytes: null pointer");
+  if (!is_pow2(group_size)) return fail(TSG_ERR_INVALID_ARGUMENT, "workspace_bytes: group must be a power of two");
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  const Layout* lay;
+  TSG_TRY(get_layout(const_cast<tsg_plan*>(plan), group_size, eb, planes, &lay));
+  *bytes_out = lay->bytes;
+  return TSG_OK;
+}
+
+tsg_status tsg_plan_launch_count(const tsg_plan* plan, int64_t slice_begin, int64_t slice_end,
+                                 int64_t group_size, int64_t* count_out) {
+  if (!plan || !count_out) return fail(TSG_ERR_INVALID_ARGUMENT, "launch_count: null pointer");
+  TSG_TRY(check_range(plan, slice_begin, slice_end, group_size));
+  int64_t indep = 0, dep = 0;
+  for (const auto& s : plan->steps) (s.dep ? dep : indep)++;
+  const int64_t groups = (slice_end - slice_begin + group_size - 1) / group_size;
+  *count_out = plan->steps.back().dep ? indep + groups * (dep + 1) : indep + 1;
+  return TSG_OK;
+}
+
+tsg_status tsg_plan_run(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                        const uint32_t* primes, const uint8_t* leaf_pool_dev,
+                        int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                        void* workspace_dev, int64_t workspace_bytes, void* result_dev,
+                        int32_t accumulate, void* stream) {
+  if (!plan || !leaf_pool_dev || !result_dev)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: null pointer");
+  return run_impl(plan, ring, num_primes, primes, leaf_pool_dev, slice_begin, slice_end,
+                  group_size, workspace_dev, workspace_bytes, result_dev, accumulate,
+                  (cudaStream_t)stream, /*dry=*/false);
+}
+
+tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                             const uint32_t* primes, int64_t slice_begin, int64_t slice_end,
+                             int64_t group_size) {
+  if (!plan) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_validate: null plan");
+  return run_impl(plan, ring, num_primes, primes, nullptr, slice_begin, slice_end, group_size,
+                  nullptr, 0, nullptr, 0, nullptr, /*dry=*/true);
+}
+
+}  // extern "C"

@@ -1,0 +1,458 @@
+"""Contraction planning for bit-indexed tensor networks: trees, slicing and layouts.
+
+The reference delegates path search to cotengra (``ctg.array_contract_tree`` in
+``tensorsat/contractions/cotengra.py:78-85``), which is not vendored. This module is the
+project's own optimiser:
+
+* :func:`build_tree` turns a wire elimination order into a binary contraction tree. Every
+  wire that is neither an output wire nor needed by another remaining tensor is summed at
+  the first step where that becomes true (cotengra's index bookkeeping, as opposed to
+  ``SimpleContraction`` which keeps every wire until the root,
+  ``tensorsat/contractions/simple.py:263-272``).
+* :func:`minfill_order` produces elimination orders (min-fill with random tie breaking)
+  after a growth-free simplification pass that absorbs gates and unit tensors.
+* :func:`slice_tree` picks wires to slice (fix per slice) until every intermediate holds at
+  most ``2**target_bits`` entries; slices are independent sub-contractions combined by OR
+  (SAT) or sum (counts), like cotengra's sliced ``tree.contract``.
+* :class:`SlicedPlan` fixes the wire order (the HBM layout) of every intermediate and
+  emits the integer arrays consumed by ``tsg_plan_create``.
+
+Answers never depend on the tree; trees only change cost.
+"""
+
+from __future__ import annotations
+
+import math
+import random
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+TSG_MAX_BITS = 62
+
+
+@dataclass
+class Network:
+    """A tensor network over wires: leaf wire tuples, wire dims and open (output) wires."""
+
+    leaf_wires: list[tuple[int, ...]]
+    wire_dims: dict[int, int]
+    out_wires: tuple[int, ...] = ()
+
+    def __post_init__(self) -> None:
+        for ws in self.leaf_wires:
+            if len(set(ws)) != len(ws):
+                raise ValueError("leaf tensors must carry distinct wires")
+            for w in ws:
+                if w not in self.wire_dims:
+                    raise ValueError(f"wire {w} has no dimension")
+        for w in self.out_wires:
+            if w not in self.wire_dims:
+                raise ValueError(f"output wire {w} has no dimension")
+
+    @property
+    def all_bits(self) -> bool:
+        return all(d == 2 for d in self.wire_dims.values())
+
+
+@dataclass
+class ContractionTree:
+    """Binary contraction tree in SSA form.
+
+    Node ids ``0..L-1`` are the leaves; step ``s`` creates node ``L+s`` from
+    ``steps[s] = (a, b)``. ``node_wires[x]`` is the wire set of node ``x``;
+    ``summed[s]`` the wires summed at step ``s``.
+    """
+
+    num_leaves: int
+    steps: list[tuple[int, int]]
+    node_wires: list[frozenset[int]]
+    out_wires: tuple[int, ...]
+
+    @property
+    def root(self) -> int:
+        return self.num_leaves + len(self.steps) - 1
+
+    def step_union(self, s: int) -> frozenset[int]:
+        a, b = self.steps[s]
+        return self.node_wires[a] | self.node_wires[b]
+
+    def summed(self, s: int) -> frozenset[int]:
+        return self.step_union(s) - self.node_wires[self.num_leaves + s]
+
+    def cost(self, sliced: frozenset[int] = frozenset()) -> tuple[float, int, float]:
+        """(log2 total index-space size, max intermediate bits, log2 written entries)."""
+        tot = 0.0
+        wr = 0.0
+        peak = 0
+        L = self.num_leaves
+        for s in range(len(self.steps)):
+            u = len(self.step_union(s) - sliced)
+            o = len(self.node_wires[L + s] - sliced)
+            tot += 2.0**u
+            wr += 2.0**o
+            peak = max(peak, o)
+        return (math.log2(tot) if tot > 0 else 0.0, peak, math.log2(wr) if wr > 0 else 0.0)
+
+    def linear_path(self) -> tuple[tuple[int, int], ...]:
+        """The tree as an opt_einsum-style pop/append path (the format of
+        ``SimpleContraction``, ``tensorsat/contractions/simple.py:38-46``)."""
+        live = list(range(self.num_leaves))
+        path = []
+        for s, (a, b) in enumerate(self.steps):
+            i = live.index(a)
+            j = live.index(b)
+            path.append((i, j))
+            for x in sorted((i, j), reverse=True):
+                live.pop(x)
+            live.append(self.num_leaves + s)
+        return tuple(path)
+
+
+def _primal(tensors: dict[int, frozenset[int]], protect: frozenset[int]) -> dict[int, set[int]]:
+    adj: dict[int, set[int]] = {}
+    for ws in tensors.values():
+        for w in ws:
+            if w in protect:
+                continue
+            nb = adj.setdefault(w, set())
+            nb.update(x for x in ws if x != w and x not in protect)
+    return adj
+
+
+def build_tree(net: Network, order: Sequence[int]) -> ContractionTree:
+    """Builds the contraction tree that eliminates wires in ``order``.
+
+    Eliminating wire ``w`` merges every remaining tensor that carries ``w``, pairwise,
+    smallest union first. Leftover tensors (disjoint components, output-only tensors) are
+    merged at the end by smallest union.
+    """
+    L = len(net.leaf_wires)
+    out = frozenset(net.out_wires)
+    node_wires: list[frozenset[int]] = [frozenset(ws) for ws in net.leaf_wires]
+    live: dict[int, frozenset[int]] = {i: node_wires[i] for i in range(L)}
+    holders: dict[int, set[int]] = {}
+    for i, ws in live.items():
+        for w in ws:
+            holders.setdefault(w, set()).add(i)
+    steps: list[tuple[int, int]] = []
+
+    def merge(a: int, b: int) -> int:
+        wa, wb = live.pop(a), live.pop(b)
+        union = wa | wb
+        keep = []
+        for w in union:
+            hs = holders[w]
+            hs.discard(a)
+            hs.discard(b)
+            if hs or w in out:
+                keep.append(w)
+        x = L + len(steps)
+        steps.append((a, b))
+        res = frozenset(keep)
+        node_wires.append(res)
+        live[x] = res
+        for w in res:
+            holders[w].add(x)
+        return x
+
+    def merge_group(group: list[int]) -> None:
+        group = list(group)
+        while len(group) > 1:
+            best = None
+            for i in range(len(group)):
+                wi = live[group[i]]
+                for j in range(i + 1, len(group)):
+                    u = len(wi | live[group[j]])
+                    if best is None or u < best[0]:
+                        best = (u, i, j)
+            _, i, j = best
+            a, b = group[i], group[j]
+            x = merge(a, b)
+            group = [g for k, g in enumerate(group) if k not in (i, j)] + [x]
+
+    for w in order:
+        hs = holders.get(w)
+        if not hs or len(hs) < 2:
+            continue
+        merge_group(sorted(hs, key=lambda i: (len(live[i]), i)))
+    rest = sorted(live, key=lambda i: (len(live[i]), i))
+    merge_group(rest)
+    return ContractionTree(L, steps, node_wires, tuple(net.out_wires))
+
+
+def simplify_order(net: Network) -> list[int]:
+    """Growth-free eliminations: wires whose elimination yields a tensor no larger than
+    the largest tensor it absorbs (gates, NOT/unit tensors, clause trees)."""
+    out = frozenset(net.out_wires)
+    tensors = {i: frozenset(ws) for i, ws in enumerate(net.leaf_wires)}
+    holders: dict[int, set[int]] = {}
+    for i, ws in tensors.items():
+        for w in ws:
+            holders.setdefault(w, set()).add(i)
+    order: list[int] = []
+    nxt = len(tensors)
+    changed = True
+    while changed:
+        changed = False
+        for w in sorted(holders):
+            if w in out:
+                continue
+            hs = holders[w]
+            if not hs:
+                continue
+            union = frozenset().union(*(tensors[i] for i in hs))
+            # wires still needed outside this bucket
+            res = frozenset(
+                x for x in union if x in out or (holders[x] - hs)
+            )
+            if len(res) <= max(len(tensors[i]) for i in hs):
+                order.append(w)
+                for i in list(hs):
+                    for x in tensors[i]:
+                        holders[x].discard(i)
+                    del tensors[i]
+                tensors[nxt] = res
+                for x in res:
+                    holders[x].add(nxt)
+                for x in union - res:
+                    holders[x].clear()
+                nxt += 1
+                changed = True
+    return order
+
+
+def minfill_order(net: Network, rng: random.Random, prefix: Sequence[int] = ()) -> list[int]:
+    """Min-fill elimination order (ties broken at random) of the non-output wires,
+    starting after the eliminations in ``prefix``."""
+    out = frozenset(net.out_wires)
+    # replay the prefix on the hypergraph
+    tensors = {i: frozenset(ws) for i, ws in enumerate(net.leaf_wires)}
+    holders: dict[int, set[int]] = {}
+    for i, ws in tensors.items():
+        for w in ws:
+            holders.setdefault(w, set()).add(i)
+    nxt = len(tensors)
+    done: set[int] = set()
+    for w in prefix:
+        hs = holders.get(w, set())
+        done.add(w)
+        if not hs:
+            continue
+        union = frozenset().union(*(tensors[i] for i in hs))
+        res = frozenset(x for x in union if x in out or (holders[x] - hs))
+        for i in list(hs):
+            for x in tensors[i]:
+                holders[x].discard(i)
+            del tensors[i]
+        tensors[nxt] = res
+        for x in res:
+            holders[x].add(nxt)
+        nxt += 1
+        done.update(union - res)
+    adj = _primal(tensors, out)
+    for w in list(adj):
+        if w in done:
+            del adj[w]
+    for w in adj:
+        adj[w] -= done
+    order = list(prefix)
+    alive = set(adj)
+    while alive:
+        best = None
+        cands: list[int] = []
+        for v in alive:
+            nb = adj[v]
+            nbl = list(nb)
+            f = 0
+            for i in range(len(nbl)):
+                ai = adj[nbl[i]]
+                for j in range(i + 1, len(nbl)):
+                    if nbl[j] not in ai:
+                        f += 1
+            key = (f, len(nb))
+            if best is None or key < best:
+                best = key
+                cands = [v]
+            elif key == best:
+                cands.append(v)
+        v = rng.choice(cands)
+        nb = list(adj[v])
+        for a in nb:
+            adj[a].discard(v)
+            for b in nb:
+                if a != b:
+                    adj[a].add(b)
+        alive.discard(v)
+        del adj[v]
+        order.append(v)
+    return order
+
+
+def slice_tree(tree: ContractionTree, target_bits: int, forbid: frozenset[int] = frozenset()
+               ) -> frozenset[int]:
+    """Greedy slicing: repeatedly slice the wire of a largest intermediate that lowers the
+    peak most, breaking ties by the smallest total (all-slices) cost."""
+    sliced: set[int] = set()
+    L = tree.num_leaves
+    while True:
+        tot, peak, _ = tree.cost(frozenset(sliced))
+        if peak <= target_bits:
+            return frozenset(sliced)
+        cands: set[int] = set()
+        for s in range(len(tree.steps)):
+            ws = tree.node_wires[L + s] - sliced
+            if len(ws) == peak:
+                cands |= ws
+        cands -= forbid
+        if not cands:
+            raise ValueError(
+                f"cannot slice below 2^{peak} entries: the largest intermediates only carry"
+                " output wires"
+            )
+        best = None
+        for w in sorted(cands):
+            t2, p2, _ = tree.cost(frozenset(sliced | {w}))
+            key = (p2, t2 + len(sliced) + 1)
+            if best is None or key < best[0]:
+                best = (key, w)
+        sliced.add(best[1])
+
+
+def optimize(net: Network, *, target_bits: int | None = 26, trials: int = 8, seed: int = 0,
+             method: str = "minfill") -> tuple[ContractionTree, frozenset[int]]:
+    """Searches ``trials`` randomized elimination orders and returns the best
+    (tree, sliced wires) by (peak bits after slicing, log2 total cost incl. slices)."""
+    rng = random.Random(seed)
+    prefix = simplify_order(net)
+    forbid = frozenset(net.out_wires)
+    if target_bits is not None:
+        # the root holds every output wire: no slicing can go below that
+        target_bits = max(target_bits, len(forbid))
+    best = None
+    for t in range(max(1, trials)):
+        if method != "minfill":
+            raise ValueError(f"unknown optimisation method {method!r}")
+        order = minfill_order(net, rng, prefix)
+        tree = build_tree(net, order)
+        if target_bits is None:
+            sliced = frozenset()
+        else:
+            sliced = slice_tree(tree, target_bits, forbid)
+        tot, peak, _ = tree.cost(sliced)
+        key = (peak, tot + len(sliced))
+        if best is None or key < best[0]:
+            best = (key, tree, sliced)
+    return best[1], best[2]
+
+
+@dataclass
+class SlicedPlan:
+    """A tree, its sliced wires, and the wire order (layout) of every node.
+
+    Leaves keep their given wire order (sliced wires included); an intermediate stores its
+    non-sliced wires as ``new wires of the smaller operand`` followed by ``kept wires of
+    the larger operand in its order``, so the large operand's low (fastest) bits stay the
+    result's low bits and its reads coalesce.
+    """
+
+    tree: ContractionTree
+    sliced: tuple[int, ...]
+    leaf_wires: list[tuple[int, ...]]
+    node_order: list[tuple[int, ...]] = field(default_factory=list)
+
+    def __post_init__(self) -> None:
+        t = self.tree
+        L = t.num_leaves
+        sl = frozenset(self.sliced)
+        order: list[tuple[int, ...]] = [tuple(ws) for ws in self.leaf_wires]
+        for s, (a, b) in enumerate(t.steps):
+            res = t.node_wires[L + s] - sl
+            oa = [w for w in order[a] if w not in sl]
+            ob = [w for w in order[b] if w not in sl]
+            big, small = (oa, ob) if len(oa) >= len(ob) else (ob, oa)
+            if s == len(t.steps) - 1:
+                # the root is laid out in the order of the output wires
+                outs = [w for w in dict.fromkeys(t.out_wires)]
+                order.append(tuple(outs))
+                continue
+            kept_big = [w for w in big if w in res]
+            new_small = [w for w in small if w in res and w not in big]
+            order.append(tuple(new_small + kept_big))
+            assert frozenset(order[-1]) == res
+        self.node_order = order
+
+    @property
+    def num_slices(self) -> int:
+        return 1 << len(self.sliced)
+
+    def step_bits(self, s: int) -> tuple[list[int], list[int]]:
+        """(output wires by bit index, summed wires by bit index) of step ``s``."""
+        t = self.tree
+        L = t.num_leaves
+        outw = list(reversed(self.node_order[L + s]))  # bit i = wire order[-1-i]
+        sl = frozenset(self.sliced)
+        summed = sorted(t.step_union(s) - t.node_wires[L + s] - sl)
+        return outw, summed
+
+    def native_arrays(self) -> dict[str, np.ndarray]:
+        """Integer arrays for ``tsg_plan_create`` (leaf offsets are left to the caller)."""
+        t = self.tree
+        L = t.num_leaves
+        nsl = len(self.sliced)
+        slice_index = {w: j for j, w in enumerate(self.sliced)}
+        leaf_ranks = np.array([len(ws) for ws in self.leaf_wires], dtype=np.int32)
+        leaf_slice_pos = np.full((L, max(nsl, 1)), -1, dtype=np.int32)
+        for l, ws in enumerate(self.leaf_wires):
+            r = len(ws)
+            for i, w in enumerate(ws):
+                j = slice_index.get(w)
+                if j is not None:
+                    leaf_slice_pos[l, j] = r - 1 - i
+        ns = len(t.steps)
+        ops = np.zeros((ns, 2), dtype=np.int32)
+        out_bits = np.zeros(ns, dtype=np.int32)
+        sum_bits = np.zeros(ns, dtype=np.int32)
+        pos = np.full((2, ns, TSG_MAX_BITS), -1, dtype=np.int32)
+        for s, (a, b) in enumerate(t.steps):
+            outw, summed = self.step_bits(s)
+            if len(outw) + len(summed) > TSG_MAX_BITS:
+                raise ValueError("a contraction step exceeds 62 index bits")
+            out_bits[s] = len(outw)
+            sum_bits[s] = len(summed)
+            for o, x in enumerate((a, b)):
+                ops[s, o] = x if x < L else -(x - L) - 1
+                xo = self.node_order[x]
+                r = len(xo)
+                bitpos = {w: r - 1 - i for i, w in enumerate(xo)}
+                for i, w in enumerate(list(outw) + list(summed)):
+                    p = bitpos.get(w)
+                    if p is not None:
+                        pos[o, s, i] = p
+        return {
+            "leaf_ranks": leaf_ranks,
+            "leaf_slice_pos": np.ascontiguousarray(leaf_slice_pos[:, :nsl]) if nsl else
+            np.zeros((L, 0), dtype=np.int32),
+            "step_operands": ops,
+            "step_out_bits": out_bits,
+            "step_sum_bits": sum_bits,
+            "step_lhs_pos": np.ascontiguousarray(pos[0]),
+            "step_rhs_pos": np.ascontiguousarray(pos[1]),
+        }
+
+    def bytes_per_slice(self, elem_bytes: int, planes: int = 1) -> float:
+        """Algorithmic HBM bytes of one slice: each step reads both operands once and
+        writes its result once (leaves are uint8, other tensors elem_bytes * planes)."""
+        t = self.tree
+        L = t.num_leaves
+        sl = frozenset(self.sliced)
+        tot = 0.0
+        for s, (a, b) in enumerate(t.steps):
+            for x in (a, b):
+                if x < L:
+                    tot += 2.0 ** len(t.node_wires[x] - sl)
+                else:
+                    tot += 2.0 ** len(t.node_wires[x]) * elem_bytes * planes
+            tot += 2.0 ** len(t.node_wires[L + s]) * elem_bytes * planes
+        return tot

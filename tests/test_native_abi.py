@@ -1,0 +1,160 @@
+"""C ABI checks that need no GPU: the library loads, exports every declared symbol,
+validates plans and arguments, and bounds-checks every launch of real plans."""
+
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from tensorsat_gb300 import _native, planner
+from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction, NativePlan
+from tensorsat_gb300.lang.cuda_rel import CudaRel
+from tensorsat_gb300.lib.sat import CNFInstance
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "tensorsat_gb300.h"
+
+
+def declared_symbols() -> list[str]:
+    text = HEADER.read_text()
+    return re.findall(r"TSG_API\s+[\w\s\*]+?\b(tsg_\w+)\s*\(", text)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _native.lib()
+    names = declared_symbols()
+    assert len(names) >= 14
+    assert set(names) == set(_native.EXPORTED_SYMBOLS)
+    for name in names:
+        assert hasattr(lib, name), name
+    assert lib.tsg_abi_version() == 1
+
+
+def test_null_arguments_are_rejected_without_touching_the_device():
+    lib = _native.lib()
+    st = lib.tsg_contract2_or_and(None, 0, None, None, None, 0, None, None, 0, None, None, None)
+    assert st == _native.TSG_ERR_INVALID_ARGUMENT
+    assert "null" in lib.tsg_last_error().decode()
+    assert lib.tsg_union_or(None, None, None, -1, None) == _native.TSG_ERR_INVALID_ARGUMENT
+    assert lib.tsg_spider_fill(None, 2, 2, None) == _native.TSG_ERR_INVALID_ARGUMENT
+    assert lib.tsg_plan_run(None, 0, 0, None, None, 0, 1, 1, None, 0, None, 0, None) \
+        == _native.TSG_ERR_INVALID_ARGUMENT
+
+
+def _plan_for(cnf, target_bits, seed=0):
+    d = cnf.clause_diagram()
+    return GpuContraction(CudaRel, d.wiring, target_bits=target_bits, trials=2, seed=seed)
+
+
+@pytest.mark.parametrize("n,m,target", [(12, 50, 4), (20, 85, 8), (30, 128, 14), (40, 170, 20)])
+def test_every_launch_is_in_bounds(n, m, target):
+    c = _plan_for(CNFInstance.random(3, n, m, rng=1), target)
+    npl = c.native_plan()
+    ns = c.num_slices
+    for ring, primes in [(_native.TSG_RING_OR_AND, ()), (_native.TSG_RING_U64, ()),
+                         (_native.TSG_RING_MODP, PRIMES_31[:3])]:
+        for g in sorted({1, 2, min(16, ns), ns}):
+            npl.validate(ring, primes, 0, ns, g)
+        if ns >= 4:
+            npl.validate(ring, primes, 2, ns - 1, 2)
+
+
+def test_workspace_grows_with_group_and_ring():
+    c = _plan_for(CNFInstance.random(3, 30, 128, rng=0), 12)
+    npl = c.native_plan()
+    w1 = npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, 1)
+    w8 = npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, 8)
+    w8p = npl.workspace_bytes(_native.TSG_RING_MODP, 3, 8)
+    assert w1 <= w8 <= w8p
+    assert w8p >= 12 * 8 * 2 ** c.stats()["peak_bits"]
+    assert npl.launch_count(0, c.num_slices, 8) > 0
+
+
+def test_bad_ranges_and_rings_are_rejected():
+    c = _plan_for(CNFInstance.random(3, 20, 85, rng=0), 8)
+    npl = c.native_plan()
+    ns = c.num_slices
+    with pytest.raises(_native.TsgValueError):
+        npl.validate(_native.TSG_RING_OR_AND, (), 0, ns + 1, 1)
+    with pytest.raises(_native.TsgValueError):
+        npl.validate(_native.TSG_RING_OR_AND, (), 1, ns, 2)  # begin not a group multiple
+    with pytest.raises(_native.TsgValueError):
+        npl.validate(_native.TSG_RING_OR_AND, (), 0, ns, 3)  # not a power of two
+    with pytest.raises(_native.TsgValueError):
+        npl.validate(_native.TSG_RING_MODP, (4,), 0, ns, 1)  # even modulus
+    with pytest.raises(_native.TsgValueError):
+        npl.validate(7, (), 0, ns, 1)
+
+
+def _create(arrs, offsets=None):
+    lib = _native.lib()
+    ranks = arrs["leaf_ranks"]
+    if offsets is None:
+        offsets = np.cumsum([0] + [1 << int(r) for r in ranks[:-1]]).astype(np.int64)
+    h = ctypes.c_void_p()
+    lsp = np.ascontiguousarray(arrs["leaf_slice_pos"], dtype=np.int32)
+    st = lib.tsg_plan_create(
+        len(ranks), _native.ptr_i32(ranks), _native.ptr_i64(offsets), lsp.shape[1],
+        _native.ptr_i32(lsp), len(arrs["step_out_bits"]),
+        _native.ptr_i32(np.ascontiguousarray(arrs["step_operands"])),
+        _native.ptr_i32(arrs["step_out_bits"]), _native.ptr_i32(arrs["step_sum_bits"]),
+        _native.ptr_i32(arrs["step_lhs_pos"]), _native.ptr_i32(arrs["step_rhs_pos"]),
+        ctypes.byref(h))
+    if st == _native.TSG_OK:
+        lib.tsg_plan_destroy(h)
+    return st
+
+
+def test_plan_create_rejects_malformed_trees():
+    cnf = CNFInstance.random(3, 10, 30, rng=0)
+    c = _plan_for(cnf, 5)
+    good = c.sliced_plan.native_arrays()
+    assert _create(good) == _native.TSG_OK
+
+    def mutated(key, fn):
+        arrs = {k: v.copy() for k, v in good.items()}
+        fn(arrs[key])
+        return _create(arrs)
+
+    # a leaf used twice
+    assert mutated("step_operands", lambda a: a.__setitem__((1, 0), a[0, 0])) \
+        == _native.TSG_ERR_INVALID_ARGUMENT
+    # a step reading a later step
+    assert mutated("step_operands", lambda a: a.__setitem__((0, 1), -3)) \
+        == _native.TSG_ERR_INVALID_ARGUMENT
+    # an operand bit left uncovered
+    def drop_bit(a):
+        s = int(np.argmax((a >= 0).sum(axis=1)))
+        j = int(np.argmax(a[s] >= 0))
+        a[s, j] = -1
+    assert mutated("step_lhs_pos", drop_bit) == _native.TSG_ERR_INVALID_ARGUMENT
+    # a bit position outside the operand
+    assert mutated("step_rhs_pos", lambda a: a.__setitem__((0, 0), 61)) \
+        == _native.TSG_ERR_INVALID_ARGUMENT
+    # more index bits than the kernels address
+    assert mutated("step_out_bits", lambda a: a.__setitem__(0, 70)) \
+        == _native.TSG_ERR_INVALID_ARGUMENT
+
+
+def test_native_plan_leaf_pool_layout():
+    c = _plan_for(CNFInstance.random(3, 16, 60, rng=2), 6)
+    npl = NativePlan(c.sliced_plan)
+    offs = npl.leaf_offsets
+    assert all(o % 16 == 0 for o in offs)
+    assert all(offs[i] + npl.leaf_sizes[i] <= offs[i + 1] for i in range(len(offs) - 1))
+    assert npl.pool_bytes >= offs[-1] + npl.leaf_sizes[-1]
+
+
+def test_planner_native_arrays_shapes():
+    cnf = CNFInstance.random(3, 14, 56, rng=4)
+    d = cnf.clause_diagram()
+    net = planner.Network([tuple(ws) for ws in d.wiring.slot_wires_list],
+                          {w: 2 for w in range(14)}, ())
+    tree, sl = planner.optimize(net, target_bits=5, trials=2)
+    sp = planner.SlicedPlan(tree, tuple(sorted(sl)), list(net.leaf_wires))
+    arrs = sp.native_arrays()
+    assert arrs["step_lhs_pos"].shape == (len(tree.steps), planner.TSG_MAX_BITS)
+    assert arrs["leaf_slice_pos"].shape == (len(net.leaf_wires), len(sl))

@@ -1,0 +1,102 @@
+"""Planner checks on the CPU: trees are well formed, slicing meets its target, and the
+integer arrays handed to the native executor compute exact counts (numpy emulation of the
+executor's index semantics against brute force)."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import finrel_oracle as orc
+from plan_emulator import emulate_all
+from tensorsat_gb300 import planner
+from tensorsat_gb300.contractions.gpu import GpuContraction, _prepare
+from tensorsat_gb300.lang.cuda_rel import CudaRel
+from tensorsat_gb300.lib.sat import CNFInstance
+
+
+def _leaves(diagram, contraction):
+    lw = contraction._leaves
+    arrays = []
+    for slot, syn in zip(lw.slot_of_leaf, lw.synthetic):
+        arrays.append(syn if syn is not None else diagram.blocks[slot].numpy())
+    return arrays
+
+
+def _check_tree(tree, net):
+    L = tree.num_leaves
+    live = set(range(L))
+    out = set(net.out_wires)
+    for s, (a, b) in enumerate(tree.steps):
+        assert a in live and b in live
+        live -= {a, b}
+        res = tree.node_wires[L + s]
+        assert res <= tree.node_wires[a] | tree.node_wires[b]
+        live.add(L + s)
+    assert live == {tree.root}
+    assert tree.node_wires[tree.root] == out
+
+
+@pytest.mark.parametrize("n,m,seed", [(12, 50, 0), (16, 68, 1), (20, 85, 2)])
+def test_trees_well_formed_and_sliced_to_target(n, m, seed):
+    cnf = CNFInstance.random(3, n, m, rng=seed)
+    for d in ((cnf.inputs(None) >> cnf.diagram()).flatten(), cnf.clause_diagram()):
+        net = planner.Network([tuple(ws) for ws in d.wiring.slot_wires_list],
+                              {w: 2 for w in range(d.wiring.num_wires)}, ())
+        tree, sl = planner.optimize(net, target_bits=6, trials=2, seed=seed)
+        _check_tree(tree, net)
+        assert tree.cost(sl)[1] <= 6
+        replay = list(range(tree.num_leaves))
+        for s, (i, j) in enumerate(tree.linear_path()):
+            a, b = replay[i], replay[j]
+            assert (a, b) == tree.steps[s]
+            for x in sorted((i, j), reverse=True):
+                replay.pop(x)
+            replay.append(tree.num_leaves + s)
+
+
+@pytest.mark.parametrize("n,m,seed,target", [(10, 42, 0, None), (12, 50, 1, 4), (14, 60, 2, 6),
+                                             (12, 40, 3, 3)])
+def test_emulated_native_plan_counts(n, m, seed, target):
+    cnf = CNFInstance.random(3, n, m, rng=seed)
+    exp = orc.brute_force_count(n, cnf.clauses)
+    for d in ((cnf.inputs(None) >> cnf.diagram()).flatten(), cnf.clause_diagram()):
+        c = GpuContraction(CudaRel, d.wiring, target_bits=target, trials=1, seed=seed)
+        arrs = c.sliced_plan.native_arrays()
+        leaves = _leaves(d, c)
+        total = emulate_all(arrs, leaves, "count")
+        assert int(total[0]) * c.discard_factor == exp
+        sat = emulate_all(arrs, leaves, "or_and")
+        assert int(sat[0]) == int(exp > 0)
+
+
+def test_emulated_open_outputs_match_oracle():
+    cnf = CNFInstance.random(3, 8, 20, rng=4)
+    d = cnf.diagram()  # variables are open inputs
+    c = GpuContraction(CudaRel, d.wiring, target_bits=3, trials=1)
+    arrs = c.sliced_plan.native_arrays()
+    got = emulate_all(arrs, _leaves(d, c), "or_and").reshape((2,) * 8)
+    exp = np.zeros((2,) * 8, dtype=np.uint8)
+    for idx in np.ndindex(*exp.shape):
+        exp[idx] = all(any((idx[abs(l) - 1] == 1) == (l > 0) for l in cl) for cl in cnf.clauses)
+    np.testing.assert_array_equal(got, exp)
+
+
+def test_prepare_handles_dangling_and_repeated_wires():
+    from tensorsat_gb300.diagrams import Wiring
+    from tensorsat_gb300.lib.bincirc import bit
+
+    w = Wiring(wire_types=(bit,) * 4, slot_wires_list=[(0, 0, 1)], out_wires=(1, 2))
+    lw = _prepare(w)
+    assert lw.leaf_wires[0] == (0, 1)
+    assert 0 in lw.diag_slots
+    assert (2,) in lw.leaf_wires  # dangling out wire -> all-ones leaf
+    assert lw.discard_factor == 2  # wire 3 is connected to nothing
+    assert lw.out_unique == (1, 2)
+
+
+def test_slicing_never_touches_output_wires():
+    cnf = CNFInstance.random(3, 12, 40, rng=0)
+    d = cnf.clause_diagram("_" * 4 + "?" * 8)
+    c = GpuContraction(CudaRel, d.wiring, target_bits=5, trials=1)
+    assert not set(c.sliced_wires) & set(d.wiring.out_wires)
