@@ -1,0 +1,372 @@
+"""Benchmark: exact model count + SAT bit of uniform random 3-SAT, n=60, m=256, on GB300.
+
+Workload (the single-instance #SAT configuration): ``CNFInstance.random(3, 60, 256,
+rng=SEED)`` compiled to its clause network (one 2x2x2 {0,1} tensor per clause), one
+contraction tree from the project's planner with every intermediate capped at 2^26 entries
+by slicing. The exact count is carried modulo three 31-bit primes (uint32 residue planes,
+CRT on the host); the SAT bit is the OR-AND contraction of the same tree.
+
+A *step* contracts one group of G slices of that instance in both rings (count and SAT
+bit). Every slice of an instance runs the same kernels on the same shapes, so
+``instances/s = slices/s / slices per instance`` is exact for this instance. Inputs
+(leaves) are resident in HBM for ``value``; ``e2e`` goes through the public API
+(``GpuContraction.count`` / ``.contract``) from host leaves to host results each step.
+
+``--impl reference`` times the reference's CPU path for the same workload (the oracle's
+restatement of the upstream numpy contraction: per-slice einsum in the OR-AND semiring and
+over exact integers), one slice per process on all host cores.
+
+Prints one JSON line (rank 0).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "exact instances/s (SAT bit + model count), uniform random 3-SAT n=60 m=256"
+UNIT = "instances/s"
+N_VARS, N_CLAUSES = 60, 256
+TARGET_BITS = 26
+NUM_PRIMES = 3
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--group", type=int, default=0, help="slices per step (0 = auto)")
+    p.add_argument("--trials", type=int, default=8)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    try:
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int) -> None:
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=5)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(seed: int, trials: int):
+    from tensorsat_gb300.contractions.gpu import GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    cnf = CNFInstance.random(3, N_VARS, N_CLAUSES, rng=seed)
+    diagram = cnf.clause_diagram()
+    contraction = GpuContraction(CudaRel, diagram.wiring, target_bits=TARGET_BITS,
+                                 trials=trials, seed=0)
+    return cnf, diagram, contraction
+
+
+# --------------------------------------------------------------------------------------
+# CPU leg (oracle port of the reference's numpy path), one slice per process
+
+
+def _cpu_slice(args):
+    clauses, steps, sliced, sid = args
+    from oracle import finrel_oracle as orc
+
+    fixed = {w: (sid >> j) & 1 for j, w in enumerate(sliced)}
+    count = orc.cnf_count_by_tree(N_VARS, clauses, steps, "count", fixed=fixed)
+    sat = orc.cnf_count_by_tree(N_VARS, clauses, steps, "or_and", fixed=fixed)
+    return count, sat
+
+
+def cpu_pool(cores: int):
+    import multiprocessing as mp
+
+    return mp.get_context("spawn").Pool(cores)
+
+
+def cpu_sample(pool, cores: int, cnf, contraction, first_slice: int):
+    steps = list(contraction.tree.steps)
+    sliced = list(contraction.sliced_wires)
+    ns = contraction.num_slices
+    jobs = [(cnf.clauses, steps, sliced, (first_slice + i) % ns) for i in range(cores)]
+    t0 = time.perf_counter()
+    results = pool.map(_cpu_slice, jobs)
+    dt = time.perf_counter() - t0
+    return dt, results
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    pool = cpu_pool(cores)
+    cnf, _, contraction = build_workload(args.seed, args.trials)
+    ns = contraction.num_slices
+    for w in range(args.warmup):
+        cpu_sample(pool, cores, cnf, contraction, w * cores)
+    times = []
+    for k in range(args.steps):
+        dt, _ = cpu_sample(pool, cores, cnf, contraction, (args.warmup + k) * cores)
+        times.append(dt)
+    pool.close()
+    total = sum(times)
+    value = args.steps * cores / ns / total
+    sample = (f"{cores} slices of {ns} per step (one per process), count over exact "
+              f"integers + OR-AND bit per slice")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "uint64/uint8 (numpy einsum)",
+        "data": "synthetic (seeded CNFInstance.random)",
+        "config": workload_config(args, contraction, group=cores),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, contraction, group: int) -> dict:
+    st = contraction.stats()
+    return {
+        "workload": f"3-SAT n={N_VARS} m={N_CLAUSES} rng={args.seed}, clause network, "
+                    f"peak 2^{TARGET_BITS} entries",
+        "k": 3, "n": N_VARS, "m": N_CLAUSES, "seed": args.seed,
+        "slices_per_instance": contraction.num_slices,
+        "sliced_wires": st["num_sliced"],
+        "log2_index_space_per_slice": round(st["log2_index_space_per_slice"], 3),
+        "slices_per_step": group,
+        "count_ring": f"mod {NUM_PRIMES} primes < 2^31 (CRT)",
+        "l2": "inputs larger than L2 (intermediates up to 2^26 entries x slices)",
+    }
+
+
+# --------------------------------------------------------------------------------------
+# GPU leg
+
+
+def run_gb300(args) -> None:
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    cores = os.cpu_count() or 1
+    want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
+    pool = cpu_pool(cores) if want_cpu else None  # spawn before the first CUDA call
+
+    from tensorsat_gb300 import _native
+    from tensorsat_gb300.contractions.gpu import PRIMES_31
+
+    lib = _native.lib()
+    cnf, diagram, contraction = build_workload(args.seed, args.trials)
+    npl = contraction.native_plan()
+    primes = PRIMES_31[:NUM_PRIMES]
+    ns = contraction.num_slices
+    dev = torch.device("cuda", local)
+    if args.group:
+        group = args.group
+    else:
+        free, _ = torch.cuda.mem_get_info()
+        budget = int(free * 0.75)
+        group = min(ns, 256)
+        while group > 1 and (npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, group)
+                             + npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, group)) > budget:
+            group //= 2
+    ws_count = torch.empty(npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, group),
+                           dtype=torch.uint8, device=dev)
+    ws_sat = torch.empty(npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, group),
+                         dtype=torch.uint8, device=dev)
+    pool_dev = contraction.leaf_pool(diagram)
+    res_count = torch.zeros(NUM_PRIMES, dtype=torch.int32, device=dev)
+    res_sat = torch.zeros(1, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = int(stream.cuda_stream)
+    groups_per_instance = ns // group
+
+    def slice_range(i: int) -> tuple[int, int]:
+        g = (rank * (args.warmup + args.steps) + i) % groups_per_instance
+        return g * group, (g + 1) * group
+
+    def step(i: int) -> None:
+        b, e = slice_range(i)
+        npl.run(_native.TSG_RING_MODP, primes, pool_dev, b, e, group, ws_count, res_count,
+                False, sh)
+        npl.run(_native.TSG_RING_OR_AND, (), pool_dev, b, e, group, ws_sat, res_sat, False, sh)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        ev[0].record(stream)
+        for k in range(args.steps):
+            step(args.warmup + k)
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    elapsed = sum(step_ms) / 1000.0
+    if dist:
+        t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = world * args.steps * group / ns / elapsed
+    launches_per_step = (npl.launch_count(*slice_range(0), group) * 2)
+
+    # roofline: algorithmic bytes of the step kernels / step time
+    sp = contraction.sliced_plan
+    bytes_count = sp.bytes_per_slice(4, NUM_PRIMES) * group
+    bytes_sat = sp.bytes_per_slice(1, 1) * group
+    step_s = elapsed / args.steps
+    peak, peak_kind = measured_peaks()
+    achieved = (bytes_count + bytes_sat) / step_s / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic_n60.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get("dram_bytes_per_step_scaled")
+        except Exception:
+            traffic = None
+
+    # end to end through the public API: host leaves in, host results out, every step
+    e2e_times = []
+    h2d = 2 * npl.pool_bytes
+    d2h = 4 * NUM_PRIMES + 1
+    for k in range(args.e2e_steps + 1):
+        b, e = slice_range(args.warmup + args.steps + k)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES, group=group,
+                          slice_range=(b, e), cache_leaves=False)
+        bool(contraction.contract(diagram, group=group, slice_range=(b, e), cache_leaves=False))
+        torch.cuda.synchronize()
+        if k > 0:  # the first call allocates workspaces in torch's caching allocator
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_value = world * group / ns / statistics.mean(e2e_times)
+
+    cpu = None
+    if want_cpu:
+        dt, _ = cpu_sample(pool, cores, cnf, contraction, 0)
+        pool.close()
+        cpu = {"value": cores / ns / dt, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{cores} slices of {ns} (one per process, exact-integer count + "
+                         f"OR-AND bit per slice, numpy einsum), {dt:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * step_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 residues mod 3 primes + u8 OR-AND",
+            "data": "synthetic (seeded CNFInstance.random, no dataset)",
+            "config": workload_config(args, contraction, group),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "kernel": "tree_step_kernel (all steps of a slice group)"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks.summary(),
+            "step_ms": [round(x, 3) for x in step_ms],
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

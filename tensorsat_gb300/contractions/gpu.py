@@ -296,10 +296,11 @@ class GpuContraction(Contraction):
 
     # -- leaves -----------------------------------------------------------------------
 
-    def leaf_pool(self, diagram: Diagram) -> torch.Tensor:
-        """The diagram's leaf tensors packed into one device uint8 buffer (cached for the
-        last diagram)."""
-        if self._pool_cache is not None and self._pool_cache[0] == id(diagram):
+    def leaf_pool(self, diagram: Diagram, cache: bool = True) -> torch.Tensor:
+        """The diagram's leaf tensors packed into one device uint8 buffer (one host-to-
+        device copy for host leaves; cached for the last diagram unless ``cache`` is
+        False)."""
+        if cache and self._pool_cache is not None and self._pool_cache[0] == id(diagram):
             return self._pool_cache[1]
         dev = _device.require_cuda()
         npl = self.native_plan()
@@ -338,7 +339,8 @@ class GpuContraction(Contraction):
                 _native.check(st)
             else:
                 pool[off: off + t.numel()].copy_(t.reshape(-1))
-        self._pool_cache = (id(diagram), pool)
+        if cache:
+            self._pool_cache = (id(diagram), pool)
         return pool
 
     # -- execution --------------------------------------------------------------------
@@ -361,7 +363,8 @@ class GpuContraction(Contraction):
     def run(self, diagram: Diagram | None, ring: int, primes: Sequence[int] = (),
             slice_range: tuple[int, int] | None = None, group: int | None = None,
             pool: torch.Tensor | None = None, workspace: torch.Tensor | None = None,
-            result: torch.Tensor | None = None, accumulate: bool = False) -> torch.Tensor:
+            result: torch.Tensor | None = None, accumulate: bool = False,
+            cache_leaves: bool = True) -> torch.Tensor:
         """Runs the tree executor over a slice range and returns the device result
         (uint8 / uint64 / uint32[planes] over the root's 2^bits entries)."""
         dev = _device.require_cuda()
@@ -370,7 +373,7 @@ class GpuContraction(Contraction):
             if diagram is None:
                 raise ValueError("run() needs a diagram or a leaf pool")
             self.validate(diagram)
-            pool = self.leaf_pool(diagram)
+            pool = self.leaf_pool(diagram, cache=cache_leaves)
         planes = len(primes) if ring == _native.TSG_RING_MODP else 1
         b, e = slice_range if slice_range is not None else (0, self.num_slices)
         if group is None:
@@ -391,11 +394,18 @@ class GpuContraction(Contraction):
         return result
 
     def contract(self, diagram: Diagram, *, progbar: bool = False, order: Any = None,
-                 autojit: Any = "auto", group: int | None = None) -> CudaRel:
+                 autojit: Any = "auto", group: int | None = None,
+                 slice_range: tuple[int, int] | None = None,
+                 cache_leaves: bool = True) -> CudaRel:
         """Validates and contracts the diagram in the OR-AND semiring; returns the result
-        box (a scalar box for a SAT network: ``bool(box)`` is the SAT bit)."""
+        box (a scalar box for a SAT network: ``bool(box)`` is the SAT bit).
+
+        ``slice_range`` restricts the run to slices ``[begin, end)`` (the OR of those
+        slices only); ``progbar``, ``order`` and ``autojit`` are accepted for signature
+        parity with ``CotengraContraction.contract`` and have no effect."""
         self.validate(diagram)
-        res = self.run(diagram, _native.TSG_RING_OR_AND, group=group)
+        res = self.run(diagram, _native.TSG_RING_OR_AND, group=group, slice_range=slice_range,
+                       cache_leaves=cache_leaves)
         lw = self._leaves
         k = len(lw.out_unique)
         box = CudaRel._new(res.reshape((2,) * k))
@@ -404,13 +414,16 @@ class GpuContraction(Contraction):
         return box
 
     def count(self, diagram: Diagram, *, ring: str = "auto", num_primes: int | None = None,
-              group: int | None = None) -> Any:
+              group: int | None = None, slice_range: tuple[int, int] | None = None,
+              cache_leaves: bool = True) -> Any:
         """Exact model count (``int``) of a closed network, or a numpy object array of
         counts indexed by the out wires.
 
         ``ring="u64"`` counts modulo 2^64, ``"modp"`` modulo ``num_primes`` 31-bit primes
         with CRT, ``"auto"`` picks u64 when the count bound is below 2^64 and otherwise
-        enough primes for the bound.
+        enough primes for the bound. ``slice_range`` restricts the run to slices
+        ``[begin, end)``: the result is then that range's share of the count (shares of
+        disjoint ranges add up to the count).
         """
         self.validate(diagram)
         arrays = []
@@ -425,7 +438,8 @@ class GpuContraction(Contraction):
         if ring == "u64":
             if bound >= 64:
                 raise OverflowError("count bound exceeds 2^64: use ring='modp'")
-            res = self.run(diagram, _native.TSG_RING_U64, group=group)
+            res = self.run(diagram, _native.TSG_RING_U64, group=group, slice_range=slice_range,
+                           cache_leaves=cache_leaves)
             vals = res.cpu().numpy().view(np.uint64)
             counts = np.array([int(v) for v in vals], dtype=object)
         elif ring == "modp":
@@ -436,7 +450,8 @@ class GpuContraction(Contraction):
                 raise OverflowError(
                     f"count bound 2^{bound:.0f} needs more than {num_primes} 31-bit primes"
                 )
-            res = self.run(diagram, _native.TSG_RING_MODP, primes=primes, group=group)
+            res = self.run(diagram, _native.TSG_RING_MODP, primes=primes, group=group,
+                           slice_range=slice_range, cache_leaves=cache_leaves)
             planes = res.cpu().numpy().view(np.uint32).reshape(num_primes, -1)
             counts = crt([planes[p] for p in range(num_primes)], primes)
         else:

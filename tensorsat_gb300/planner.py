@@ -453,6 +453,6 @@ class SlicedPlan:
                 if x < L:
                     tot += 2.0 ** len(t.node_wires[x] - sl)
                 else:
-                    tot += 2.0 ** len(t.node_wires[x]) * elem_bytes * planes
-            tot += 2.0 ** len(t.node_wires[L + s]) * elem_bytes * planes
+                    tot += 2.0 ** len(t.node_wires[x] - sl) * elem_bytes * planes
+            tot += 2.0 ** len(t.node_wires[L + s] - sl) * elem_bytes * planes
         return tot
