@@ -103,6 +103,22 @@ def contract2_or_and(lhs: np.ndarray, lhs_wires: Sequence[int], rhs: np.ndarray,
     return np.sign(res, dtype=np.uint8)
 
 
+def contract2_einsum_definition(lhs: np.ndarray, lhs_wires: Sequence[int], rhs: np.ndarray,
+                                rhs_wires: Sequence[int], out_wires: Sequence[int]) -> np.ndarray:
+    """The einsum-defined result of a pairwise contraction with sign: output port i
+    carries wire out_wires[i]; ports sharing a wire form a diagonal (zero elsewhere).
+    Upstream agrees with this except when repeated output wires are interleaved with
+    others out of sorted order, where ``rewire_array`` transposes blocks or raises."""
+    uniq = list(dict.fromkeys(out_wires))
+    res = _einsum(lhs.astype(np.uint64), lhs_wires, rhs.astype(np.uint64), rhs_wires, uniq)
+    out = np.zeros([res.shape[uniq.index(w)] for w in out_wires], dtype=np.uint8)
+    for idx in np.ndindex(*out.shape):
+        val: dict[int, int] = {}
+        if all(val.setdefault(w, v) == v for w, v in zip(out_wires, idx)):
+            out[idx] = 1 if res[tuple(val[w] for w in uniq)] else 0
+    return out
+
+
 def rewire_or_and(t: np.ndarray, out_ports: Sequence[int]) -> np.ndarray:
     """FinRel._rewire: transpose when out_ports is a permutation, otherwise
     duplicate/discard ports (summing discarded ones) and take the sign."""

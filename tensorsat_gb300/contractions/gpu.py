@@ -28,8 +28,44 @@ from ..diagrams import Diagram, TensorLikeType, Wiring
 from ..lang.cuda_rel import CudaRel, leaf_array
 from .abc import Contraction
 
-PRIMES_31 = (2147483647, 2147483629, 2147483587, 2147483579)
-"""Moduli of the residue count ring: the four largest primes below 2^31."""
+def _is_prime(n: int) -> bool:
+    """Deterministic Miller-Rabin for n < 3.3e9 (bases 2, 3, 5, 7)."""
+    if n < 2:
+        return False
+    for q in (2, 3, 5, 7):
+        if n % q == 0:
+            return n == q
+    d, r = n - 1, 0
+    while d % 2 == 0:
+        d //= 2
+        r += 1
+    for a in (2, 3, 5, 7):
+        x = pow(a, d, n)
+        if x in (1, n - 1):
+            continue
+        for _ in range(r - 1):
+            x = x * x % n
+            if x == n - 1:
+                break
+        else:
+            return False
+    return True
+
+
+def _primes_below(limit: int, count: int) -> tuple[int, ...]:
+    out = []
+    n = limit - 1
+    while len(out) < count:
+        if _is_prime(n):
+            out.append(n)
+        n -= 2 if n % 2 else 1
+    return tuple(out)
+
+
+PRIMES_31 = _primes_below(2**31, 64)
+"""Moduli of the residue count ring: the largest primes below 2^31, in decreasing order
+(2147483647, 2147483629, 2147483587, ...). A run carries at most 4 of them; counts that
+need more run several passes."""
 
 DEFAULT_TARGET_BITS = 26
 
@@ -77,28 +113,48 @@ def _prepare(wiring: Wiring) -> _Leaves:
                    tuple(dict.fromkeys(wiring.out_wires)), dims)
 
 
-def _functional_wire(t: np.ndarray) -> int | None:
-    """A port whose value is a function of the other ports (exactly one 1 per assignment
-    of the others), if any."""
+def _functional_ports(t: np.ndarray) -> list[int]:
+    """Ports whose value is a function of the other ports (exactly one 1 per assignment of
+    the others), last port first (gates put their output last)."""
     if t.ndim == 0 or t.size > 1 << 12:
-        return None
-    for p in range(t.ndim):
-        if np.all(t.sum(axis=p) == 1):
-            return p
-    return None
+        return []
+    return [p for p in reversed(range(t.ndim)) if np.all(t.sum(axis=p) == 1)]
 
 
 def count_bound_bits(wiring: Wiring, arrays: Sequence[np.ndarray]) -> float:
-    """log2 of an upper bound on every entry of the count tensor of a 0/1 network: a
-    wire whose value is a function of the others at one tensor (a gate output, a
-    constant) adds nothing, every other summed wire adds log2(dim)."""
-    determined: set[int] = set()
+    """log2 of an upper bound on every entry of the count tensor of a 0/1 network.
+
+    A wire that one tensor determines from its other wires (a gate output, a constant)
+    adds nothing, provided the determinations are acyclic: then every assignment of the
+    remaining summed wires extends in at most one way. Every other summed wire adds
+    log2(dim). Wires are oriented greedily (a gate's last port first) and the orientation
+    is dropped altogether if it is cyclic."""
+    determined: dict[int, tuple[int, ...]] = {}
     for ws, arr in zip(wiring.slot_wires_list, arrays):
         if len(set(ws)) != len(ws):
             continue
-        p = _functional_wire(arr)
-        if p is not None and ws[p] not in determined:
-            determined.add(ws[p])
+        for p in _functional_ports(np.asarray(arr)):
+            if ws[p] not in determined:
+                determined[ws[p]] = tuple(w for w in ws if w != ws[p])
+                break
+    # acyclicity: Kahn's algorithm over "determined wire <- its tensor's other wires"
+    indeg = {w: sum(1 for u in deps if u in determined) for w, deps in determined.items()}
+    users: dict[int, list[int]] = {}
+    for w, deps in determined.items():
+        for u in deps:
+            if u in determined:
+                users.setdefault(u, []).append(w)
+    queue = [w for w, d in indeg.items() if d == 0]
+    seen = 0
+    while queue:
+        u = queue.pop()
+        seen += 1
+        for w in users.get(u, ()):
+            indeg[w] -= 1
+            if indeg[w] == 0:
+                queue.append(w)
+    if seen != len(determined):
+        determined = {}
     out = set(wiring.out_wires)
     bits = 0.0
     for w, t in enumerate(wiring.wire_types):
@@ -444,16 +500,24 @@ class GpuContraction(Contraction):
             counts = np.array([int(v) for v in vals], dtype=object)
         elif ring == "modp":
             if num_primes is None:
-                num_primes = max(1, min(4, math.ceil((bound + 1) / 30.9)))
+                num_primes = 1
+                while sum(math.log2(p) for p in PRIMES_31[:num_primes]) <= bound:
+                    num_primes += 1
+            if num_primes > len(PRIMES_31):
+                raise OverflowError(f"count bound 2^{bound:.0f} exceeds the residue range")
             primes = PRIMES_31[:num_primes]
             if sum(math.log2(p) for p in primes) <= bound:
                 raise OverflowError(
                     f"count bound 2^{bound:.0f} needs more than {num_primes} 31-bit primes"
                 )
-            res = self.run(diagram, _native.TSG_RING_MODP, primes=primes, group=group,
-                           slice_range=slice_range, cache_leaves=cache_leaves)
-            planes = res.cpu().numpy().view(np.uint32).reshape(num_primes, -1)
-            counts = crt([planes[p] for p in range(num_primes)], primes)
+            residues = []
+            for i in range(0, num_primes, _native.TSG_MAX_PRIMES):
+                chunk = primes[i: i + _native.TSG_MAX_PRIMES]
+                res = self.run(diagram, _native.TSG_RING_MODP, primes=chunk, group=group,
+                               slice_range=slice_range, cache_leaves=cache_leaves)
+                planes = res.cpu().numpy().view(np.uint32).reshape(len(chunk), -1)
+                residues.extend(planes[p] for p in range(len(chunk)))
+            counts = crt(residues, primes)
         else:
             raise ValueError(f"unknown count ring {ring!r}")
         lw = self._leaves

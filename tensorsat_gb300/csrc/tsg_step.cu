@@ -55,6 +55,7 @@ struct GenericArgs {
   int32_t n_wires;        // distinct wires on output ports
   int32_t rhs_is_one;     // rhs is the scalar 1 (used by rewire)
   int64_t total;          // output entries
+  int64_t ksize;          // size of the summed index space
   int64_t out_dim[TSG_MAX_PORTS];
   int32_t out_wire[TSG_MAX_PORTS];   // distinct-wire id of each output port
   int64_t wire_ls[kMaxWires];        // lhs stride of each distinct output wire
@@ -116,6 +117,67 @@ __global__ void generic_contract_kernel(const T* __restrict__ lhs, const T* __re
       if (kOrAnd) acc = acc ? (T)1 : (T)0;
     }
     out[t] = acc;
+  }
+}
+
+// Split-K form for few outputs over a large summed space: one block per output entry,
+// threads stride over the summed index (decoded per thread), then a block reduction.
+template <typename T, bool kOrAnd>
+__global__ void generic_contract_splitk_kernel(const T* __restrict__ lhs,
+                                               const T* __restrict__ rhs, T* __restrict__ out,
+                                               GenericArgs a, int64_t ksize) {
+  __shared__ T red[128];
+  for (int64_t t = blockIdx.x; t < a.total; t += gridDim.x) {
+    int64_t coord[kMaxWires];
+    for (int w = 0; w < a.n_wires; ++w) coord[w] = -1;
+    int64_t rem = t, lo = 0, ro = 0;
+    bool on_diagonal = true;
+    for (int p = a.n_out - 1; p >= 0; --p) {
+      const int64_t d = a.out_dim[p];
+      const int64_t c = rem % d;
+      rem /= d;
+      const int w = a.out_wire[p];
+      if (coord[w] < 0) {
+        coord[w] = c;
+        lo += c * a.wire_ls[w];
+        ro += c * a.wire_rs[w];
+      } else if (coord[w] != c) {
+        on_diagonal = false;
+      }
+    }
+    T acc = 0;
+    if (on_diagonal) {
+      for (int64_t kk = threadIdx.x; kk < ksize; kk += blockDim.x) {
+        int64_t r2 = kk, klo = 0, kro = 0;
+        for (int i = a.n_sum - 1; i >= 0; --i) {
+          const int64_t c = r2 % a.sum_dim[i];
+          r2 /= a.sum_dim[i];
+          klo += c * a.sum_ls[i];
+          kro += c * a.sum_rs[i];
+        }
+        const T l = lhs[lo + klo];
+        const T r = a.rhs_is_one ? (T)1 : rhs[ro + kro];
+        if (kOrAnd) {
+          acc |= (T)(l & r);
+        } else {
+          acc += l * r;
+        }
+      }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) {
+        if (kOrAnd) {
+          red[threadIdx.x] |= red[threadIdx.x + s];
+        } else {
+          red[threadIdx.x] += red[threadIdx.x + s];
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[t] = kOrAnd ? (red[0] ? (T)1 : (T)0) : red[0];
+    __syncthreads();
   }
 }
 
@@ -208,6 +270,7 @@ tsg_status build_generic(int32_t lhs_rank, const int64_t* lhs_wires, const int64
     ++ns;
   }
   a->n_sum = ns;
+  a->ksize = ksize;
   return TSG_OK;
 }
 
@@ -216,8 +279,15 @@ tsg_status launch_generic(const T* lhs, const T* rhs, T* out, const GenericArgs&
                           cudaStream_t stream) {
   if (a.total == 0) return TSG_OK;
   const unsigned threads = 128;
-  generic_contract_kernel<T, kOrAnd>
-      <<<grid_for((uint64_t)a.total, threads, 8), threads, 0, stream>>>(lhs, rhs, out, a);
+  if (a.ksize > 256 && a.total < 4096) {
+    // few outputs over a large summed space: spread each output's sum over a block
+    const unsigned blocks = (unsigned)std::min<int64_t>(a.total, (int64_t)device_sm_count() * 8);
+    generic_contract_splitk_kernel<T, kOrAnd>
+        <<<blocks, threads, 0, stream>>>(lhs, rhs, out, a, a.ksize);
+  } else {
+    generic_contract_kernel<T, kOrAnd>
+        <<<grid_for((uint64_t)a.total, threads, 8), threads, 0, stream>>>(lhs, rhs, out, a);
+  }
   TSG_CUDA_TRY(cudaGetLastError());
   return TSG_OK;
 }

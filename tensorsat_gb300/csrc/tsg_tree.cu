@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <map>
 #include <vector>
 
@@ -119,6 +120,172 @@ __global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArg
 #pragma unroll
       for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
         if (p < ring.np) out[t + p * a.o_plane] = barrett_reduce(acc[p], ring.p[p], ring.m[p]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Narrow step kernel: the common case where a slice's tensors have < 2^32 entries.
+// The slice slot g is blockIdx.y, so each block resolves the 64-bit slice offsets once and
+// threads work in 32-bit offsets. Each thread produces `v` (1, 2 or 4) consecutive outputs:
+// their operand offsets differ by the precomputed `tab` entries, which lets an operand whose
+// fastest output bits are its own fastest bits be read with one vector load (mode kContig)
+// and an operand that does not carry those bits be read once (mode kBcast).
+
+constexpr int kMaxNarrowRuns = 32;
+constexpr int kModeGather = 0;
+constexpr int kModeContig = 1;
+constexpr int kModeBcast = 2;
+
+struct NarrowMap {
+  int32_t n;
+  uint8_t src[kMaxNarrowRuns];
+  uint8_t len[kMaxNarrowRuns];
+  uint8_t dst[kMaxNarrowRuns];
+};
+
+struct StepArgs2 {
+  const uint8_t* lhs;
+  const uint8_t* rhs;
+  uint8_t* out;
+  uint64_t l_base, r_base;             // constant element offsets
+  uint64_t l_plane, r_plane, o_plane;  // residue-plane strides (elements)
+  uint32_t n_out;                      // outputs per slice (2^out_bits)
+  int32_t k_bits;
+  int32_t v;                           // outputs per thread (1, 2, 4), divides n_out
+  int32_t l_mode, r_mode;
+  uint32_t l_tab[4], r_tab[4];         // offsets of outputs j < v relative to output 0
+  NarrowMap lo, ro, lk, rk;            // output-bit and summed-bit runs
+  BitMap lg, rg;                       // slice-slot bits (64-bit destinations)
+};
+
+__device__ __forceinline__ uint32_t scatter32(const NarrowMap& m, uint32_t x) {
+  uint32_t r = 0;
+#pragma unroll 1
+  for (int i = 0; i < m.n; ++i) r |= ((x >> m.src[i]) & ((1u << m.len[i]) - 1u)) << m.dst[i];
+  return r;
+}
+
+// Loads v values of one operand (plane p) starting at element offset `off`.
+template <typename T, bool kLeaf>
+__device__ __forceinline__ void load_v(const uint8_t* base, uint64_t off, int mode, int v,
+                                       const uint32_t* tab, uint64_t out[4]) {
+  if (mode == kModeBcast) {
+    const uint64_t x = kLeaf ? (uint64_t)base[off] : (uint64_t)reinterpret_cast<const T*>(base)[off];
+    out[0] = out[1] = out[2] = out[3] = x;
+    return;
+  }
+  if (mode == kModeContig) {  // v == 4, off is a multiple of 4 (checked on the host)
+    if constexpr (kLeaf || sizeof(T) == 1) {
+      const uint32_t w = *reinterpret_cast<const uint32_t*>(base + off);
+      out[0] = w & 0xff;
+      out[1] = (w >> 8) & 0xff;
+      out[2] = (w >> 16) & 0xff;
+      out[3] = w >> 24;
+    } else if constexpr (sizeof(T) == 4) {
+      const uint4 w = *reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(base) + off);
+      out[0] = w.x;
+      out[1] = w.y;
+      out[2] = w.z;
+      out[3] = w.w;
+    } else {
+      const ulonglong2* p = reinterpret_cast<const ulonglong2*>(reinterpret_cast<const T*>(base) + off);
+      const ulonglong2 w0 = p[0], w1 = p[1];
+      out[0] = w0.x;
+      out[1] = w0.y;
+      out[2] = w1.x;
+      out[3] = w1.y;
+    }
+    return;
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (j < v) {
+      out[j] = kLeaf ? (uint64_t)base[off + tab[j]]
+                     : (uint64_t)reinterpret_cast<const T*>(base)[off + tab[j]];
+    }
+  }
+}
+
+template <int kRing, bool kLLeaf, bool kRLeaf>
+__global__ void __launch_bounds__(kThreads) tree_step_narrow_kernel(StepArgs2 a, RingArgs ring) {
+  using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
+            typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
+  constexpr int kPlanes = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
+  const uint32_t g = blockIdx.y;
+  const uint64_t lg = a.l_base + scatter_bits(a.lg, g);
+  const uint64_t rg = a.r_base + scatter_bits(a.rg, g);
+  const uint64_t og = (uint64_t)g * a.n_out;
+  const uint32_t nk = 1u << a.k_bits;
+  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
+  const int v = a.v;
+  const uint32_t step = gridDim.x * blockDim.x * (uint32_t)v;
+  for (uint32_t o0 = (blockIdx.x * blockDim.x + threadIdx.x) * (uint32_t)v; o0 < a.n_out;
+       o0 += step) {
+    const uint64_t lo = lg + scatter32(a.lo, o0);
+    const uint64_t ro = rg + scatter32(a.ro, o0);
+    uint64_t acc[kPlanes][4];
+#pragma unroll
+    for (int p = 0; p < kPlanes; ++p)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[p][j] = 0;
+    for (uint32_t kk = 0; kk < nk; ++kk) {
+      const uint64_t lko = lo + scatter32(a.lk, kk);
+      const uint64_t rko = ro + scatter32(a.rk, kk);
+#pragma unroll
+      for (int p = 0; p < kPlanes; ++p) {
+        if (p >= np) break;
+        uint64_t lv[4], rv[4];
+        load_v<T, kLLeaf>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane), a.l_mode, v, a.l_tab, lv);
+        load_v<T, kRLeaf>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane), a.r_mode, v, a.r_tab, rv);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if constexpr (kRing == TSG_RING_OR_AND) {
+            acc[p][j] |= lv[j] & rv[j];
+          } else {
+            acc[p][j] += lv[j] * rv[j];
+          }
+        }
+        if constexpr (kRing == TSG_RING_MODP) {
+          // residues < 2^31: three products plus a reduced value stay below 2^64
+          if (kk % 3 == 2) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[p][j] = barrett_reduce(acc[p][j], ring.p[p], ring.m[p]);
+          }
+        }
+      }
+    }
+    const uint64_t oo = og + o0;
+#pragma unroll
+    for (int p = 0; p < kPlanes; ++p) {
+      if (p >= np) break;
+      if constexpr (kRing == TSG_RING_OR_AND) {
+        if (v == 4) {
+          const uint32_t w = (acc[p][0] ? 1u : 0u) | (acc[p][1] ? 1u << 8 : 0u) |
+                             (acc[p][2] ? 1u << 16 : 0u) | (acc[p][3] ? 1u << 24 : 0u);
+          *reinterpret_cast<uint32_t*>(a.out + oo) = w;
+        } else {
+          for (int j = 0; j < v; ++j) a.out[oo + j] = acc[p][j] ? 1 : 0;
+        }
+      } else if constexpr (kRing == TSG_RING_U64) {
+        uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oo;
+        if (v == 4) {
+          reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[p][0], acc[p][1]);
+          reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[p][2], acc[p][3]);
+        } else {
+          for (int j = 0; j < v; ++j) out[j] = acc[p][j];
+        }
+      } else {
+        uint32_t r[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j] = barrett_reduce(acc[p][j], ring.p[p], ring.m[p]);
+        uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane + oo;
+        if (v == 4) {
+          *reinterpret_cast<uint4*>(out) = make_uint4(r[0], r[1], r[2], r[3]);
+        } else {
+          for (int j = 0; j < v; ++j) out[j] = r[j];
+        }
       }
     }
   }
@@ -444,85 +611,210 @@ tsg_status check_step_bounds(const RunCtx& c, int s, const StepArgs& a, const bo
   return TSG_OK;
 }
 
+// Index description of one operand of one launch: output-bit, summed-bit and slot-bit
+// pairs (source bit -> operand bit) and the constant element offset.
+struct OperandDesc {
+  std::vector<std::pair<int, int>> tp, kp, gp;
+  uint64_t base = 0;
+  const uint8_t* ptr = nullptr;
+  uint64_t plane = 0;
+  bool leaf = false;
+};
+
+OperandDesc describe_operand(const RunCtx& c, const StepInfo& st, int o, int64_t base) {
+  const tsg_plan* plan = c.plan;
+  const int gb = st.dep ? c.g_bits : 0;
+  OperandDesc d;
+  const int v = st.op[o];
+  for (int i = 0; i < st.out_bits; ++i)
+    if (st.pos[o][i] >= 0) d.tp.push_back({i, st.pos[o][i]});
+  for (int i = 0; i < st.k_bits; ++i)
+    if (st.pos[o][st.out_bits + i] >= 0) d.kp.push_back({i, st.pos[o][st.out_bits + i]});
+  if (v >= 0) {
+    const LeafInfo& lf = plan->leaves[v];
+    d.ptr = c.pool;
+    d.base = (uint64_t)lf.offset;
+    for (int j = 0; j < plan->num_sliced; ++j) {
+      if (lf.spos[j] < 0 || !st.dep) continue;
+      if (j < gb) {
+        d.gp.push_back({j, lf.spos[j]});
+      } else {
+        d.base += (uint64_t)((base >> j) & 1) << lf.spos[j];
+      }
+    }
+    d.leaf = true;
+  } else {
+    const int x = -v - 1;
+    const StepInfo& xs = plan->steps[x];
+    d.ptr = c.ws ? c.ws + c.lay->offset[x] : nullptr;
+    d.plane = (uint64_t)c.lay->plane[x];
+    if (xs.dep)
+      for (int j = 0; j < gb; ++j) d.gp.push_back({j, xs.out_bits + j});
+  }
+  return d;
+}
+
+tsg_status make_narrow(std::vector<std::pair<int, int>> pairs, NarrowMap* m, bool* ok) {
+  std::sort(pairs.begin(), pairs.end());
+  std::memset(m, 0, sizeof(*m));
+  for (const auto& pr : pairs) {
+    if (pr.second >= 32 || pr.first >= 32) {
+      *ok = false;
+      return TSG_OK;
+    }
+    if (m->n > 0) {
+      const int i = m->n - 1;
+      if (m->src[i] + m->len[i] == pr.first && m->dst[i] + m->len[i] == pr.second) {
+        m->len[i]++;
+        continue;
+      }
+    }
+    if (m->n >= kMaxNarrowRuns) {
+      *ok = false;
+      return TSG_OK;
+    }
+    m->src[m->n] = (uint8_t)pr.first;
+    m->dst[m->n] = (uint8_t)pr.second;
+    m->len[m->n] = 1;
+    m->n++;
+  }
+  return TSG_OK;
+}
+
+uint32_t narrow_scatter_host(const NarrowMap& m, uint32_t x) {
+  uint32_t r = 0;
+  for (int i = 0; i < m.n; ++i) r |= ((x >> m.src[i]) & ((1u << m.len[i]) - 1u)) << m.dst[i];
+  return r;
+}
+
+struct LaunchArgs {
+  StepArgs a;       // general form (also used for the bounds check)
+  StepArgs2 a2;     // narrow form, valid when `narrow`
+  bool narrow;
+  bool is_leaf[2];
+  uint64_t cnt;     // slices of this launch
+};
+
 // Fills the kernel arguments of step s for slices [base, base + cnt) (cnt == 1 and base
-// ignored for slice-independent steps).
-tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, StepArgs* out,
-                      bool is_leaf_out[2]) {
+// ignored for slice-independent steps) and bounds-checks them.
+tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchArgs* la) {
   const tsg_plan* plan = c.plan;
   const StepInfo& st = plan->steps[s];
-  const int gb = st.dep ? c.g_bits : 0;
-  StepArgs& a = *out;
+  StepArgs& a = la->a;
   std::memset(&a, 0, sizeof(a));
-  a.total = (uint64_t)(st.dep ? cnt : 1) << st.out_bits;
+  la->cnt = (uint64_t)(st.dep ? cnt : 1);
+  a.total = la->cnt << st.out_bits;
   a.k_bits = st.k_bits;
-  a.out = c.ws + c.lay->offset[s];
+  a.out = c.ws ? c.ws + c.lay->offset[s] : nullptr;
   a.o_plane = (uint64_t)c.lay->plane[s];
-  bool is_leaf[2];
+  OperandDesc d[2] = {describe_operand(c, st, 0, base), describe_operand(c, st, 1, base)};
   for (int o = 0; o < 2; ++o) {
-    const int v = st.op[o];
-    std::vector<std::pair<int, int>> tp, kp;
-    for (int i = 0; i < st.out_bits; ++i)
-      if (st.pos[o][i] >= 0) tp.push_back({i, st.pos[o][i]});
-    for (int i = 0; i < st.k_bits; ++i)
-      if (st.pos[o][st.out_bits + i] >= 0) kp.push_back({i, st.pos[o][st.out_bits + i]});
-    uint64_t basec = 0;
-    const uint8_t* ptr;
-    uint64_t plane = 0;
-    if (v >= 0) {
-      const LeafInfo& lf = plan->leaves[v];
-      ptr = c.pool;
-      basec = (uint64_t)lf.offset;
-      for (int j = 0; j < plan->num_sliced; ++j) {
-        if (lf.spos[j] < 0) continue;
-        if (st.dep && j < gb) {
-          tp.push_back({st.out_bits + j, lf.spos[j]});
-        } else if (st.dep) {
-          basec += (uint64_t)((base >> j) & 1) << lf.spos[j];
-        }
+    std::vector<std::pair<int, int>> tp = d[o].tp;
+    for (const auto& pr : d[o].gp) tp.push_back({st.out_bits + pr.first, pr.second});
+    TSG_TRY(make_bitmap(tp, o == 0 ? &a.lt : &a.rt));
+    TSG_TRY(make_bitmap(d[o].kp, o == 0 ? &a.lk : &a.rk));
+    (o == 0 ? a.lhs : a.rhs) = d[o].ptr;
+    (o == 0 ? a.l_base : a.r_base) = d[o].base;
+    (o == 0 ? a.l_plane : a.r_plane) = d[o].plane;
+    la->is_leaf[o] = d[o].leaf;
+  }
+  TSG_TRY(check_step_bounds(c, s, a, la->is_leaf));
+  // narrow form
+  StepArgs2& n = la->a2;
+  std::memset(&n, 0, sizeof(n));
+  bool ok = st.out_bits <= 30 && st.k_bits <= 30 && la->cnt <= 65535;
+  if (ok) {
+    n.lhs = a.lhs;
+    n.rhs = a.rhs;
+    n.out = a.out;
+    n.l_base = a.l_base;
+    n.r_base = a.r_base;
+    n.l_plane = a.l_plane;
+    n.r_plane = a.r_plane;
+    n.o_plane = a.o_plane;
+    n.n_out = 1u << st.out_bits;
+    n.k_bits = st.k_bits;
+    n.v = st.out_bits >= 2 ? 4 : (1 << st.out_bits);
+    for (int o = 0; o < 2 && ok; ++o) {
+      NarrowMap* om = o == 0 ? &n.lo : &n.ro;
+      NarrowMap* km = o == 0 ? &n.lk : &n.rk;
+      TSG_TRY(make_narrow(d[o].tp, om, &ok));
+      if (ok) TSG_TRY(make_narrow(d[o].kp, km, &ok));
+      if (!ok) break;
+      TSG_TRY(make_bitmap(d[o].gp, o == 0 ? &n.lg : &n.rg));
+      uint32_t* tab = o == 0 ? n.l_tab : n.r_tab;
+      bool contig = n.v == 4, bcast = true;
+      for (int j = 0; j < n.v; ++j) {
+        tab[j] = narrow_scatter_host(*om, (uint32_t)j);
+        contig = contig && tab[j] == (uint32_t)j;
+        bcast = bcast && tab[j] == 0;
       }
-      is_leaf[o] = true;
-    } else {
-      const int x = -v - 1;
-      const StepInfo& xs = plan->steps[x];
-      ptr = c.ws + c.lay->offset[x];
-      plane = (uint64_t)c.lay->plane[x];
-      if (xs.dep)
-        for (int j = 0; j < gb; ++j) tp.push_back({st.out_bits + j, xs.out_bits + j});
-      is_leaf[o] = false;
-    }
-    BitMap* tm = o == 0 ? &a.lt : &a.rt;
-    BitMap* km = o == 0 ? &a.lk : &a.rk;
-    TSG_TRY(make_bitmap(tp, tm));
-    TSG_TRY(make_bitmap(kp, km));
-    if (o == 0) {
-      a.lhs = ptr;
-      a.l_base = basec;
-      a.l_plane = plane;
-    } else {
-      a.rhs = ptr;
-      a.r_base = basec;
-      a.r_plane = plane;
+      // vector loads need 4-element alignment of every start offset: the low two bits
+      // are output bits 0-1 (so no other wire maps there) and the constant part must be
+      // a multiple of 4 (leaf offsets are the caller's; workspace buffers are aligned)
+      const uint64_t cbase = o == 0 ? n.l_base : n.r_base;
+      if (contig && (cbase & 3) != 0) contig = false;
+      (o == 0 ? n.l_mode : n.r_mode) = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
     }
   }
-  is_leaf_out[0] = is_leaf[0];
-  is_leaf_out[1] = is_leaf[1];
-  return check_step_bounds(c, s, a, is_leaf);
+  la->narrow = ok;
+  return TSG_OK;
+}
+
+template <int kRing, bool kL, bool kR>
+void launch_narrow_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  const StepArgs2& n = la.a2;
+  const uint64_t work = (uint64_t)n.n_out / (uint64_t)n.v;  // threads per slice
+  unsigned threads = 32;
+  while (threads < kThreads && threads < work) threads <<= 1;
+  uint64_t bx = (work + threads - 1) / threads;
+  const uint64_t target = (uint64_t)device_sm_count() * 16;
+  const uint64_t cap = std::max<uint64_t>(1, (target + la.cnt - 1) / la.cnt);
+  if (bx > cap) bx = cap;
+  dim3 grid((unsigned)bx, (unsigned)la.cnt);
+  tree_step_narrow_kernel<kRing, kL, kR><<<grid, threads, 0, st>>>(n, ra);
+}
+
+template <int kRing>
+void launch_narrow_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  if (la.is_leaf[0]) {
+    if (la.is_leaf[1]) launch_narrow_t<kRing, true, true>(la, ra, st);
+    else launch_narrow_t<kRing, true, false>(la, ra, st);
+  } else {
+    if (la.is_leaf[1]) launch_narrow_t<kRing, false, true>(la, ra, st);
+    else launch_narrow_t<kRing, false, false>(la, ra, st);
+  }
 }
 
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
-  StepArgs a;
-  bool is_leaf[2];
-  TSG_TRY(build_step(c, s, base, cnt, &a, is_leaf));
+  LaunchArgs la;
+  TSG_TRY(build_step(c, s, base, cnt, &la));
+  if (la.narrow) {
+    switch (c.ring) {
+      case TSG_RING_OR_AND:
+        launch_narrow_t<TSG_RING_OR_AND, true, true>(la, c.ra, c.stream);
+        break;
+      case TSG_RING_U64:
+        launch_narrow_ring<TSG_RING_U64>(la, c.ra, c.stream);
+        break;
+      default:
+        launch_narrow_ring<TSG_RING_MODP>(la, c.ra, c.stream);
+        break;
+    }
+    TSG_CUDA_TRY(cudaGetLastError());
+    return TSG_OK;
+  }
+  const StepArgs& a = la.a;
   switch (c.ring) {
     case TSG_RING_OR_AND:
       // every OR_AND operand is uint8, leaf or not
       launch_step_t<TSG_RING_OR_AND, true, true>(a, c.ra, c.stream);
       break;
     case TSG_RING_U64:
-      launch_step_ring<TSG_RING_U64>(is_leaf[0], is_leaf[1], a, c.ra, c.stream);
+      launch_step_ring<TSG_RING_U64>(la.is_leaf[0], la.is_leaf[1], a, c.ra, c.stream);
       break;
     default:
-      launch_step_ring<TSG_RING_MODP>(is_leaf[0], is_leaf[1], a, c.ra, c.stream);
+      launch_step_ring<TSG_RING_MODP>(la.is_leaf[0], la.is_leaf[1], a, c.ra, c.stream);
       break;
   }
   TSG_CUDA_TRY(cudaGetLastError());
@@ -621,9 +913,8 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
   const int ns = (int)plan->steps.size();
   auto step = [&](int s, int64_t base, int64_t cnt) -> tsg_status {
     if (!dry) return launch_step(c, s, base, cnt);
-    StepArgs a;
-    bool is_leaf[2];
-    return build_step(c, s, base, cnt, &a, is_leaf);
+    LaunchArgs la;
+    return build_step(c, s, base, cnt, &la);
   };
   for (int s = 0; s < ns; ++s)
     if (!plan->steps[s].dep) TSG_TRY(step(s, 0, 1));
