@@ -326,7 +326,7 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
         if k > 0:  # the first call allocates workspaces in torch's caching allocator
             e2e_times.append(time.perf_counter() - t0)
-    e2e_value = world * group / ns / statistics.mean(e2e_times)
+    e2e_value = world * group / ns / statistics.mean(e2e_times) if e2e_times else None
 
     cpu = None
     if want_cpu:
@@ -349,8 +349,8 @@ def run_gb300(args) -> None:
                          "peak_source": peak_kind,
                          "kernel": "tree_step_kernel (all steps of a slice group)"},
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+            "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                     "d2h_bytes_per_step": d2h} if e2e_value is not None else None),
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(),
             "step_ms": [round(x, 3) for x in step_ms],

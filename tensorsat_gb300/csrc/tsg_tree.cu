@@ -126,17 +126,23 @@ __global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArg
 }
 
 // ------------------------------------------------------------------------------------
-// Narrow step kernel: the common case where a slice's tensors have < 2^32 entries.
-// The slice slot g is blockIdx.y, so each block resolves the 64-bit slice offsets once and
-// threads work in 32-bit offsets. Each thread produces `v` (1, 2 or 4) consecutive outputs:
-// their operand offsets differ by the precomputed `tab` entries, which lets an operand whose
-// fastest output bits are its own fastest bits be read with one vector load (mode kContig)
-// and an operand that does not carry those bits be read once (mode kBcast).
+// Tile kernel: the common case where a slice's tensors have < 2^32 entries and at most
+// 4 wires are summed. Output bits split into three groups:
+//   E  up to 2 "enumerated" bits, looped over inside a thread: the output bits the larger
+//      operand does not carry, so that operand is read once and reused for every E value;
+//   F  the remaining output bits; the low `tile_bits` of them index threads (V consecutive
+//      positions per thread), the rest index blocks (blockIdx.x);
+//   g  the slice slot (blockIdx.y).
+// Every operand offset is base + scatter(g) + scatter(F high) [uniform per block] +
+// scatter(F low) [once per thread] + tables for the V positions, E values and summed
+// combinations, so the per-output index work is a few table adds.
 
 constexpr int kMaxNarrowRuns = 32;
 constexpr int kModeGather = 0;
 constexpr int kModeContig = 1;
 constexpr int kModeBcast = 2;
+constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
+constexpr int kMaxK = 16;  // summed combinations kept in tables (k <= 4)
 
 struct NarrowMap {
   int32_t n;
@@ -145,19 +151,31 @@ struct NarrowMap {
   uint8_t dst[kMaxNarrowRuns];
 };
 
-struct StepArgs2 {
-  const uint8_t* lhs;
-  const uint8_t* rhs;
+struct TileOperand {
+  const uint8_t* ptr;
+  uint64_t base;          // constant element offset
+  uint64_t plane;         // residue-plane stride (elements); 0 for leaves
+  NarrowMap f_lo, f_hi;   // F bits below / at or above tile_bits -> operand bits
+  BitMap g;               // slice-slot bits -> operand bits
+  uint32_t tab[4];        // offsets of the V consecutive F positions
+  uint32_t e_off[kMaxE];  // offsets of the E combinations
+  uint32_t k_off[kMaxK];  // offsets of the summed combinations
+  int32_t mode;           // kModeContig / kModeBcast / kModeGather for the V positions
+  int32_t has_e;          // carries E bits (reloaded per E combination)
+  int32_t leaf;           // uint8 leaf (widened on load)
+};
+
+struct TileArgs {
+  TileOperand op[2];
   uint8_t* out;
-  uint64_t l_base, r_base;             // constant element offsets
-  uint64_t l_plane, r_plane, o_plane;  // residue-plane strides (elements)
-  uint32_t n_out;                      // outputs per slice (2^out_bits)
-  int32_t k_bits;
-  int32_t v;                           // outputs per thread (1, 2, 4), divides n_out
-  int32_t l_mode, r_mode;
-  uint32_t l_tab[4], r_tab[4];         // offsets of outputs j < v relative to output 0
-  NarrowMap lo, ro, lk, rk;            // output-bit and summed-bit runs
-  BitMap lg, rg;                       // slice-slot bits (64-bit destinations)
+  uint64_t o_plane;
+  uint32_t n_out;          // outputs per slice
+  NarrowMap of_lo, of_hi;  // F bits -> output bit positions
+  uint32_t o_tab[4];
+  uint32_t o_e[kMaxE];
+  int32_t tile_bits;
+  int32_t n_k;             // summed combinations (2^k)
+  int32_t o_contig;        // the V positions are consecutive outputs
 };
 
 __device__ __forceinline__ uint32_t scatter32(const NarrowMap& m, uint32_t x) {
@@ -167,124 +185,141 @@ __device__ __forceinline__ uint32_t scatter32(const NarrowMap& m, uint32_t x) {
   return r;
 }
 
-// Loads v values of one operand (plane p) starting at element offset `off`.
-template <typename T, bool kLeaf>
-__device__ __forceinline__ void load_v(const uint8_t* base, uint64_t off, int mode, int v,
-                                       const uint32_t* tab, uint64_t out[4]) {
-  if (mode == kModeBcast) {
-    const uint64_t x = kLeaf ? (uint64_t)base[off] : (uint64_t)reinterpret_cast<const T*>(base)[off];
-    out[0] = out[1] = out[2] = out[3] = x;
-    return;
-  }
-  if (mode == kModeContig) {  // v == 4, off is a multiple of 4 (checked on the host)
-    if constexpr (kLeaf || sizeof(T) == 1) {
+// Loads the V values of one operand (residue plane already folded into `off`).
+template <typename T, typename VT, int V>
+__device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, VT (&out)[V]) {
+  const uint8_t* base = op.ptr;
+  if (op.leaf) {
+    if (V == 4 && op.mode == kModeContig) {
       const uint32_t w = *reinterpret_cast<const uint32_t*>(base + off);
-      out[0] = w & 0xff;
-      out[1] = (w >> 8) & 0xff;
-      out[2] = (w >> 16) & 0xff;
-      out[3] = w >> 24;
-    } else if constexpr (sizeof(T) == 4) {
-      const uint4 w = *reinterpret_cast<const uint4*>(reinterpret_cast<const T*>(base) + off);
-      out[0] = w.x;
-      out[1] = w.y;
-      out[2] = w.z;
-      out[3] = w.w;
+#pragma unroll
+      for (int j = 0; j < V; ++j) out[j] = (VT)((w >> (8 * j)) & 0xff);
+    } else if (op.mode == kModeBcast) {
+      const VT x = (VT)base[off];
+#pragma unroll
+      for (int j = 0; j < V; ++j) out[j] = x;
     } else {
-      const ulonglong2* p = reinterpret_cast<const ulonglong2*>(reinterpret_cast<const T*>(base) + off);
-      const ulonglong2 w0 = p[0], w1 = p[1];
-      out[0] = w0.x;
-      out[1] = w0.y;
-      out[2] = w1.x;
-      out[3] = w1.y;
+#pragma unroll
+      for (int j = 0; j < V; ++j) out[j] = (VT)base[off + op.tab[j]];
     }
     return;
   }
+  const T* p = reinterpret_cast<const T*>(base);
+  if (V == 4 && op.mode == kModeContig) {
+    if constexpr (sizeof(T) == 1) {
+      const uint32_t w = *reinterpret_cast<const uint32_t*>(p + off);
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    if (j < v) {
-      out[j] = kLeaf ? (uint64_t)base[off + tab[j]]
-                     : (uint64_t)reinterpret_cast<const T*>(base)[off + tab[j]];
+      for (int j = 0; j < V; ++j) out[j] = (VT)((w >> (8 * j)) & 0xff);
+    } else if constexpr (sizeof(T) == 4) {
+      const uint4 w = *reinterpret_cast<const uint4*>(p + off);
+      out[0] = w.x;
+      out[1 % V] = w.y;
+      out[2 % V] = w.z;
+      out[3 % V] = w.w;
+    } else {
+      const ulonglong2* q = reinterpret_cast<const ulonglong2*>(p + off);
+      const ulonglong2 w0 = q[0], w1 = q[1];
+      out[0] = w0.x;
+      out[1 % V] = w0.y;
+      out[2 % V] = w1.x;
+      out[3 % V] = w1.y;
     }
+  } else if (op.mode == kModeBcast) {
+    const VT x = (VT)p[off];
+#pragma unroll
+    for (int j = 0; j < V; ++j) out[j] = x;
+  } else {
+#pragma unroll
+    for (int j = 0; j < V; ++j) out[j] = (VT)p[off + op.tab[j]];
   }
 }
 
-template <int kRing, bool kLLeaf, bool kRLeaf>
-__global__ void __launch_bounds__(kThreads) tree_step_narrow_kernel(StepArgs2 a, RingArgs ring) {
+template <int kRing, int V, int NE>
+__global__ void __launch_bounds__(kThreads) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
   using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
             typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
-  constexpr int kPlanes = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
+  using VT = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
+  using AT = typename std::conditional<kRing == TSG_RING_OR_AND, uint32_t, uint64_t>::type;
   const uint32_t g = blockIdx.y;
-  const uint64_t lg = a.l_base + scatter_bits(a.lg, g);
-  const uint64_t rg = a.r_base + scatter_bits(a.rg, g);
-  const uint64_t og = (uint64_t)g * a.n_out;
-  const uint32_t nk = 1u << a.k_bits;
+  const uint32_t f_hi = blockIdx.x << a.tile_bits;
+  const uint32_t f_lo = threadIdx.x * (uint32_t)V;
+  uint64_t xo[2];
+#pragma unroll
+  for (int o = 0; o < 2; ++o) {
+    const TileOperand& op = a.op[o];
+    xo[o] = op.base + scatter_bits(op.g, g) + scatter32(op.f_hi, f_hi) + scatter32(op.f_lo, f_lo);
+  }
+  const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
   const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
-  const int v = a.v;
-  const uint32_t step = gridDim.x * blockDim.x * (uint32_t)v;
-  for (uint32_t o0 = (blockIdx.x * blockDim.x + threadIdx.x) * (uint32_t)v; o0 < a.n_out;
-       o0 += step) {
-    const uint64_t lo = lg + scatter32(a.lo, o0);
-    const uint64_t ro = rg + scatter32(a.ro, o0);
-    uint64_t acc[kPlanes][4];
+  const TileOperand& L = a.op[0];
+  const TileOperand& R = a.op[1];
+  for (int p = 0; p < np; ++p) {
+    const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
+    const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
+    AT acc[NE][V];
 #pragma unroll
-    for (int p = 0; p < kPlanes; ++p)
+    for (int e = 0; e < NE; ++e)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) acc[p][j] = 0;
-    for (uint32_t kk = 0; kk < nk; ++kk) {
-      const uint64_t lko = lo + scatter32(a.lk, kk);
-      const uint64_t rko = ro + scatter32(a.rk, kk);
+      for (int j = 0; j < V; ++j) acc[e][j] = 0;
+    for (int kk = 0; kk < a.n_k; ++kk) {
+      VT lv[V], rv[V];
+      if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[kk], lv);
+      if (!R.has_e) tile_load<T, VT, V>(R, rp + R.k_off[kk], rv);
 #pragma unroll
-      for (int p = 0; p < kPlanes; ++p) {
-        if (p >= np) break;
-        uint64_t lv[4], rv[4];
-        load_v<T, kLLeaf>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane), a.l_mode, v, a.l_tab, lv);
-        load_v<T, kRLeaf>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane), a.r_mode, v, a.r_tab, rv);
+      for (int e = 0; e < NE; ++e) {
+        if (L.has_e) tile_load<T, VT, V>(L, lp + L.e_off[e] + L.k_off[kk], lv);
+        if (R.has_e) tile_load<T, VT, V>(R, rp + R.e_off[e] + R.k_off[kk], rv);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < V; ++j) {
           if constexpr (kRing == TSG_RING_OR_AND) {
-            acc[p][j] |= lv[j] & rv[j];
+            acc[e][j] |= lv[j] & rv[j];
           } else {
-            acc[p][j] += lv[j] * rv[j];
-          }
-        }
-        if constexpr (kRing == TSG_RING_MODP) {
-          // residues < 2^31: three products plus a reduced value stay below 2^64
-          if (kk % 3 == 2) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) acc[p][j] = barrett_reduce(acc[p][j], ring.p[p], ring.m[p]);
+            acc[e][j] += (AT)lv[j] * (AT)rv[j];
           }
         }
       }
-    }
-    const uint64_t oo = og + o0;
+      if constexpr (kRing == TSG_RING_MODP) {
+        // residues < 2^31: three products plus a reduced value stay below 2^64
+        if (kk % 3 == 2) {
 #pragma unroll
-    for (int p = 0; p < kPlanes; ++p) {
-      if (p >= np) break;
+          for (int e = 0; e < NE; ++e)
+#pragma unroll
+            for (int j = 0; j < V; ++j) acc[e][j] = barrett_reduce(acc[e][j], ring.p[p], ring.m[p]);
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      const uint64_t oe = oo + a.o_e[e];
       if constexpr (kRing == TSG_RING_OR_AND) {
-        if (v == 4) {
-          const uint32_t w = (acc[p][0] ? 1u : 0u) | (acc[p][1] ? 1u << 8 : 0u) |
-                             (acc[p][2] ? 1u << 16 : 0u) | (acc[p][3] ? 1u << 24 : 0u);
-          *reinterpret_cast<uint32_t*>(a.out + oo) = w;
+        if (V == 4 && a.o_contig) {
+          uint32_t w = 0;
+#pragma unroll
+          for (int j = 0; j < V; ++j) w |= (acc[e][j] ? 1u : 0u) << (8 * j);
+          *reinterpret_cast<uint32_t*>(a.out + oe) = w;
         } else {
-          for (int j = 0; j < v; ++j) a.out[oo + j] = acc[p][j] ? 1 : 0;
+#pragma unroll
+          for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = acc[e][j] ? 1 : 0;
         }
       } else if constexpr (kRing == TSG_RING_U64) {
-        uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oo;
-        if (v == 4) {
-          reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[p][0], acc[p][1]);
-          reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[p][2], acc[p][3]);
+        uint64_t* out = reinterpret_cast<uint64_t*>(a.out);
+        if (V == 4 && a.o_contig) {
+          reinterpret_cast<ulonglong2*>(out + oe)[0] = make_ulonglong2(acc[e][0], acc[e][1 % V]);
+          reinterpret_cast<ulonglong2*>(out + oe)[1] = make_ulonglong2(acc[e][2 % V], acc[e][3 % V]);
         } else {
-          for (int j = 0; j < v; ++j) out[j] = acc[p][j];
+#pragma unroll
+          for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = acc[e][j];
         }
       } else {
-        uint32_t r[4];
+        uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane;
+        uint32_t r[V];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) r[j] = barrett_reduce(acc[p][j], ring.p[p], ring.m[p]);
-        uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane + oo;
-        if (v == 4) {
-          *reinterpret_cast<uint4*>(out) = make_uint4(r[0], r[1], r[2], r[3]);
+        for (int j = 0; j < V; ++j) r[j] = barrett_reduce(acc[e][j], ring.p[p], ring.m[p]);
+        if (V == 4 && a.o_contig) {
+          *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1 % V], r[2 % V], r[3 % V]);
         } else {
-          for (int j = 0; j < v; ++j) out[j] = r[j];
+#pragma unroll
+          for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
         }
       }
     }
@@ -681,19 +716,173 @@ tsg_status make_narrow(std::vector<std::pair<int, int>> pairs, NarrowMap* m, boo
   return TSG_OK;
 }
 
-uint32_t narrow_scatter_host(const NarrowMap& m, uint32_t x) {
-  uint32_t r = 0;
-  for (int i = 0; i < m.n; ++i) r |= ((x >> m.src[i]) & ((1u << m.len[i]) - 1u)) << m.dst[i];
+// Scatter of x through (src bit -> dst bit) pairs, computed directly on the host.
+uint64_t scatter_pairs(const std::vector<std::pair<int, int>>& pairs, uint64_t x) {
+  uint64_t r = 0;
+  for (const auto& pr : pairs)
+    if ((x >> pr.first) & 1) r |= 1ull << pr.second;
   return r;
 }
 
+struct TileShape {
+  int v, ne;          // template parameters
+  unsigned threads;
+  uint64_t tiles;
+};
+
 struct LaunchArgs {
   StepArgs a;       // general form (also used for the bounds check)
-  StepArgs2 a2;     // narrow form, valid when `narrow`
-  bool narrow;
+  TileArgs t;       // tile form, valid when `tile`
+  TileShape shape;
+  bool tile;
   bool is_leaf[2];
   uint64_t cnt;     // slices of this launch
 };
+
+// Builds the tile form of step s from the operand descriptions; sets *ok = false when the
+// step is outside what the tile kernel handles (it then runs the general kernel).
+tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs& a,
+                      uint64_t cnt, TileArgs* t, TileShape* shape, bool* ok) {
+  std::memset(t, 0, sizeof(*t));
+  *ok = st.out_bits <= 30 && st.k_bits <= 4 && cnt <= 65535;
+  if (!*ok) return TSG_OK;
+  // E: output bits the larger operand does not carry (at most 2, highest first)
+  int carried[2] = {0, 0};
+  for (int o = 0; o < 2; ++o)
+    for (const auto& pr : d[o].tp) carried[o]++;
+  const int big = carried[0] >= carried[1] ? 0 : 1;
+  std::vector<int> ebits, fbits;
+  {
+    std::vector<int> cand;
+    for (int i = 0; i < st.out_bits; ++i)
+      if (st.pos[big][i] < 0) cand.push_back(i);
+    while (cand.size() > 2) cand.erase(cand.begin());  // keep the two highest
+    ebits = cand;
+    for (int i = 0; i < st.out_bits; ++i)
+      if (std::find(ebits.begin(), ebits.end(), i) == ebits.end()) fbits.push_back(i);
+  }
+  const int nf = (int)fbits.size();
+  const int v = nf >= 2 ? 4 : 1;
+  const int ne = 1 << ebits.size();
+  uint64_t positions = (uint64_t)1 << nf;           // F positions per slice
+  uint64_t threads = std::min<uint64_t>(kThreads, positions / v);
+  if (threads == 0) threads = 1;
+  int tile_bits = 0;
+  while (((uint64_t)1 << tile_bits) < threads * v) tile_bits++;
+  shape->v = v;
+  shape->ne = ne;
+  shape->threads = (unsigned)threads;
+  shape->tiles = positions >> tile_bits;
+  if (shape->tiles >= (1ull << 31)) {
+    *ok = false;
+    return TSG_OK;
+  }
+  t->tile_bits = tile_bits;
+  t->n_k = 1 << st.k_bits;
+  t->n_out = 1u << st.out_bits;
+  t->out = a.out;
+  t->o_plane = a.o_plane;
+  // output maps: F index bit fi -> output bit fbits[fi]; E combo bits -> output bits
+  std::vector<std::pair<int, int>> olo, ohi, oe;
+  for (int fi = 0; fi < nf; ++fi) (fi < tile_bits ? olo : ohi).push_back({fi, fbits[fi]});
+  for (size_t b = 0; b < ebits.size(); ++b) oe.push_back({(int)b, ebits[b]});
+  TSG_TRY(make_narrow(olo, &t->of_lo, ok));
+  if (*ok) TSG_TRY(make_narrow(ohi, &t->of_hi, ok));
+  if (!*ok) return TSG_OK;
+  bool ocontig = v == 4;
+  for (int j = 0; j < v; ++j) {
+    t->o_tab[j] = (uint32_t)scatter_pairs(olo, j);
+    ocontig = ocontig && t->o_tab[j] == (uint32_t)j;
+  }
+  t->o_contig = ocontig ? 1 : 0;
+  for (int e = 0; e < ne; ++e) t->o_e[e] = (uint32_t)scatter_pairs(oe, e);
+  for (int o = 0; o < 2; ++o) {
+    TileOperand& op = t->op[o];
+    op.ptr = o == 0 ? a.lhs : a.rhs;
+    op.base = d[o].base;
+    op.plane = d[o].plane;
+    op.leaf = d[o].leaf ? 1 : 0;
+    std::vector<std::pair<int, int>> lo, hi, ep;
+    for (int fi = 0; fi < nf; ++fi) {
+      const int p = st.pos[o][fbits[fi]];
+      if (p >= 0) (fi < tile_bits ? lo : hi).push_back({fi, p});
+    }
+    for (size_t b = 0; b < ebits.size(); ++b) {
+      const int p = st.pos[o][ebits[b]];
+      if (p >= 0) ep.push_back({(int)b, p});
+    }
+    TSG_TRY(make_narrow(lo, &op.f_lo, ok));
+    if (*ok) TSG_TRY(make_narrow(hi, &op.f_hi, ok));
+    for (const auto& pr : d[o].kp)
+      if (pr.second >= 32) *ok = false;
+    if (!*ok) return TSG_OK;
+    TSG_TRY(make_bitmap(d[o].gp, &op.g));
+    bool contig = v == 4, bcast = true;
+    for (int j = 0; j < v; ++j) {
+      op.tab[j] = (uint32_t)scatter_pairs(lo, j);
+      contig = contig && op.tab[j] == (uint32_t)j;
+      bcast = bcast && op.tab[j] == 0;
+    }
+    // vector loads need every start offset to be a multiple of 4 elements: output bits
+    // 0-1 occupy the operand's bits 0-1, so only the constant part can break that
+    // (leaf offsets are the caller's; workspace buffers are 256-byte aligned)
+    if (contig && (op.base & 3) != 0) contig = false;
+    op.mode = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
+    op.has_e = ep.empty() ? 0 : 1;
+    for (int e = 0; e < ne; ++e) op.e_off[e] = (uint32_t)scatter_pairs(ep, e);
+    for (int kk = 0; kk < t->n_k; ++kk) op.k_off[kk] = (uint32_t)scatter_pairs(d[o].kp, kk);
+  }
+  return TSG_OK;
+}
+
+// Largest scatter of a source value whose set bits lie in [from, to).
+uint32_t narrow_max(const NarrowMap& m, int to, int from = 0) {
+  uint32_t r = 0;
+  for (int i = 0; i < m.n; ++i)
+    for (int b = 0; b < m.len[i]; ++b) {
+      const int src = m.src[i] + b;
+      if (src >= from && src < to) r |= 1u << (m.dst[i] + b);
+    }
+  return r;
+}
+
+// Bounds check of the tile form: the largest offset each term can take (slot, tile,
+// thread, V position, E combination, summed combination) added up must stay inside the
+// operand and the output buffer.
+tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
+  const tsg_plan* plan = c.plan;
+  const StepInfo& st = plan->steps[s];
+  const TileArgs& t = la.t;
+  const TileShape& sh = la.shape;
+  const int gbits = bit_width(la.cnt - 1);
+  const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
+  const int vbits = sh.v == 4 ? 2 : 0;  // thread positions are multiples of V
+  if ((uint64_t)sh.threads * sh.v != (1ull << t.tile_bits))
+    return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: threads x V is not the tile size");
+  for (int o = 0; o < 2; ++o) {
+    const TileOperand& op = t.op[o];
+    uint32_t tab = 0, eo = 0, ko = 0;
+    for (int j = 0; j < sh.v; ++j) tab = std::max(tab, op.tab[j]);
+    for (int e = 0; e < sh.ne; ++e) eo = std::max(eo, op.e_off[e]);
+    for (int kk = 0; kk < t.n_k; ++kk) ko = std::max(ko, op.k_off[kk]);
+    const uint64_t hi = op.base + scatter_max(op.g, gbits) + narrow_max(op.f_hi, nbits) +
+                        narrow_max(op.f_lo, t.tile_bits, vbits) + tab + eo + ko;
+    const int v = st.op[o];
+    const uint64_t lo_ext = la.is_leaf[o] ? (uint64_t)plan->leaves[v].offset : 0;
+    const uint64_t hi_ext = la.is_leaf[o] ? lo_ext + (1ull << plan->leaves[v].rank)
+                                          : (uint64_t)c.lay->plane[-v - 1];
+    if (op.base < lo_ext || hi >= hi_ext)
+      return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: operand offset outside its tensor");
+  }
+  uint32_t otab = 0, oe = 0;
+  for (int j = 0; j < sh.v; ++j) otab = std::max(otab, t.o_tab[j]);
+  for (int e = 0; e < sh.ne; ++e) oe = std::max(oe, t.o_e[e]);
+  const uint64_t ohi = (la.cnt - 1) * (uint64_t)t.n_out + narrow_max(t.of_hi, nbits) +
+                       narrow_max(t.of_lo, t.tile_bits, vbits) + otab + oe;
+  if (ohi >= (uint64_t)c.lay->plane[s])
+    return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: output offset outside its buffer");
+  return TSG_OK;
+}
 
 // Fills the kernel arguments of step s for slices [base, base + cnt) (cnt == 1 and base
 // ignored for slice-independent steps) and bounds-checks them.
@@ -719,86 +908,46 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
     la->is_leaf[o] = d[o].leaf;
   }
   TSG_TRY(check_step_bounds(c, s, a, la->is_leaf));
-  // narrow form
-  StepArgs2& n = la->a2;
-  std::memset(&n, 0, sizeof(n));
-  bool ok = st.out_bits <= 30 && st.k_bits <= 30 && la->cnt <= 65535;
-  if (ok) {
-    n.lhs = a.lhs;
-    n.rhs = a.rhs;
-    n.out = a.out;
-    n.l_base = a.l_base;
-    n.r_base = a.r_base;
-    n.l_plane = a.l_plane;
-    n.r_plane = a.r_plane;
-    n.o_plane = a.o_plane;
-    n.n_out = 1u << st.out_bits;
-    n.k_bits = st.k_bits;
-    n.v = st.out_bits >= 2 ? 4 : (1 << st.out_bits);
-    for (int o = 0; o < 2 && ok; ++o) {
-      NarrowMap* om = o == 0 ? &n.lo : &n.ro;
-      NarrowMap* km = o == 0 ? &n.lk : &n.rk;
-      TSG_TRY(make_narrow(d[o].tp, om, &ok));
-      if (ok) TSG_TRY(make_narrow(d[o].kp, km, &ok));
-      if (!ok) break;
-      TSG_TRY(make_bitmap(d[o].gp, o == 0 ? &n.lg : &n.rg));
-      uint32_t* tab = o == 0 ? n.l_tab : n.r_tab;
-      bool contig = n.v == 4, bcast = true;
-      for (int j = 0; j < n.v; ++j) {
-        tab[j] = narrow_scatter_host(*om, (uint32_t)j);
-        contig = contig && tab[j] == (uint32_t)j;
-        bcast = bcast && tab[j] == 0;
-      }
-      // vector loads need 4-element alignment of every start offset: the low two bits
-      // are output bits 0-1 (so no other wire maps there) and the constant part must be
-      // a multiple of 4 (leaf offsets are the caller's; workspace buffers are aligned)
-      const uint64_t cbase = o == 0 ? n.l_base : n.r_base;
-      if (contig && (cbase & 3) != 0) contig = false;
-      (o == 0 ? n.l_mode : n.r_mode) = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
-    }
-  }
-  la->narrow = ok;
+  bool ok = false;
+  TSG_TRY(build_tile(st, d, a, la->cnt, &la->t, &la->shape, &ok));
+  la->tile = ok;
+  if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
   return TSG_OK;
 }
 
-template <int kRing, bool kL, bool kR>
-void launch_narrow_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  const StepArgs2& n = la.a2;
-  const uint64_t work = (uint64_t)n.n_out / (uint64_t)n.v;  // threads per slice
-  unsigned threads = 32;
-  while (threads < kThreads && threads < work) threads <<= 1;
-  uint64_t bx = (work + threads - 1) / threads;
-  const uint64_t target = (uint64_t)device_sm_count() * 16;
-  const uint64_t cap = std::max<uint64_t>(1, (target + la.cnt - 1) / la.cnt);
-  if (bx > cap) bx = cap;
-  dim3 grid((unsigned)bx, (unsigned)la.cnt);
-  tree_step_narrow_kernel<kRing, kL, kR><<<grid, threads, 0, st>>>(n, ra);
+template <int kRing, int V, int NE>
+void launch_tile_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  dim3 grid((unsigned)la.shape.tiles, (unsigned)la.cnt);
+  tree_step_tile_kernel<kRing, V, NE><<<grid, la.shape.threads, 0, st>>>(la.t, ra);
 }
 
 template <int kRing>
-void launch_narrow_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  if (la.is_leaf[0]) {
-    if (la.is_leaf[1]) launch_narrow_t<kRing, true, true>(la, ra, st);
-    else launch_narrow_t<kRing, true, false>(la, ra, st);
+void launch_tile_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  const int v = la.shape.v, ne = la.shape.ne;
+  if (v == 4) {
+    if (ne == 1) launch_tile_t<kRing, 4, 1>(la, ra, st);
+    else if (ne == 2) launch_tile_t<kRing, 4, 2>(la, ra, st);
+    else launch_tile_t<kRing, 4, 4>(la, ra, st);
   } else {
-    if (la.is_leaf[1]) launch_narrow_t<kRing, false, true>(la, ra, st);
-    else launch_narrow_t<kRing, false, false>(la, ra, st);
+    if (ne == 1) launch_tile_t<kRing, 1, 1>(la, ra, st);
+    else if (ne == 2) launch_tile_t<kRing, 1, 2>(la, ra, st);
+    else launch_tile_t<kRing, 1, 4>(la, ra, st);
   }
 }
 
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   LaunchArgs la;
   TSG_TRY(build_step(c, s, base, cnt, &la));
-  if (la.narrow) {
+  if (la.tile) {
     switch (c.ring) {
       case TSG_RING_OR_AND:
-        launch_narrow_t<TSG_RING_OR_AND, true, true>(la, c.ra, c.stream);
+        launch_tile_ring<TSG_RING_OR_AND>(la, c.ra, c.stream);
         break;
       case TSG_RING_U64:
-        launch_narrow_ring<TSG_RING_U64>(la, c.ra, c.stream);
+        launch_tile_ring<TSG_RING_U64>(la, c.ra, c.stream);
         break;
       default:
-        launch_narrow_ring<TSG_RING_MODP>(la, c.ra, c.stream);
+        launch_tile_ring<TSG_RING_MODP>(la, c.ra, c.stream);
         break;
     }
     TSG_CUDA_TRY(cudaGetLastError());
