@@ -60,7 +60,7 @@ typedef int32_t tsg_status;
 
 /* Arithmetic of a tree run (tsg_plan_run). */
 #define TSG_RING_OR_AND 0 /* uint8 {0,1}: out = OR_k (L AND R); the SAT-bit semiring */
-#define TSG_RING_MODP 1   /* uint32 residues mod odd primes < 2^31, one plane per prime */
+#define TSG_RING_MODP 1   /* uint32 residues mod odd primes in (2^31-2^26, 2^31), one plane each */
 #define TSG_RING_U64 2    /* uint64 with wrap-around: the count modulo 2^64 */
 
 #define TSG_MAX_PORTS 64  /* ports per operand of a per-step contraction */

@@ -53,4 +53,26 @@ __device__ __forceinline__ uint32_t barrett_reduce(uint64_t x, uint32_t p, uint6
   return (uint32_t)(r >= p ? r - p : r);
 }
 
+// Montgomery reduction (P. L. Montgomery, Math. Comp. 44, 1985) with R = 2^32 for an odd
+// p < 2^31: returns T * R^-1 mod p for T < p * 2^32, given pinv = -p^-1 mod 2^32.
+// m = T * pinv (mod 2^32) makes T + m * p divisible by 2^32; the quotient is < 2p.
+__device__ __forceinline__ uint32_t mont_redc(uint64_t T, uint32_t p, uint32_t pinv) {
+  const uint32_t m = (uint32_t)T * pinv;
+  const uint32_t t = (uint32_t)((T + (uint64_t)m * p) >> 32);
+  return t >= p ? t - p : t;
+}
+
+// x mod p for x < 32 * 2^31 and p = 2^31 - d with d < 2^10: x = q * 2^31 + s gives
+// x - q * p = q * d + s < 2p, so one conditional subtraction finishes.
+__device__ __forceinline__ uint32_t small_mod(uint64_t x, uint32_t p) {
+  const uint64_t q = x >> 31;
+  const uint64_t r = x - q * (uint64_t)p;
+  return (uint32_t)(r >= p ? r - p : r);
+}
+
+__device__ __forceinline__ uint32_t add_mod(uint32_t a, uint32_t b, uint32_t p) {
+  const uint32_t s = a + b;  // a, b < p < 2^31: no wrap
+  return s >= p ? s - p : s;
+}
+
 }  // namespace tsg

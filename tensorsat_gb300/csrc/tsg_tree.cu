@@ -49,11 +49,27 @@ struct StepArgs {
   BitMap lt, lk, rt, rk;
 };
 
+// Residues mod p are kept in Montgomery form (x * 2^32 mod p) in every intermediate; the
+// root reduction converts back, so results are plain residues.
 struct RingArgs {
   int32_t np;
   uint32_t p[TSG_MAX_PRIMES];
-  uint64_t m[TSG_MAX_PRIMES];  // Barrett constants floor((2^64-1)/p)
+  uint64_t m[TSG_MAX_PRIMES];     // Barrett constants floor((2^64-1)/p)
+  uint32_t pinv[TSG_MAX_PRIMES];  // -p^-1 mod 2^32
+  uint32_t r1[TSG_MAX_PRIMES];    // 2^32 mod p (Montgomery form of 1)
 };
+
+// Montgomery-form value of sum_k L*R for one output and prime, from the 64-bit sum of
+// products `acc` (operands: plain 0/1 for leaves, Montgomery residues otherwise):
+//   both leaves:   acc is a plain count <= 16      -> acc * (2^32 mod p) mod p
+//   one leaf:      acc is a sum of <= 16 residues  -> reduce the small multiple
+//   no leaf:       acc < 2 p^2 (two products)      -> Montgomery reduction
+__device__ __forceinline__ uint32_t mont_finish(uint64_t acc, int leaves, const RingArgs& ring,
+                                                int p) {
+  if (leaves == 2) return small_mod(acc * ring.r1[p], ring.p[p]);
+  if (leaves == 1) return small_mod(acc, ring.p[p]);
+  return mont_redc(acc, ring.p[p], ring.pinv[p]);
+}
 
 __device__ __forceinline__ uint64_t scatter_bits(const BitMap& m, uint64_t x) {
   uint64_t r = 0;
@@ -96,22 +112,22 @@ __global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArg
       }
       reinterpret_cast<uint64_t*>(a.out)[t] = acc;
     } else {
-      uint64_t acc[TSG_MAX_PRIMES] = {0, 0, 0, 0};
+      // Montgomery residues; products of two residues are reduced pairwise (2 p^2 < p 2^32)
+      constexpr int leaves = (kLLeaf ? 1 : 0) + (kRLeaf ? 1 : 0);
+      uint32_t acc[TSG_MAX_PRIMES] = {0, 0, 0, 0};
+      uint64_t part[TSG_MAX_PRIMES] = {0, 0, 0, 0};
       for (uint64_t kk = 0; kk < nk; ++kk) {
         const uint64_t lko = lo + scatter_bits(a.lk, kk);
         const uint64_t rko = ro + scatter_bits(a.rk, kk);
-        if constexpr (kLLeaf && kRLeaf) {
-          const uint64_t v = (uint64_t)(a.lhs[lko] & a.rhs[rko]);
 #pragma unroll
-          for (int p = 0; p < TSG_MAX_PRIMES; ++p) acc[p] += v;
-        } else {
-#pragma unroll
-          for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
-            if (p < ring.np) {
-              const uint64_t l = load_elem<kLLeaf, uint32_t>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane));
-              const uint64_t r = load_elem<kRLeaf, uint32_t>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane));
-              // acc < p < 2^31 and l * r < 2^62, so the sum stays below 2^63
-              acc[p] = barrett_reduce(acc[p] + l * r, ring.p[p], ring.m[p]);
+        for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
+          if (p < ring.np) {
+            const uint32_t l = load_elem<kLLeaf, uint32_t>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane));
+            const uint32_t r = load_elem<kRLeaf, uint32_t>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane));
+            part[p] += (uint64_t)l * r;
+            if (leaves == 0 ? (kk & 1) : ((kk & 15) == 15)) {
+              acc[p] = add_mod(acc[p], mont_finish(part[p], leaves, ring, p), ring.p[p]);
+              part[p] = 0;
             }
           }
         }
@@ -119,7 +135,8 @@ __global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArg
       uint32_t* out = reinterpret_cast<uint32_t*>(a.out);
 #pragma unroll
       for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
-        if (p < ring.np) out[t + p * a.o_plane] = barrett_reduce(acc[p], ring.p[p], ring.m[p]);
+        if (p < ring.np)
+          out[t + p * a.o_plane] = add_mod(acc[p], mont_finish(part[p], leaves, ring, p), ring.p[p]);
       }
     }
   }
@@ -235,7 +252,7 @@ __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, V
 }
 
 template <int kRing, int V, int NE>
-__global__ void __launch_bounds__(kThreads) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
+__global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
   using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
             typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
   using VT = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
@@ -253,14 +270,22 @@ __global__ void __launch_bounds__(kThreads) tree_step_tile_kernel(TileArgs a, Ri
   const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
   const TileOperand& L = a.op[0];
   const TileOperand& R = a.op[1];
-  for (int p = 0; p < np; ++p) {
+  const int leaves = L.leaf + R.leaf;
+  // planes unrolled so every ring constant is indexed by a compile-time prime number
+#pragma unroll
+  for (int p = 0; p < (kRing == TSG_RING_MODP ? TSG_MAX_PRIMES : 1); ++p) {
+    if (p >= np) break;
     const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
     const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
     AT acc[NE][V];
+    uint32_t done[NE][V];  // MODP: reduced chunks (Montgomery form) for n_k > 2
 #pragma unroll
     for (int e = 0; e < NE; ++e)
 #pragma unroll
-      for (int j = 0; j < V; ++j) acc[e][j] = 0;
+      for (int j = 0; j < V; ++j) {
+        acc[e][j] = 0;
+        done[e][j] = 0;
+      }
     for (int kk = 0; kk < a.n_k; ++kk) {
       VT lv[V], rv[V];
       if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[kk], lv);
@@ -279,12 +304,16 @@ __global__ void __launch_bounds__(kThreads) tree_step_tile_kernel(TileArgs a, Ri
         }
       }
       if constexpr (kRing == TSG_RING_MODP) {
-        // residues < 2^31: three products plus a reduced value stay below 2^64
-        if (kk % 3 == 2) {
+        // two Montgomery products stay below p 2^32: reduce every pair of summed terms
+        if (leaves == 0 && (kk & 1) && kk + 1 < a.n_k) {
 #pragma unroll
           for (int e = 0; e < NE; ++e)
 #pragma unroll
-            for (int j = 0; j < V; ++j) acc[e][j] = barrett_reduce(acc[e][j], ring.p[p], ring.m[p]);
+            for (int j = 0; j < V; ++j) {
+              done[e][j] = add_mod(done[e][j], mont_redc(acc[e][j], ring.p[p], ring.pinv[p]),
+                                   ring.p[p]);
+              acc[e][j] = 0;
+            }
         }
       }
     }
@@ -314,7 +343,8 @@ __global__ void __launch_bounds__(kThreads) tree_step_tile_kernel(TileArgs a, Ri
         uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane;
         uint32_t r[V];
 #pragma unroll
-        for (int j = 0; j < V; ++j) r[j] = barrett_reduce(acc[e][j], ring.p[p], ring.m[p]);
+        for (int j = 0; j < V; ++j)
+          r[j] = add_mod(done[e][j], mont_finish(acc[e][j], leaves, ring, p), ring.p[p]);
         if (V == 4 && a.o_contig) {
           *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1 % V], r[2 % V], r[3 % V]);
         } else {
@@ -371,9 +401,12 @@ __global__ void __launch_bounds__(kThreads)
           uint64_t* r = reinterpret_cast<uint64_t*>(result);
           r[e] = accumulate ? r[e] + v : v;
         } else {
+          // v < 256 p: reduce, then leave Montgomery form (REDC of x < p is x R^-1 mod p)
           uint32_t* r = reinterpret_cast<uint32_t*>(result) + p * entries;
-          if (accumulate) v += r[e];
-          r[e] = barrett_reduce(v, ring.p[p], ring.m[p]);
+          uint64_t plain = mont_redc(barrett_reduce(v, ring.p[p], ring.m[p]), ring.p[p],
+                                     ring.pinv[p]);
+          if (accumulate) plain += r[e];
+          r[e] = barrett_reduce(plain, ring.p[p], ring.m[p]);
         }
       }
       __syncthreads();
@@ -1035,10 +1068,15 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
     if (!primes) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: MODP needs primes");
     ra.np = num_primes;
     for (int p = 0; p < num_primes; ++p) {
-      if (primes[p] < 3 || primes[p] >= (1u << 31) || (primes[p] % 2) == 0)
-        return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: moduli must be odd and in [3, 2^31)");
+      if (primes[p] <= (1u << 31) - (1u << 26) || primes[p] >= (1u << 31) || (primes[p] % 2) == 0)
+        return fail(TSG_ERR_INVALID_ARGUMENT,
+                    "plan_run: moduli must be odd and in (2^31 - 2^26, 2^31)");
       ra.p[p] = primes[p];
       ra.m[p] = UINT64_MAX / primes[p];
+      uint32_t inv = primes[p];  // Newton iteration for p^-1 mod 2^32 (5 steps: 2^32 bits)
+      for (int it = 0; it < 5; ++it) inv *= 2u - primes[p] * inv;
+      ra.pinv[p] = 0u - inv;
+      ra.r1[p] = (uint32_t)((1ull << 32) % primes[p]);
     }
   }
   const Layout* lay;
