@@ -158,6 +158,7 @@ constexpr int kMaxNarrowRuns = 32;
 constexpr int kModeGather = 0;
 constexpr int kModeContig = 1;
 constexpr int kModeBcast = 2;
+constexpr int kModePair = 3;  // two distinct offsets: 0 and tab[3]; pair_sel picks per position
 constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
 constexpr int kMaxK = 16;  // summed combinations kept in tables (k <= 4)
 
@@ -177,7 +178,8 @@ struct TileOperand {
   uint32_t tab[4];        // offsets of the V consecutive F positions
   uint32_t e_off[kMaxE];  // offsets of the E combinations
   uint32_t k_off[kMaxK];  // offsets of the summed combinations
-  int32_t mode;           // kModeContig / kModeBcast / kModeGather for the V positions
+  int32_t mode;           // kModeContig / kModeBcast / kModePair / kModeGather
+  int32_t pair_sel;       // kModePair: bit j set when position j reads offset tab[3]
   int32_t has_e;          // carries E bits (reloaded per E combination)
   int32_t leaf;           // uint8 leaf (widened on load)
 };
@@ -215,6 +217,10 @@ __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, V
       const VT x = (VT)base[off];
 #pragma unroll
       for (int j = 0; j < V; ++j) out[j] = x;
+    } else if (V == 4 && op.mode == kModePair) {
+      const VT x0 = (VT)base[off], x1 = (VT)base[off + op.tab[3]];
+#pragma unroll
+      for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
     } else {
 #pragma unroll
       for (int j = 0; j < V; ++j) out[j] = (VT)base[off + op.tab[j]];
@@ -245,6 +251,10 @@ __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, V
     const VT x = (VT)p[off];
 #pragma unroll
     for (int j = 0; j < V; ++j) out[j] = x;
+  } else if (V == 4 && op.mode == kModePair) {
+    const VT x0 = (VT)p[off], x1 = (VT)p[off + op.tab[3]];
+#pragma unroll
+    for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
   } else {
 #pragma unroll
     for (int j = 0; j < V; ++j) out[j] = (VT)p[off + op.tab[j]];
@@ -861,6 +871,19 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
     // (leaf offsets are the caller's; workspace buffers are 256-byte aligned)
     if (contig && (op.base & 3) != 0) contig = false;
     op.mode = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
+    if (op.mode == kModeGather && v == 4) {
+      // exactly two distinct offsets, 0 and tab[3] (one of the two fastest output bits)
+      bool pair = op.tab[0] == 0 && op.tab[3] != 0;
+      int sel = 0;
+      for (int j = 0; j < v && pair; ++j) {
+        if (op.tab[j] == op.tab[3]) sel |= 1 << j;
+        else if (op.tab[j] != 0) pair = false;
+      }
+      if (pair) {
+        op.mode = kModePair;
+        op.pair_sel = sel;
+      }
+    }
     op.has_e = ep.empty() ? 0 : 1;
     for (int e = 0; e < ne; ++e) op.e_off[e] = (uint32_t)scatter_pairs(ep, e);
     for (int kk = 0; kk < t->n_k; ++kk) op.k_off[kk] = (uint32_t)scatter_pairs(d[o].kp, kk);

@@ -351,10 +351,15 @@ def optimize(net: Network, *, target_bits: int | None = 26, trials: int = 8, see
 class SlicedPlan:
     """A tree, its sliced wires, and the wire order (layout) of every node.
 
-    Leaves keep their given wire order (sliced wires included); an intermediate stores its
-    non-sliced wires as ``new wires of the smaller operand`` followed by ``kept wires of
-    the larger operand in its order``, so the large operand's low (fastest) bits stay the
-    result's low bits and its reads coalesce.
+    Leaves keep their given wire order (sliced wires included). Intermediates are laid
+    out top down, each from its consumer's needs: the root follows the output wires; in a
+    step whose result order is fixed, the larger operand (the one carrying more result
+    wires) takes the result's order for its kept wires, with its summed wires above them;
+    the smaller operand takes ``new wires (not in the larger) | summed wires | shared
+    wires in the result's order``. Along a chain of steps the lowest bits are therefore
+    the longest-lived wires, so the large operand reads coalesce and match the output
+    (vector loads), and the small operand either follows the same low wires or does not
+    carry them (one load serves several outputs).
     """
 
     tree: ContractionTree
@@ -366,22 +371,36 @@ class SlicedPlan:
         t = self.tree
         L = t.num_leaves
         sl = frozenset(self.sliced)
-        order: list[tuple[int, ...]] = [tuple(ws) for ws in self.leaf_wires]
-        for s, (a, b) in enumerate(t.steps):
-            res = t.node_wires[L + s] - sl
-            oa = [w for w in order[a] if w not in sl]
-            ob = [w for w in order[b] if w not in sl]
-            big, small = (oa, ob) if len(oa) >= len(ob) else (ob, oa)
-            if s == len(t.steps) - 1:
-                # the root is laid out in the order of the output wires
-                outs = [w for w in dict.fromkeys(t.out_wires)]
-                order.append(tuple(outs))
-                continue
-            kept_big = [w for w in big if w in res]
-            new_small = [w for w in small if w in res and w not in big]
-            order.append(tuple(new_small + kept_big))
-            assert frozenset(order[-1]) == res
-        self.node_order = order
+        n_nodes = L + len(t.steps)
+        order: list[tuple[int, ...] | None] = [None] * n_nodes
+        for l, ws in enumerate(self.leaf_wires):
+            order[l] = tuple(ws)
+        if t.steps:
+            order[n_nodes - 1] = tuple(dict.fromkeys(t.out_wires))
+        for s in range(len(t.steps) - 1, -1, -1):
+            out_order = [w for w in order[L + s] if w not in sl]
+            out_set = frozenset(out_order)
+            a, b = t.steps[s]
+            wa = t.node_wires[a] - sl
+            wb = t.node_wires[b] - sl
+            ca = len(wa & out_set)
+            cb = len(wb & out_set)
+            big, small = (a, b) if (ca, len(wa)) >= (cb, len(wb)) else (b, a)
+            wbig = wa if big == a else wb
+            wsmall = wb if big == a else wa
+            summed = sorted((wa | wb) - out_set)
+            if big >= L:
+                kept = [w for w in out_order if w in wbig]
+                top = [w for w in summed if w in wbig]
+                order[big] = tuple(top + kept)
+                assert frozenset(order[big]) == wbig
+            if small >= L:
+                new = [w for w in out_order if w in wsmall and w not in wbig]
+                mid = [w for w in summed if w in wsmall]
+                shared = [w for w in out_order if w in wsmall and w in wbig]
+                order[small] = tuple(new + mid + shared)
+                assert frozenset(order[small]) == wsmall
+        self.node_order = [o if o is not None else () for o in order]
 
     @property
     def num_slices(self) -> int:
