@@ -175,7 +175,7 @@ struct TileOperand {
   uint64_t plane;         // residue-plane stride (elements); 0 for leaves
   NarrowMap f_lo, f_hi;   // F bits below / at or above tile_bits -> operand bits
   BitMap g;               // slice-slot bits -> operand bits
-  uint32_t tab[4];        // offsets of the V consecutive F positions
+  uint32_t tab[16];       // offsets of the V consecutive F positions
   uint32_t e_off[kMaxE];  // offsets of the E combinations
   uint32_t k_off[kMaxK];  // offsets of the summed combinations
   int32_t mode;           // kModeContig / kModeBcast / kModePair / kModeGather
@@ -190,7 +190,7 @@ struct TileArgs {
   uint64_t o_plane;
   uint32_t n_out;          // outputs per slice
   NarrowMap of_lo, of_hi;  // F bits -> output bit positions
-  uint32_t o_tab[4];
+  uint32_t o_tab[16];
   uint32_t o_e[kMaxE];
   int32_t tile_bits;
   int32_t n_k;             // summed combinations (2^k)
@@ -209,7 +209,12 @@ template <typename T, typename VT, int V>
 __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, VT (&out)[V]) {
   const uint8_t* base = op.ptr;
   if (op.leaf) {
-    if (V == 4 && op.mode == kModeContig) {
+    if (V == 16 && op.mode == kModeContig) {
+      const uint4 w = *reinterpret_cast<const uint4*>(base + off);
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int j = 0; j < V; ++j) out[j] = (VT)((ws[j / 4] >> (8 * (j % 4))) & 0xff);
+    } else if (V == 4 && op.mode == kModeContig) {
       const uint32_t w = *reinterpret_cast<const uint32_t*>(base + off);
 #pragma unroll
       for (int j = 0; j < V; ++j) out[j] = (VT)((w >> (8 * j)) & 0xff);
@@ -228,7 +233,14 @@ __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, V
     return;
   }
   const T* p = reinterpret_cast<const T*>(base);
-  if (V == 4 && op.mode == kModeContig) {
+  if (V == 16 && op.mode == kModeContig) {
+    if constexpr (sizeof(T) == 1) {
+      const uint4 w = *reinterpret_cast<const uint4*>(p + off);
+      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int j = 0; j < V; ++j) out[j] = (VT)((ws[j / 4] >> (8 * (j % 4))) & 0xff);
+    }
+  } else if (V == 4 && op.mode == kModeContig) {
     if constexpr (sizeof(T) == 1) {
       const uint32_t w = *reinterpret_cast<const uint32_t*>(p + off);
 #pragma unroll
@@ -261,12 +273,51 @@ __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, V
   }
 }
 
-template <int kRing, int V, int NE>
+// OR-AND values are 0/1 bytes, so four positions packed in a 32-bit word combine with
+// word-wide AND / OR. Loads `V` positions (V = 4 or 16) as V/4 packed words.
+template <int V>
+__device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t off,
+                                                 uint32_t (&w)[V / 4]) {
+  const uint8_t* base = op.ptr;
+  if (op.mode == kModeContig) {
+    if constexpr (V == 16) {
+      const uint4 x = *reinterpret_cast<const uint4*>(base + off);
+      w[0] = x.x;
+      w[1 % (V / 4)] = x.y;
+      w[2 % (V / 4)] = x.z;
+      w[3 % (V / 4)] = x.w;
+    } else {
+      w[0] = *reinterpret_cast<const uint32_t*>(base + off);
+    }
+  } else if (op.mode == kModeBcast) {
+    const uint32_t x = (uint32_t)base[off] * 0x01010101u;
+#pragma unroll
+    for (int i = 0; i < V / 4; ++i) w[i] = x;
+  } else if (V == 4 && op.mode == kModePair) {
+    const uint32_t x0 = base[off], x1 = base[off + op.tab[3]];
+    uint32_t r = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) r |= (((op.pair_sel >> j) & 1) ? x1 : x0) << (8 * j);
+    w[0] = r;
+  } else {
+#pragma unroll
+    for (int i = 0; i < V / 4; ++i) {
+      uint32_t r = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) r |= (uint32_t)base[off + op.tab[4 * i + j]] << (8 * j);
+      w[i] = r;
+    }
+  }
+}
+
+template <int kRing, int V, int NE, int NK>
 __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
   using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
             typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
   using VT = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
-  using AT = typename std::conditional<kRing == TSG_RING_OR_AND, uint32_t, uint64_t>::type;
+  using AT = uint64_t;
+  constexpr bool kPacked = (kRing == TSG_RING_OR_AND) && (V % 4 == 0);
+  constexpr int W = kPacked ? V / 4 : 1;  // packed words per operand (OR-AND)
   const uint32_t g = blockIdx.y;
   const uint32_t f_hi = blockIdx.x << a.tile_bits;
   const uint32_t f_lo = threadIdx.x * (uint32_t)V;
@@ -281,85 +332,140 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
   const TileOperand& L = a.op[0];
   const TileOperand& R = a.op[1];
   const int leaves = L.leaf + R.leaf;
+  // NK > 0: the summed combinations are unrolled and the operand without E bits is loaded
+  // once for all of them before the E loop; NK == 0: runtime count, loads in the loop
+  constexpr int KU = NK > 0 ? NK : 1;
+  const int nk = NK > 0 ? NK : a.n_k;
   // planes unrolled so every ring constant is indexed by a compile-time prime number
 #pragma unroll
   for (int p = 0; p < (kRing == TSG_RING_MODP ? TSG_MAX_PRIMES : 1); ++p) {
     if (p >= np) break;
     const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
     const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
-    AT acc[NE][V];
-    uint32_t done[NE][V];  // MODP: reduced chunks (Montgomery form) for n_k > 2
+    if constexpr (kPacked) {
+      uint32_t lpre[KU][W], rpre[KU][W];
+      if (NK > 0) {
 #pragma unroll
-    for (int e = 0; e < NE; ++e)
-#pragma unroll
-      for (int j = 0; j < V; ++j) {
-        acc[e][j] = 0;
-        done[e][j] = 0;
+        for (int ku = 0; ku < KU; ++ku) {
+          if (!L.has_e) tile_load_packed<V>(L, lp + L.k_off[ku], lpre[ku]);
+          if (!R.has_e) tile_load_packed<V>(R, rp + R.k_off[ku], rpre[ku]);
+        }
       }
-    for (int kk = 0; kk < a.n_k; ++kk) {
-      VT lv[V], rv[V];
-      if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[kk], lv);
-      if (!R.has_e) tile_load<T, VT, V>(R, rp + R.k_off[kk], rv);
 #pragma unroll
       for (int e = 0; e < NE; ++e) {
-        if (L.has_e) tile_load<T, VT, V>(L, lp + L.e_off[e] + L.k_off[kk], lv);
-        if (R.has_e) tile_load<T, VT, V>(R, rp + R.e_off[e] + R.k_off[kk], rv);
+        uint32_t acc[W];
 #pragma unroll
-        for (int j = 0; j < V; ++j) {
-          if constexpr (kRing == TSG_RING_OR_AND) {
-            acc[e][j] |= lv[j] & rv[j];
-          } else {
-            acc[e][j] += (AT)lv[j] * (AT)rv[j];
+        for (int i = 0; i < W; ++i) acc[i] = 0;
+        for (int kk0 = 0; kk0 < nk; kk0 += KU) {
+#pragma unroll
+          for (int ku = 0; ku < KU; ++ku) {
+            const int kk = kk0 + ku;
+            uint32_t lw[W], rw[W];
+            if (L.has_e) tile_load_packed<V>(L, lp + L.e_off[e] + L.k_off[kk], lw);
+            else if (NK > 0) {
+#pragma unroll
+              for (int i = 0; i < W; ++i) lw[i] = lpre[ku][i];
+            } else tile_load_packed<V>(L, lp + L.k_off[kk], lw);
+            if (R.has_e) tile_load_packed<V>(R, rp + R.e_off[e] + R.k_off[kk], rw);
+            else if (NK > 0) {
+#pragma unroll
+              for (int i = 0; i < W; ++i) rw[i] = rpre[ku][i];
+            } else tile_load_packed<V>(R, rp + R.k_off[kk], rw);
+#pragma unroll
+            for (int i = 0; i < W; ++i) acc[i] |= lw[i] & rw[i];
           }
         }
-      }
-      if constexpr (kRing == TSG_RING_MODP) {
-        // two Montgomery products stay below p 2^32: reduce every pair of summed terms
-        if (leaves == 0 && (kk & 1) && kk + 1 < a.n_k) {
+        const uint64_t oe = oo + a.o_e[e];
+        if (a.o_contig) {
+          if constexpr (V == 16) {
+            *reinterpret_cast<uint4*>(a.out + oe) =
+                make_uint4(acc[0], acc[1 % W], acc[2 % W], acc[3 % W]);
+          } else {
+            *reinterpret_cast<uint32_t*>(a.out + oe) = acc[0];
+          }
+        } else {
 #pragma unroll
-          for (int e = 0; e < NE; ++e)
+          for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = (acc[j / 4] >> (8 * (j % 4))) & 0xff;
+        }
+      }
+    } else {
+      VT lpre[KU][V], rpre[KU][V];
+      if (NK > 0) {
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku) {
+          if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[ku], lpre[ku]);
+          if (!R.has_e) tile_load<T, VT, V>(R, rp + R.k_off[ku], rpre[ku]);
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        AT acc[V];
+        uint32_t done[V];  // MODP: reduced chunks (Montgomery form) when more than 2 sums
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          acc[j] = 0;
+          done[j] = 0;
+        }
+        for (int kk0 = 0; kk0 < nk; kk0 += KU) {
+#pragma unroll
+          for (int ku = 0; ku < KU; ++ku) {
+            const int kk = kk0 + ku;
+            VT lv[V], rv[V];
+            if (L.has_e) tile_load<T, VT, V>(L, lp + L.e_off[e] + L.k_off[kk], lv);
+            else if (NK > 0) {
+#pragma unroll
+              for (int j = 0; j < V; ++j) lv[j] = lpre[ku][j];
+            } else tile_load<T, VT, V>(L, lp + L.k_off[kk], lv);
+            if (R.has_e) tile_load<T, VT, V>(R, rp + R.e_off[e] + R.k_off[kk], rv);
+            else if (NK > 0) {
+#pragma unroll
+              for (int j = 0; j < V; ++j) rv[j] = rpre[ku][j];
+            } else tile_load<T, VT, V>(R, rp + R.k_off[kk], rv);
 #pragma unroll
             for (int j = 0; j < V; ++j) {
-              done[e][j] = add_mod(done[e][j], mont_redc(acc[e][j], ring.p[p], ring.pinv[p]),
-                                   ring.p[p]);
-              acc[e][j] = 0;
+              if constexpr (kRing == TSG_RING_OR_AND) {
+                acc[j] |= lv[j] & rv[j];
+              } else {
+                acc[j] += (AT)lv[j] * (AT)rv[j];
+              }
             }
+            if constexpr (kRing == TSG_RING_MODP) {
+              // two Montgomery products stay below p 2^32: reduce every pair of sums
+              if (leaves == 0 && (kk & 1) && kk + 1 < nk) {
+#pragma unroll
+                for (int j = 0; j < V; ++j) {
+                  done[j] = add_mod(done[j], mont_redc(acc[j], ring.p[p], ring.pinv[p]), ring.p[p]);
+                  acc[j] = 0;
+                }
+              }
+            }
+          }
         }
-      }
-    }
+        const uint64_t oe = oo + a.o_e[e];
+        if constexpr (kRing == TSG_RING_OR_AND) {
 #pragma unroll
-    for (int e = 0; e < NE; ++e) {
-      const uint64_t oe = oo + a.o_e[e];
-      if constexpr (kRing == TSG_RING_OR_AND) {
-        if (V == 4 && a.o_contig) {
-          uint32_t w = 0;
+          for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = acc[j] ? 1 : 0;
+        } else if constexpr (kRing == TSG_RING_U64) {
+          uint64_t* out = reinterpret_cast<uint64_t*>(a.out);
+          if (V == 4 && a.o_contig) {
+            reinterpret_cast<ulonglong2*>(out + oe)[0] = make_ulonglong2(acc[0], acc[1 % V]);
+            reinterpret_cast<ulonglong2*>(out + oe)[1] = make_ulonglong2(acc[2 % V], acc[3 % V]);
+          } else {
 #pragma unroll
-          for (int j = 0; j < V; ++j) w |= (acc[e][j] ? 1u : 0u) << (8 * j);
-          *reinterpret_cast<uint32_t*>(a.out + oe) = w;
+            for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = acc[j];
+          }
         } else {
+          uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane;
+          uint32_t r[V];
 #pragma unroll
-          for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = acc[e][j] ? 1 : 0;
-        }
-      } else if constexpr (kRing == TSG_RING_U64) {
-        uint64_t* out = reinterpret_cast<uint64_t*>(a.out);
-        if (V == 4 && a.o_contig) {
-          reinterpret_cast<ulonglong2*>(out + oe)[0] = make_ulonglong2(acc[e][0], acc[e][1 % V]);
-          reinterpret_cast<ulonglong2*>(out + oe)[1] = make_ulonglong2(acc[e][2 % V], acc[e][3 % V]);
-        } else {
+          for (int j = 0; j < V; ++j)
+            r[j] = add_mod(done[j], mont_finish(acc[j], leaves, ring, p), ring.p[p]);
+          if (V == 4 && a.o_contig) {
+            *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1 % V], r[2 % V], r[3 % V]);
+          } else {
 #pragma unroll
-          for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = acc[e][j];
-        }
-      } else {
-        uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane;
-        uint32_t r[V];
-#pragma unroll
-        for (int j = 0; j < V; ++j)
-          r[j] = add_mod(done[e][j], mont_finish(acc[e][j], leaves, ring, p), ring.p[p]);
-        if (V == 4 && a.o_contig) {
-          *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1 % V], r[2 % V], r[3 % V]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
+            for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
+          }
         }
       }
     }
@@ -768,7 +874,7 @@ uint64_t scatter_pairs(const std::vector<std::pair<int, int>>& pairs, uint64_t x
 }
 
 struct TileShape {
-  int v, ne;          // template parameters
+  int v, ne, nk;      // template parameters (nk 0: runtime summed count)
   unsigned threads;
   uint64_t tiles;
 };
@@ -785,7 +891,7 @@ struct LaunchArgs {
 // Builds the tile form of step s from the operand descriptions; sets *ok = false when the
 // step is outside what the tile kernel handles (it then runs the general kernel).
 tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs& a,
-                      uint64_t cnt, TileArgs* t, TileShape* shape, bool* ok) {
+                      uint64_t cnt, int ring, TileArgs* t, TileShape* shape, bool* ok) {
   std::memset(t, 0, sizeof(*t));
   *ok = st.out_bits <= 30 && st.k_bits <= 4 && cnt <= 65535;
   if (!*ok) return TSG_OK;
@@ -805,7 +911,25 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
       if (std::find(ebits.begin(), ebits.end(), i) == ebits.end()) fbits.push_back(i);
   }
   const int nf = (int)fbits.size();
-  const int v = nf >= 2 ? 4 : 1;
+  int v = nf >= 2 ? 4 : 1;
+  if (ring == TSG_RING_OR_AND && nf >= 4) {
+    // 16 byte-wide positions when every operand and the output take the 4 fastest F bits
+    // as their own 4 fastest bits (vector load) or not at all (broadcast)
+    bool ok16 = true;
+    for (int b = 0; b < 4 && ok16; ++b) ok16 = fbits[b] == b;
+    for (int o = 0; o < 2 && ok16; ++o) {
+      int carried = 0;
+      for (int b = 0; b < 4; ++b) {
+        const int p = st.pos[o][fbits[b]];
+        if (p >= 0) {
+          carried++;
+          ok16 = ok16 && p == b;
+        }
+      }
+      ok16 = ok16 && (carried == 0 || carried == 4) && (carried == 0 || (d[o].base & 15) == 0);
+    }
+    if (ok16) v = 16;
+  }
   const int ne = 1 << ebits.size();
   uint64_t positions = (uint64_t)1 << nf;           // F positions per slice
   uint64_t threads = std::min<uint64_t>(kThreads, positions / v);
@@ -814,6 +938,7 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   while (((uint64_t)1 << tile_bits) < threads * v) tile_bits++;
   shape->v = v;
   shape->ne = ne;
+  shape->nk = st.k_bits == 0 ? 1 : (st.k_bits == 1 ? 2 : 0);
   shape->threads = (unsigned)threads;
   shape->tiles = positions >> tile_bits;
   if (shape->tiles >= (1ull << 31)) {
@@ -832,7 +957,7 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   TSG_TRY(make_narrow(olo, &t->of_lo, ok));
   if (*ok) TSG_TRY(make_narrow(ohi, &t->of_hi, ok));
   if (!*ok) return TSG_OK;
-  bool ocontig = v == 4;
+  bool ocontig = v >= 4;
   for (int j = 0; j < v; ++j) {
     t->o_tab[j] = (uint32_t)scatter_pairs(olo, j);
     ocontig = ocontig && t->o_tab[j] == (uint32_t)j;
@@ -860,16 +985,16 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
       if (pr.second >= 32) *ok = false;
     if (!*ok) return TSG_OK;
     TSG_TRY(make_bitmap(d[o].gp, &op.g));
-    bool contig = v == 4, bcast = true;
+    bool contig = v >= 4, bcast = true;
     for (int j = 0; j < v; ++j) {
       op.tab[j] = (uint32_t)scatter_pairs(lo, j);
       contig = contig && op.tab[j] == (uint32_t)j;
       bcast = bcast && op.tab[j] == 0;
     }
-    // vector loads need every start offset to be a multiple of 4 elements: output bits
-    // 0-1 occupy the operand's bits 0-1, so only the constant part can break that
-    // (leaf offsets are the caller's; workspace buffers are 256-byte aligned)
-    if (contig && (op.base & 3) != 0) contig = false;
+    // vector loads need every start offset to be a multiple of V elements: the fastest
+    // output bits occupy the operand's fastest bits, so only the constant part can break
+    // that (leaf offsets are the caller's; workspace buffers are 256-byte aligned)
+    if (contig && (op.base & (uint64_t)(v - 1)) != 0) contig = false;
     op.mode = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
     if (op.mode == kModeGather && v == 4) {
       // exactly two distinct offsets, 0 and tab[3] (one of the two fastest output bits)
@@ -912,7 +1037,7 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
   const TileShape& sh = la.shape;
   const int gbits = bit_width(la.cnt - 1);
   const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
-  const int vbits = sh.v == 4 ? 2 : 0;  // thread positions are multiples of V
+  const int vbits = sh.v == 16 ? 4 : (sh.v == 4 ? 2 : 0);  // thread positions: multiples of V
   if ((uint64_t)sh.threads * sh.v != (1ull << t.tile_bits))
     return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: threads x V is not the tile size");
   for (int o = 0; o < 2; ++o) {
@@ -965,30 +1090,46 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   }
   TSG_TRY(check_step_bounds(c, s, a, la->is_leaf));
   bool ok = false;
-  TSG_TRY(build_tile(st, d, a, la->cnt, &la->t, &la->shape, &ok));
+  TSG_TRY(build_tile(st, d, a, la->cnt, c.ring, &la->t, &la->shape, &ok));
   la->tile = ok;
   if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
   return TSG_OK;
 }
 
-template <int kRing, int V, int NE>
+template <int kRing, int V, int NE, int NK>
 void launch_tile_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
   dim3 grid((unsigned)la.shape.tiles, (unsigned)la.cnt);
-  tree_step_tile_kernel<kRing, V, NE><<<grid, la.shape.threads, 0, st>>>(la.t, ra);
+  tree_step_tile_kernel<kRing, V, NE, NK><<<grid, la.shape.threads, 0, st>>>(la.t, ra);
+}
+
+template <int kRing, int V, int NE>
+void launch_tile_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  switch (la.shape.nk) {
+    case 1: launch_tile_t<kRing, V, NE, 1>(la, ra, st); break;
+    case 2: launch_tile_t<kRing, V, NE, 2>(la, ra, st); break;
+    default: launch_tile_t<kRing, V, NE, 0>(la, ra, st); break;
+  }
+}
+
+template <int kRing, int V>
+void launch_tile_ne(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  switch (la.shape.ne) {
+    case 1: launch_tile_nk<kRing, V, 1>(la, ra, st); break;
+    case 2: launch_tile_nk<kRing, V, 2>(la, ra, st); break;
+    default: launch_tile_nk<kRing, V, 4>(la, ra, st); break;
+  }
 }
 
 template <int kRing>
 void launch_tile_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  const int v = la.shape.v, ne = la.shape.ne;
-  if (v == 4) {
-    if (ne == 1) launch_tile_t<kRing, 4, 1>(la, ra, st);
-    else if (ne == 2) launch_tile_t<kRing, 4, 2>(la, ra, st);
-    else launch_tile_t<kRing, 4, 4>(la, ra, st);
-  } else {
-    if (ne == 1) launch_tile_t<kRing, 1, 1>(la, ra, st);
-    else if (ne == 2) launch_tile_t<kRing, 1, 2>(la, ra, st);
-    else launch_tile_t<kRing, 1, 4>(la, ra, st);
+  if constexpr (kRing == TSG_RING_OR_AND) {
+    if (la.shape.v == 16) {
+      launch_tile_ne<kRing, 16>(la, ra, st);
+      return;
+    }
   }
+  if (la.shape.v == 4) launch_tile_ne<kRing, 4>(la, ra, st);
+  else launch_tile_ne<kRing, 1>(la, ra, st);
 }
 
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
