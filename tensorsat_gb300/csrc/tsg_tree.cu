@@ -336,13 +336,10 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
   // once for all of them before the E loop; NK == 0: runtime count, loads in the loop
   constexpr int KU = NK > 0 ? NK : 1;
   const int nk = NK > 0 ? NK : a.n_k;
-  // planes unrolled so every ring constant is indexed by a compile-time prime number
-#pragma unroll
-  for (int p = 0; p < (kRing == TSG_RING_MODP ? TSG_MAX_PRIMES : 1); ++p) {
-    if (p >= np) break;
-    const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
-    const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
-    if constexpr (kPacked) {
+  if constexpr (kPacked) {
+    const uint64_t lp = xo[0];
+    const uint64_t rp = xo[1];
+    {
       uint32_t lpre[KU][W], rpre[KU][W];
       if (NK > 0) {
 #pragma unroll
@@ -388,17 +385,32 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
           for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = (acc[j / 4] >> (8 * (j % 4))) & 0xff;
         }
       }
-    } else {
-      VT lpre[KU][V], rpre[KU][V];
-      if (NK > 0) {
+    }
+  }
+  if constexpr (!kPacked) {
+    // planes outermost; the E-free operand of plane p+1 is loaded while plane p is being
+    // combined (two planes of loads in flight per thread), and reused across E values
+    constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
+    VT lcur[KU][V], rcur[KU][V], lnxt[KU][V], rnxt[KU][V];
+    auto preload = [&](int p, VT (&lb)[KU][V], VT (&rb)[KU][V]) {
+      const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
+      const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
 #pragma unroll
-        for (int ku = 0; ku < KU; ++ku) {
-          if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[ku], lpre[ku]);
-          if (!R.has_e) tile_load<T, VT, V>(R, rp + R.k_off[ku], rpre[ku]);
-        }
+      for (int ku = 0; ku < KU; ++ku) {
+        if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[ku], lb[ku]);
+        if (!R.has_e) tile_load<T, VT, V>(R, rp + R.k_off[ku], rb[ku]);
       }
+    };
+    if (NK > 0) preload(0, lcur, rcur);
+#pragma unroll
+    for (int p = 0; p < PP; ++p) {
+      if (p >= np) break;
+      if (NK > 0 && p + 1 < np) preload(p + 1, lnxt, rnxt);
+      const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
+      const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
 #pragma unroll
       for (int e = 0; e < NE; ++e) {
+        const uint64_t oe = oo + a.o_e[e];
         AT acc[V];
         uint32_t done[V];  // MODP: reduced chunks (Montgomery form) when more than 2 sums
 #pragma unroll
@@ -414,12 +426,12 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
             if (L.has_e) tile_load<T, VT, V>(L, lp + L.e_off[e] + L.k_off[kk], lv);
             else if (NK > 0) {
 #pragma unroll
-              for (int j = 0; j < V; ++j) lv[j] = lpre[ku][j];
+              for (int j = 0; j < V; ++j) lv[j] = lcur[ku][j];
             } else tile_load<T, VT, V>(L, lp + L.k_off[kk], lv);
             if (R.has_e) tile_load<T, VT, V>(R, rp + R.e_off[e] + R.k_off[kk], rv);
             else if (NK > 0) {
 #pragma unroll
-              for (int j = 0; j < V; ++j) rv[j] = rpre[ku][j];
+              for (int j = 0; j < V; ++j) rv[j] = rcur[ku][j];
             } else tile_load<T, VT, V>(R, rp + R.k_off[kk], rv);
 #pragma unroll
             for (int j = 0; j < V; ++j) {
@@ -441,7 +453,6 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
             }
           }
         }
-        const uint64_t oe = oo + a.o_e[e];
         if constexpr (kRing == TSG_RING_OR_AND) {
 #pragma unroll
           for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = acc[j] ? 1 : 0;
@@ -467,6 +478,15 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
             for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
           }
         }
+      }
+      if (NK > 0) {
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku)
+#pragma unroll
+          for (int j = 0; j < V; ++j) {
+            lcur[ku][j] = lnxt[ku][j];
+            rcur[ku][j] = rnxt[ku][j];
+          }
       }
     }
   }
