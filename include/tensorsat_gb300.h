@@ -174,6 +174,36 @@ TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t
                              const uint32_t* primes, int64_t slice_begin,
                              int64_t slice_end, int64_t group_size);
 
+/* ---------------------------------------------------------------------------------
+ * Allocation-free variant (no counterpart in the reference).
+ *
+ * tsg_plan_run with its scratch taken from a 64 MiB array in device global memory that
+ * the library itself owns (a file-scope static __device__ array), instead of a caller
+ * workspace. It is for callers that cannot allocate device memory themselves: host
+ * bindings that only pass pointers to buffers the application already owns (ctypes,
+ * cgo, JNI, N-API stubs with no CUDA allocator of their own) and services that must not
+ * grow their device memory after start-up. It makes no cudaMalloc / cudaFree call and
+ * uses no allocating library routine; the caller still provides the leaf pool and the
+ * result buffer.
+ *   - Limit: plans whose tsg_plan_workspace_bytes(plan, ring, num_primes, group_size)
+ *     exceeds tsg_static_scratch_bytes() (64 MiB) are rejected with TSG_ERR_WORKSPACE
+ *     before any device work; lower group_size or use tsg_plan_run.
+ *   - The first call on a device resolves the array's device address with
+ *     cudaGetSymbolAddress (with that device current) and caches it; make that first
+ *     call before any stream capture.
+ *   - Every call shares the one array and reuses whatever the previous call left in it:
+ *     the executor writes each intermediate before reading it, so nothing needs clearing;
+ *     result_dev follows the `accumulate` rule of tsg_plan_run.
+ *   - Calls whose work overlaps on the GPU (concurrent streams, or several host threads)
+ *     race on the array: serialize them on one stream.
+ *   - Every GPU that loads the library holds the 64 MiB until the process exits. */
+TSG_API int64_t tsg_static_scratch_bytes(void);
+
+TSG_API tsg_status tsg_plan_run_static(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                               const uint32_t* primes, const uint8_t* leaf_pool_dev,
+                               int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                               void* result_dev, int32_t accumulate, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

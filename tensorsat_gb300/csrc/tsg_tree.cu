@@ -21,6 +21,7 @@
 #include <cstring>
 #include <type_traits>
 #include <map>
+#include <mutex>
 #include <vector>
 
 #include "tsg_common.cuh"
@@ -1307,6 +1308,39 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
 }  // namespace
 }  // namespace tsg
 
+namespace tsg {
+namespace {
+
+// Scratch memory of tsg_plan_run_static: a fixed 64 MiB array in device global memory,
+// owned by this library, held by every GPU that loads it until the process exits. Host
+// code cannot use the array's name as a device address; the address comes from
+// cudaGetSymbolAddress, resolved once per device (with that device current) on the first
+// call and cached.
+constexpr int64_t kStaticScratchBytes = int64_t(64) << 20;
+static __device__ __align__(256) uint8_t g_static_scratch[kStaticScratchBytes];
+
+std::mutex g_static_scratch_mu;
+void* g_static_scratch_ptr[64] = {};
+
+tsg_status static_scratch_address(void** out) {
+  int dev = 0;
+  TSG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64)
+    return fail(TSG_ERR_UNSUPPORTED, "plan_run_static: device ordinal outside 0..63");
+  std::lock_guard<std::mutex> lock(g_static_scratch_mu);
+  if (g_static_scratch_ptr[dev] == nullptr) {
+    void* ptr = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress(&ptr, g_static_scratch);
+    if (err != cudaSuccess) return cuda_status(err, "cudaGetSymbolAddress(static scratch)");
+    g_static_scratch_ptr[dev] = ptr;
+  }
+  *out = g_static_scratch_ptr[dev];
+  return TSG_OK;
+}
+
+}  // namespace
+}  // namespace tsg
+
 using namespace tsg;
 
 extern "C" {
@@ -1470,6 +1504,29 @@ tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_pri
   if (!plan) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_validate: null plan");
   return run_impl(plan, ring, num_primes, primes, nullptr, slice_begin, slice_end, group_size,
                   nullptr, 0, nullptr, 0, nullptr, /*dry=*/true);
+}
+
+int64_t tsg_static_scratch_bytes(void) { return kStaticScratchBytes; }
+
+tsg_status tsg_plan_run_static(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                               const uint32_t* primes, const uint8_t* leaf_pool_dev,
+                               int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                               void* result_dev, int32_t accumulate, void* stream) {
+  if (!plan || !leaf_pool_dev || !result_dev)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run_static: null pointer");
+  // the size check and every argument check happen on the host, before any device work
+  int64_t need = 0;
+  TSG_TRY(tsg_plan_workspace_bytes(plan, ring, num_primes, group_size, &need));
+  if (need > kStaticScratchBytes)
+    return fail(TSG_ERR_WORKSPACE,
+                "plan_run_static: this plan and group size need " + std::to_string(need) +
+                    " bytes of scratch, more than the 64 MiB static array; use tsg_plan_run "
+                    "with a caller workspace or a smaller group size");
+  void* scratch = nullptr;
+  TSG_TRY(static_scratch_address(&scratch));
+  return run_impl(plan, ring, num_primes, primes, leaf_pool_dev, slice_begin, slice_end,
+                  group_size, scratch, kStaticScratchBytes, result_dev, accumulate,
+                  (cudaStream_t)stream, /*dry=*/false);
 }
 
 }  // extern "C"
