@@ -174,6 +174,11 @@ TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t
                              const uint32_t* primes, int64_t slice_begin,
                              int64_t slice_end, int64_t group_size);
 
+/* Synchronizes `stream` and reports whether any kernel of this library recorded a device-
+ * side failure since the last call (a bounded wait that gave up: TSG_ERR_TIMEOUT); the
+ * record is cleared. Runs launched before the failure are invalid. */
+TSG_API tsg_status tsg_take_device_error(void* stream);
+
 /* ---------------------------------------------------------------------------------
  * Allocation-free variant (no counterpart in the reference).
  *

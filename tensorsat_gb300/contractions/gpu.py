@@ -449,6 +449,12 @@ class GpuContraction(Contraction):
                 _device.stream_handle())
         return result
 
+    @staticmethod
+    def check_device() -> None:
+        """Synchronizes the current stream and raises if a kernel recorded a device-side
+        failure (a bounded wait that gave up)."""
+        _native.check(_native.lib().tsg_take_device_error(_device.stream_handle()))
+
     def contract(self, diagram: Diagram, *, progbar: bool = False, order: Any = None,
                  autojit: Any = "auto", group: int | None = None,
                  slice_range: tuple[int, int] | None = None,
@@ -462,6 +468,7 @@ class GpuContraction(Contraction):
         self.validate(diagram)
         res = self.run(diagram, _native.TSG_RING_OR_AND, group=group, slice_range=slice_range,
                        cache_leaves=cache_leaves)
+        self.check_device()
         lw = self._leaves
         k = len(lw.out_unique)
         box = CudaRel._new(res.reshape((2,) * k))
@@ -496,6 +503,7 @@ class GpuContraction(Contraction):
                 raise OverflowError("count bound exceeds 2^64: use ring='modp'")
             res = self.run(diagram, _native.TSG_RING_U64, group=group, slice_range=slice_range,
                            cache_leaves=cache_leaves)
+            self.check_device()
             vals = res.cpu().numpy().view(np.uint64)
             counts = np.array([int(v) for v in vals], dtype=object)
         elif ring == "modp":
@@ -515,6 +523,7 @@ class GpuContraction(Contraction):
                 chunk = primes[i: i + _native.TSG_MAX_PRIMES]
                 res = self.run(diagram, _native.TSG_RING_MODP, primes=chunk, group=group,
                                slice_range=slice_range, cache_leaves=cache_leaves)
+                self.check_device()
                 planes = res.cpu().numpy().view(np.uint32).reshape(len(chunk), -1)
                 residues.extend(planes[p] for p in range(len(chunk)))
             counts = crt(residues, primes)

@@ -493,6 +493,191 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
   }
 }
 
+// ------------------------------------------------------------------------------------
+// Streaming kernel for the large steps (the bulk of the HBM traffic). Persistent blocks
+// walk the (tile, slice) work items; thread 0 stages the E-free operand's tile for the
+// next item (every residue plane and summed combination: contiguous 4 KB chunks) into
+// shared memory with TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx) while the
+// block combines the current item from the other stage. The other operand (small, cached
+// in L2) is read with ordinary loads as in the tile kernel; outputs are written from
+// registers. Every mbarrier wait is bounded: on expiry the block records an error in
+// g_device_error, waits (bounded) for its own copies in flight, and returns.
+
+constexpr int kStreamTileBits = 10;                    // 256 threads x 4 positions
+constexpr int kStreamTile = 1 << kStreamTileBits;
+constexpr long long kSpinLimit = 1ll << 24;            // try_wait polls per wait
+
+__device__ int g_device_error = 0;  // 0 = ok, else TSG_ERR_TIMEOUT
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar`; false when the limit expired.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (long long i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+struct StreamArgs {
+  int32_t big;           // operand staged through shared memory (0 = lhs, 1 = rhs)
+  uint32_t tiles;        // tiles per slice
+  uint64_t work;         // tiles * slices
+  uint32_t chunk_bytes;  // one (plane, summed combination) chunk of the staged operand
+};
+
+template <int kRing, int NE, int NK>
+__global__ void __launch_bounds__(kThreads, 3)
+    tree_step_stream_kernel(TileArgs a, RingArgs ring, StreamArgs sa) {
+  using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
+  using VT = T;
+  constexpr int V = 4;
+  constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
+  constexpr int KU = NK;  // NK in {1, 2}
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ int bail;
+  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
+  const TileOperand& B = a.op[sa.big];
+  const TileOperand& S = a.op[1 - sa.big];
+  const int leaves = a.op[0].leaf + a.op[1].leaf;
+  const uint32_t stage_bytes = (uint32_t)(np * KU) * sa.chunk_bytes;
+  const uint32_t f_lo = threadIdx.x * V;
+  const uint64_t s_lo = scatter32(S.f_lo, f_lo);
+  const uint64_t o_lo = scatter32(a.of_lo, f_lo);
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    bail = 0;
+  }
+  __syncthreads();
+
+  auto item_offsets = [&](uint64_t w, uint64_t* bo, uint64_t* so, uint64_t* oo) {
+    const uint32_t g = (uint32_t)(w / sa.tiles);
+    const uint32_t f_hi = (uint32_t)(w % sa.tiles) << kStreamTileBits;
+    *bo = B.base + scatter_bits(B.g, g) + scatter32(B.f_hi, f_hi);
+    *so = S.base + scatter_bits(S.g, g) + scatter32(S.f_hi, f_hi) + s_lo;
+    *oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + o_lo;
+  };
+  auto issue = [&](uint64_t w, int stage) {
+    uint64_t bo, so, oo;
+    item_offsets(w, &bo, &so, &oo);
+    uint8_t* dst = smem + stage * stage_bytes;
+    mbar_expect_tx(&bars[stage], stage_bytes);
+    const T* base = reinterpret_cast<const T*>(B.ptr);
+    for (int p = 0; p < np; ++p)
+      for (int ku = 0; ku < KU; ++ku)
+        tma_load_1d(dst + (p * KU + ku) * sa.chunk_bytes, base + bo + p * B.plane + B.k_off[ku],
+                    sa.chunk_bytes, &bars[stage]);
+  };
+
+  uint64_t w = blockIdx.x;
+  if (threadIdx.x == 0 && w < sa.work) issue(w, 0);
+  uint32_t phase[2] = {0, 0};
+  for (int it = 0; w < sa.work; ++it, w += gridDim.x) {
+    const int stage = it & 1;
+    const uint64_t wn = w + gridDim.x;
+    if (threadIdx.x == 0 && wn < sa.work) issue(wn, stage ^ 1);
+    if (!mbar_wait_bounded(&bars[stage], phase[stage])) {
+      atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
+      bail = 1;
+    }
+    phase[stage] ^= 1;
+    __syncthreads();
+    if (bail) {
+      // drain: the copies issued for the other stage must land before the block exits
+      if (threadIdx.x == 0 && wn < sa.work) (void)mbar_wait_bounded(&bars[stage ^ 1], phase[stage ^ 1]);
+      return;
+    }
+    uint64_t bo, so, oo;
+    item_offsets(w, &bo, &so, &oo);
+    const uint8_t* st = smem + stage * stage_bytes;
+#pragma unroll
+    for (int p = 0; p < PP; ++p) {
+      if (p >= np) break;
+      VT bv[KU][V];
+#pragma unroll
+      for (int ku = 0; ku < KU; ++ku) {
+        const T* src = reinterpret_cast<const T*>(st + (p * KU + ku) * sa.chunk_bytes) + f_lo;
+        if constexpr (sizeof(T) == 4) {
+          const uint4 x = *reinterpret_cast<const uint4*>(src);
+          bv[ku][0] = x.x;
+          bv[ku][1] = x.y;
+          bv[ku][2] = x.z;
+          bv[ku][3] = x.w;
+        } else {
+          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
+          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
+          bv[ku][0] = x0.x;
+          bv[ku][1] = x0.y;
+          bv[ku][2] = x1.x;
+          bv[ku][3] = x1.y;
+        }
+      }
+      const uint64_t sp = so + (S.leaf ? 0 : p * S.plane);
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        uint64_t acc[V] = {0, 0, 0, 0};
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku) {
+          VT sv[V];
+          tile_load<T, VT, V>(S, sp + S.e_off[e] + S.k_off[ku], sv);
+#pragma unroll
+          for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
+        }
+        const uint64_t oe = oo + a.o_e[e];
+        if constexpr (kRing == TSG_RING_U64) {
+          uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
+          reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[0], acc[1]);
+          reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[2], acc[3]);
+        } else {
+          uint32_t r[V];
+#pragma unroll
+          for (int j = 0; j < V; ++j) r[j] = mont_finish(acc[j], leaves, ring, p);
+          *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane + oe) =
+              make_uint4(r[0], r[1], r[2], r[3]);
+        }
+      }
+    }
+    __syncthreads();  // the stage is refilled two items later
+  }
+}
+
 // Combines the root tensors of `cnt` slices (layout [plane][cnt][E]) into result[E]
 // (OR for OR_AND, sum mod 2^64 for U64, sum mod p per plane for MODP). One block per root
 // entry; threads stride over slices, then a shared-memory tree reduction.
@@ -904,7 +1089,9 @@ struct LaunchArgs {
   StepArgs a;       // general form (also used for the bounds check)
   TileArgs t;       // tile form, valid when `tile`
   TileShape shape;
+  StreamArgs stream;
   bool tile;
+  bool streamed;    // run by the streaming (TMA-staged) kernel
   bool is_leaf[2];
   uint64_t cnt;     // slices of this launch
 };
@@ -1076,6 +1263,39 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
     if (op.base < lo_ext || hi >= hi_ext)
       return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: operand offset outside its tensor");
   }
+  // Vector accesses: a contiguous operand (V positions = its V fastest elements) and a
+  // contiguous output are read / written V elements at a time, so every other term of
+  // their offsets must be a multiple of V: bit positions of the slot, tile, E and summed
+  // maps at or above log2(V), constant and plane offsets multiples of V.
+  const uint32_t vmask = (uint32_t)sh.v - 1;
+  const int vb = vbits;
+  auto map_ok = [&](const NarrowMap& m) {
+    for (int i = 0; i < m.n; ++i)
+      if (m.dst[i] < vb && m.src[i] >= vb) return false;
+    return true;
+  };
+  auto bitmap_ok = [&](const BitMap& m) {
+    for (int i = 0; i < m.n; ++i)
+      if (m.dst[i] < vb) return false;
+    return true;
+  };
+  for (int o = 0; o < 2 && sh.v > 1; ++o) {
+    const TileOperand& op = t.op[o];
+    if (op.mode != kModeContig) continue;
+    bool ok = (op.base & vmask) == 0 && (op.plane & vmask) == 0 && bitmap_ok(op.g) &&
+              map_ok(op.f_hi) && map_ok(op.f_lo);
+    for (int j = 0; j < sh.v; ++j) ok = ok && op.tab[j] == (uint32_t)j;
+    for (int e = 0; e < sh.ne; ++e) ok = ok && (op.e_off[e] & vmask) == 0;
+    for (int kk = 0; kk < t.n_k; ++kk) ok = ok && (op.k_off[kk] & vmask) == 0;
+    if (!ok) return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: vector load not aligned");
+  }
+  if (t.o_contig && sh.v > 1) {
+    bool ok = (t.n_out & vmask) == 0 && (la.a.o_plane & vmask) == 0 && map_ok(t.of_hi) &&
+              map_ok(t.of_lo);
+    for (int j = 0; j < sh.v; ++j) ok = ok && t.o_tab[j] == (uint32_t)j;
+    for (int e = 0; e < sh.ne; ++e) ok = ok && (t.o_e[e] & vmask) == 0;
+    if (!ok) return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: vector store not aligned");
+  }
   uint32_t otab = 0, oe = 0;
   for (int j = 0; j < sh.v; ++j) otab = std::max(otab, t.o_tab[j]);
   for (int e = 0; e < sh.ne; ++e) oe = std::max(oe, t.o_e[e]);
@@ -1084,6 +1304,43 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
   if (ohi >= (uint64_t)c.lay->plane[s])
     return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: output offset outside its buffer");
   return TSG_OK;
+}
+
+// The streaming kernel takes large steps whose E-free operand is an intermediate read
+// as whole 1024-element tiles: its first 10 F bits are its own bits 0-9, every other
+// offset term is a multiple of 1024 elements (so each chunk is contiguous and 16-byte
+// aligned for TMA), and the tile kernel would use 256 threads x 4 positions.
+void choose_stream(LaunchArgs& la, int ring) {
+  if (ring == TSG_RING_OR_AND) return;
+  const TileArgs& t = la.t;
+  const TileShape& sh = la.shape;
+  // the streaming kernel stores 4 consecutive outputs as one vector: only when the 4
+  // positions of a thread are 4 consecutive, aligned outputs
+  if (sh.v != 4 || (sh.nk != 1 && sh.nk != 2) || t.tile_bits != kStreamTileBits || !t.o_contig)
+    return;
+  if (sh.tiles * la.cnt < (uint64_t)device_sm_count() * 8) return;  // too small to stream
+  int big = -1;
+  for (int o = 0; o < 2; ++o) {
+    const TileOperand& op = t.op[o];
+    if (op.leaf || op.has_e) continue;
+    if (op.f_lo.n != 1 || op.f_lo.src[0] != 0 || op.f_lo.dst[0] != 0 ||
+        op.f_lo.len[0] != kStreamTileBits)
+      continue;
+    bool aligned = (op.base % kStreamTile) == 0 && (op.plane % kStreamTile) == 0;
+    for (int i = 0; i < op.g.n; ++i) aligned = aligned && op.g.dst[i] >= kStreamTileBits;
+    for (int i = 0; i < op.f_hi.n; ++i) aligned = aligned && op.f_hi.dst[i] >= kStreamTileBits;
+    for (int kk = 0; kk < t.n_k; ++kk) aligned = aligned && (op.k_off[kk] % kStreamTile) == 0;
+    if (aligned) {
+      big = o;
+      break;
+    }
+  }
+  if (big < 0) return;
+  la.stream.big = big;
+  la.stream.tiles = (uint32_t)sh.tiles;
+  la.stream.work = sh.tiles * la.cnt;
+  la.stream.chunk_bytes = kStreamTile * (ring == TSG_RING_U64 ? 8 : 4);
+  la.streamed = true;
 }
 
 // Fills the kernel arguments of step s for slices [base, base + cnt) (cnt == 1 and base
@@ -1113,7 +1370,9 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   bool ok = false;
   TSG_TRY(build_tile(st, d, a, la->cnt, c.ring, &la->t, &la->shape, &ok));
   la->tile = ok;
+  la->streamed = false;
   if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
+  if (ok) choose_stream(*la, c.ring);
   return TSG_OK;
 }
 
@@ -1153,9 +1412,50 @@ void launch_tile_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st)
   else launch_tile_ne<kRing, 1>(la, ra, st);
 }
 
+template <int kRing, int NE, int NK>
+tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  auto kernel = tree_step_stream_kernel<kRing, NE, NK>;
+  const int np = kRing == TSG_RING_MODP ? ra.np : 1;
+  const size_t smem = 2ull * np * NK * la.stream.chunk_bytes;
+  static bool configured[64] = {};  // one attribute call per instantiation and device
+  int dev = 0;
+  TSG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(TSG_ERR_UNSUPPORTED, "device ordinal outside 0..63");
+  if (!configured[dev]) {
+    const int max_smem = 2 * TSG_MAX_PRIMES * 2 * kStreamTile * 8;
+    TSG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      max_smem));
+    configured[dev] = true;
+  }
+  const uint64_t blocks = std::min<uint64_t>(la.stream.work, (uint64_t)device_sm_count() * 3);
+  kernel<<<(unsigned)blocks, kThreads, smem, st>>>(la.t, ra, la.stream);
+  return TSG_OK;
+}
+
+template <int kRing, int NE>
+tsg_status launch_stream_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  return la.shape.nk == 1 ? launch_stream_t<kRing, NE, 1>(la, ra, st)
+                          : launch_stream_t<kRing, NE, 2>(la, ra, st);
+}
+
+template <int kRing>
+tsg_status launch_stream_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  switch (la.shape.ne) {
+    case 1: return launch_stream_nk<kRing, 1>(la, ra, st);
+    case 2: return launch_stream_nk<kRing, 2>(la, ra, st);
+    default: return launch_stream_nk<kRing, 4>(la, ra, st);
+  }
+}
+
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   LaunchArgs la;
   TSG_TRY(build_step(c, s, base, cnt, &la));
+  if (la.streamed) {
+    if (c.ring == TSG_RING_U64) TSG_TRY(launch_stream_ring<TSG_RING_U64>(la, c.ra, c.stream));
+    else TSG_TRY(launch_stream_ring<TSG_RING_MODP>(la, c.ra, c.stream));
+    TSG_CUDA_TRY(cudaGetLastError());
+    return TSG_OK;
+  }
   if (la.tile) {
     switch (c.ring) {
       case TSG_RING_OR_AND:
@@ -1507,6 +1807,21 @@ tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_pri
 }
 
 int64_t tsg_static_scratch_bytes(void) { return kStaticScratchBytes; }
+
+tsg_status tsg_take_device_error(void* stream) {
+  int err = 0;
+  const int zero = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  TSG_CUDA_TRY(cudaMemcpyFromSymbolAsync(&err, g_device_error, sizeof(int), 0,
+                                         cudaMemcpyDeviceToHost, st));
+  TSG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (err == 0) return TSG_OK;
+  TSG_CUDA_TRY(cudaMemcpyToSymbolAsync(g_device_error, &zero, sizeof(int), 0,
+                                       cudaMemcpyHostToDevice, st));
+  TSG_CUDA_TRY(cudaStreamSynchronize(st));
+  return fail(TSG_ERR_TIMEOUT, "a bounded device-side wait gave up (TMA staging did not "
+                               "complete); results of the affected runs are invalid");
+}
 
 tsg_status tsg_plan_run_static(const tsg_plan* plan, int32_t ring, int32_t num_primes,
                                const uint32_t* primes, const uint8_t* leaf_pool_dev,

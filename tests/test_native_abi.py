@@ -158,3 +158,27 @@ def test_planner_native_arrays_shapes():
     arrs = sp.native_arrays()
     assert arrs["step_lhs_pos"].shape == (len(tree.steps), planner.TSG_MAX_BITS)
     assert arrs["leaf_slice_pos"].shape == (len(net.leaf_wires), len(sl))
+
+
+def test_kissat_and_benchmark_plans_validate_in_every_ring():
+    """Bounds and vector-alignment proofs over every launch of real plans (gate networks
+    of the known-answer set, the n=60 benchmark tree), all rings and several groups."""
+    import json
+
+    golden = Path(__file__).resolve().parent / "golden" / "kissat.json"
+    for case in json.loads(golden.read_text())[::4] + [
+            c for c in json.loads(golden.read_text()) if c["file"] == "prime121"]:
+        cnf = CNFInstance(case["num_vars"], [tuple(c) for c in case["clauses"]])
+        d = (cnf.inputs(None) >> cnf.diagram()).flatten()
+        c = GpuContraction(CudaRel, d.wiring, trials=1)
+        npl = c.native_plan()
+        for ring, primes in [(_native.TSG_RING_OR_AND, ()), (_native.TSG_RING_MODP, PRIMES_31[:4]),
+                             (_native.TSG_RING_U64, ())]:
+            npl.validate(ring, primes, 0, c.num_slices, 1)
+    cnf = CNFInstance.random(3, 60, 256, rng=0)
+    c = GpuContraction(CudaRel, cnf.clause_diagram().wiring, target_bits=26, trials=2)
+    npl = c.native_plan()
+    for ring, primes in [(_native.TSG_RING_OR_AND, ()), (_native.TSG_RING_MODP, PRIMES_31[:3]),
+                         (_native.TSG_RING_U64, ())]:
+        for g in (1, 64):
+            npl.validate(ring, primes, 0, 2 * g, g)
