@@ -557,7 +557,42 @@ struct StreamArgs {
   uint32_t tiles;        // tiles per slice
   uint64_t work;         // tiles * slices
   uint32_t chunk_bytes;  // one (plane, summed combination) chunk of the staged operand
+  uint32_t s_span;       // elements of one staged chunk of the other operand per (plane, E
+                         // combination, summed combination); 0: read from global memory
 };
+
+// Loads the V values of the other operand from its staged chunk: `p` points at the
+// thread's first position, the tile's positions sit at the operand's tab offsets.
+template <typename T, int V>
+__device__ __forceinline__ void smem_load(const TileOperand& op, const T* p, T (&out)[V]) {
+  if (op.mode == kModeContig) {
+    if constexpr (sizeof(T) == 4) {
+      const uint4 x = *reinterpret_cast<const uint4*>(p);
+      out[0] = x.x;
+      out[1 % V] = x.y;
+      out[2 % V] = x.z;
+      out[3 % V] = x.w;
+    } else {
+      const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(p)[0];
+      const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(p)[1];
+      out[0] = x0.x;
+      out[1 % V] = x0.y;
+      out[2 % V] = x1.x;
+      out[3 % V] = x1.y;
+    }
+  } else if (op.mode == kModeBcast) {
+    const T x = p[0];
+#pragma unroll
+    for (int j = 0; j < V; ++j) out[j] = x;
+  } else if (op.mode == kModePair) {
+    const T x0 = p[0], x1 = p[op.tab[3]];
+#pragma unroll
+    for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
+  } else {
+#pragma unroll
+    for (int j = 0; j < V; ++j) out[j] = p[op.tab[j]];
+  }
+}
 
 template <int kRing, int NE, int NK>
 __global__ void __launch_bounds__(kThreads, 3)
@@ -574,10 +609,14 @@ __global__ void __launch_bounds__(kThreads, 3)
   const TileOperand& B = a.op[sa.big];
   const TileOperand& S = a.op[1 - sa.big];
   const int leaves = a.op[0].leaf + a.op[1].leaf;
-  const uint32_t stage_bytes = (uint32_t)(np * KU) * sa.chunk_bytes;
+  const bool s_staged = sa.s_span != 0;
+  const uint32_t b_bytes = (uint32_t)(np * KU) * sa.chunk_bytes;
+  const uint32_t s_chunk = sa.s_span * (uint32_t)sizeof(T);
+  const uint32_t stage_bytes = b_bytes + (s_staged ? (uint32_t)(np * NE * KU) * s_chunk : 0u);
   const uint32_t f_lo = threadIdx.x * V;
   const uint64_t s_lo = scatter32(S.f_lo, f_lo);
   const uint64_t o_lo = scatter32(a.of_lo, f_lo);
+  const int lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
@@ -587,32 +626,47 @@ __global__ void __launch_bounds__(kThreads, 3)
   }
   __syncthreads();
 
+  // so: the other operand's offset for the tile, without the thread's own positions
   auto item_offsets = [&](uint64_t w, uint64_t* bo, uint64_t* so, uint64_t* oo) {
     const uint32_t g = (uint32_t)(w / sa.tiles);
     const uint32_t f_hi = (uint32_t)(w % sa.tiles) << kStreamTileBits;
     *bo = B.base + scatter_bits(B.g, g) + scatter32(B.f_hi, f_hi);
-    *so = S.base + scatter_bits(S.g, g) + scatter32(S.f_hi, f_hi) + s_lo;
+    *so = S.base + scatter_bits(S.g, g) + scatter32(S.f_hi, f_hi);
     *oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + o_lo;
   };
+  // Run by warp 0: lane 0 arms the stage's barrier with the byte count, then the lanes
+  // issue the bulk copies (np x KU tiles of B, np x NE x KU chunks of the other operand).
   auto issue = [&](uint64_t w, int stage) {
     uint64_t bo, so, oo;
     item_offsets(w, &bo, &so, &oo);
     uint8_t* dst = smem + stage * stage_bytes;
-    mbar_expect_tx(&bars[stage], stage_bytes);
-    const T* base = reinterpret_cast<const T*>(B.ptr);
-    for (int p = 0; p < np; ++p)
-      for (int ku = 0; ku < KU; ++ku)
-        tma_load_1d(dst + (p * KU + ku) * sa.chunk_bytes, base + bo + p * B.plane + B.k_off[ku],
+    if (lane == 0) mbar_expect_tx(&bars[stage], stage_bytes);
+    __syncwarp();
+    const T* bsrc = reinterpret_cast<const T*>(B.ptr);
+    const T* ssrc = reinterpret_cast<const T*>(S.ptr);
+    const int nb = np * KU;
+    const int ncopies = nb + (s_staged ? np * NE * KU : 0);
+    for (int i = lane; i < ncopies; i += 32) {
+      if (i < nb) {
+        const int p = i / KU, ku = i % KU;
+        tma_load_1d(dst + i * sa.chunk_bytes, bsrc + bo + p * B.plane + B.k_off[ku],
                     sa.chunk_bytes, &bars[stage]);
+      } else {
+        const int j = i - nb;
+        const int p = j / (NE * KU), e = (j / KU) % NE, ku = j % KU;
+        tma_load_1d(dst + b_bytes + j * s_chunk,
+                    ssrc + so + p * S.plane + S.e_off[e] + S.k_off[ku], s_chunk, &bars[stage]);
+      }
+    }
   };
 
   uint64_t w = blockIdx.x;
-  if (threadIdx.x == 0 && w < sa.work) issue(w, 0);
+  if (threadIdx.x < 32 && w < sa.work) issue(w, 0);
   uint32_t phase[2] = {0, 0};
   for (int it = 0; w < sa.work; ++it, w += gridDim.x) {
     const int stage = it & 1;
     const uint64_t wn = w + gridDim.x;
-    if (threadIdx.x == 0 && wn < sa.work) issue(wn, stage ^ 1);
+    if (threadIdx.x < 32 && wn < sa.work) issue(wn, stage ^ 1);
     if (!mbar_wait_bounded(&bars[stage], phase[stage])) {
       atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
       bail = 1;
@@ -649,14 +703,16 @@ __global__ void __launch_bounds__(kThreads, 3)
           bv[ku][3] = x1.y;
         }
       }
-      const uint64_t sp = so + (S.leaf ? 0 : p * S.plane);
+      const uint64_t sp = so + s_lo + (S.leaf ? 0 : p * S.plane);
+      const T* ss = reinterpret_cast<const T*>(st + b_bytes) + (uint64_t)p * NE * KU * sa.s_span + s_lo;
 #pragma unroll
       for (int e = 0; e < NE; ++e) {
         uint64_t acc[V] = {0, 0, 0, 0};
 #pragma unroll
         for (int ku = 0; ku < KU; ++ku) {
           VT sv[V];
-          tile_load<T, VT, V>(S, sp + S.e_off[e] + S.k_off[ku], sv);
+          if (s_staged) smem_load<T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
+          else tile_load<T, VT, V>(S, sp + S.e_off[e] + S.k_off[ku], sv);
 #pragma unroll
           for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
         }
@@ -1310,7 +1366,53 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
 // as whole 1024-element tiles: its first 10 F bits are its own bits 0-9, every other
 // offset term is a multiple of 1024 elements (so each chunk is contiguous and 16-byte
 // aligned for TMA), and the tile kernel would use 256 threads x 4 positions.
-void choose_stream(LaunchArgs& la, int ring) {
+// Shared memory of one streaming block, both stages, when the other operand is staged as
+// well: three blocks per SM.
+constexpr uint64_t kStreamSmemBudget = 72 * 1024;
+
+uint64_t stream_smem_bytes(int np, int ne, int nk, uint32_t chunk_bytes, uint32_t span,
+                           uint32_t esize) {
+  return 2ull * np * ((uint64_t)nk * chunk_bytes + (uint64_t)ne * nk * span * esize);
+}
+
+// Span of the staged chunks of the other operand of a streamed step, or 0 (plain loads).
+// Per (plane, E combination, summed combination) the tile reads that operand at
+// base + slot terms + tile terms + e_off + k_off + its within-tile offsets; the
+// within-tile offsets stay below span = 2^b and every other term is a multiple of span,
+// so one aligned block of span elements holds them all. The blocks must be whole 16-byte
+// bulk copies, end inside the operand's buffer (`extent` elements per plane), and fit the
+// shared-memory budget; leaves (uint8) are never staged.
+uint32_t stream_span(const LaunchArgs& la, int np, uint32_t esize, uint64_t extent) {
+  const TileArgs& t = la.t;
+  const TileShape& sh = la.shape;
+  const TileOperand& s = t.op[1 - la.stream.big];
+  if (s.leaf) return 0;
+  int b = bit_width(narrow_max(s.f_lo, kStreamTileBits));
+  while ((1u << b) * esize < 16) b++;
+  const uint32_t span = 1u << b;
+  const uint64_t mask = span - 1;
+  bool ok = (s.base & mask) == 0 && (s.plane & mask) == 0;
+  for (int i = 0; i < s.g.n; ++i) ok = ok && s.g.dst[i] >= b;
+  for (int i = 0; i < s.f_hi.n; ++i) ok = ok && s.f_hi.dst[i] >= b;
+  uint32_t eo = 0, ko = 0;
+  for (int e = 0; e < sh.ne; ++e) {
+    ok = ok && (s.e_off[e] & mask) == 0;
+    eo = std::max(eo, s.e_off[e]);
+  }
+  for (int kk = 0; kk < t.n_k; ++kk) {
+    ok = ok && (s.k_off[kk] & mask) == 0;
+    ko = std::max(ko, s.k_off[kk]);
+  }
+  const int gbits = bit_width(la.cnt - 1);
+  const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
+  const uint64_t end = s.base + scatter_max(s.g, gbits) + narrow_max(s.f_hi, nbits) + eo + ko + span;
+  ok = ok && end <= extent;
+  ok = ok && stream_smem_bytes(np, sh.ne, sh.nk, la.stream.chunk_bytes, span, esize) <=
+                 kStreamSmemBudget;
+  return ok ? span : 0;
+}
+
+void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   if (ring == TSG_RING_OR_AND) return;
   const TileArgs& t = la.t;
   const TileShape& sh = la.shape;
@@ -1336,10 +1438,12 @@ void choose_stream(LaunchArgs& la, int ring) {
     }
   }
   if (big < 0) return;
+  const uint32_t esize = ring == TSG_RING_U64 ? 8 : 4;
   la.stream.big = big;
   la.stream.tiles = (uint32_t)sh.tiles;
   la.stream.work = sh.tiles * la.cnt;
-  la.stream.chunk_bytes = kStreamTile * (ring == TSG_RING_U64 ? 8 : 4);
+  la.stream.chunk_bytes = kStreamTile * esize;
+  la.stream.s_span = stream_span(la, np, esize, extent[1 - big]);
   la.streamed = true;
 }
 
@@ -1372,7 +1476,12 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   la->tile = ok;
   la->streamed = false;
   if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
-  if (ok) choose_stream(*la, c.ring);
+  if (ok) {
+    uint64_t extent[2];
+    for (int o = 0; o < 2; ++o)
+      extent[o] = la->is_leaf[o] ? 0 : (uint64_t)c.lay->plane[-st.op[o] - 1];
+    choose_stream(*la, c.ring, c.ring == TSG_RING_MODP ? c.ra.np : 1, extent);
+  }
   return TSG_OK;
 }
 
@@ -1416,7 +1525,8 @@ template <int kRing, int NE, int NK>
 tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
   auto kernel = tree_step_stream_kernel<kRing, NE, NK>;
   const int np = kRing == TSG_RING_MODP ? ra.np : 1;
-  const size_t smem = 2ull * np * NK * la.stream.chunk_bytes;
+  const size_t smem = stream_smem_bytes(np, NE, NK, la.stream.chunk_bytes, la.stream.s_span,
+                                        kRing == TSG_RING_U64 ? 8 : 4);
   static bool configured[64] = {};  // one attribute call per instantiation and device
   int dev = 0;
   TSG_CUDA_TRY(cudaGetDevice(&dev));
