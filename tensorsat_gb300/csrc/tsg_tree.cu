@@ -311,104 +311,104 @@ __device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t
   }
 }
 
+// One thread's work in the tile kernel. X is an operand without E bits (loaded once per
+// residue plane and reused for every E value), Y the other one; the ring products commute,
+// so the kernel passes (lhs, rhs) or (rhs, lhs). With a fixed summed count (NK > 0) the
+// thread gathers all of Y's values of a plane before its first store: loads placed after
+// a store to a possibly aliasing address would each wait out their own latency.
 template <int kRing, int V, int NE, int NK>
-__global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
+__device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& ring,
+                                            const TileOperand& X, const TileOperand& Y,
+                                            uint64_t x0, uint64_t y0, uint64_t oo) {
   using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
             typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
   using VT = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
   using AT = uint64_t;
   constexpr bool kPacked = (kRing == TSG_RING_OR_AND) && (V % 4 == 0);
   constexpr int W = kPacked ? V / 4 : 1;  // packed words per operand (OR-AND)
-  const uint32_t g = blockIdx.y;
-  const uint32_t f_hi = blockIdx.x << a.tile_bits;
-  const uint32_t f_lo = threadIdx.x * (uint32_t)V;
-  uint64_t xo[2];
-#pragma unroll
-  for (int o = 0; o < 2; ++o) {
-    const TileOperand& op = a.op[o];
-    xo[o] = op.base + scatter_bits(op.g, g) + scatter32(op.f_hi, f_hi) + scatter32(op.f_lo, f_lo);
-  }
-  const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
-  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
-  const TileOperand& L = a.op[0];
-  const TileOperand& R = a.op[1];
-  const int leaves = L.leaf + R.leaf;
-  // NK > 0: the summed combinations are unrolled and the operand without E bits is loaded
-  // once for all of them before the E loop; NK == 0: runtime count, loads in the loop
   constexpr int KU = NK > 0 ? NK : 1;
   const int nk = NK > 0 ? NK : a.n_k;
   if constexpr (kPacked) {
-    const uint64_t lp = xo[0];
-    const uint64_t rp = xo[1];
-    {
-      uint32_t lpre[KU][W], rpre[KU][W];
-      if (NK > 0) {
+    constexpr bool kHoist = NK > 0 && NE * KU * W <= 32;
+    uint32_t xw[KU][W];
+    uint32_t yh[kHoist ? NE : 1][KU][W];
+    if (NK > 0) {
+#pragma unroll
+      for (int ku = 0; ku < KU; ++ku) tile_load_packed<V>(X, x0 + X.k_off[ku], xw[ku]);
+    }
+    if constexpr (kHoist) {
+#pragma unroll
+      for (int e = 0; e < NE; ++e)
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku)
+          tile_load_packed<V>(Y, y0 + Y.e_off[e] + Y.k_off[ku], yh[e][ku]);
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      uint32_t acc[W];
+#pragma unroll
+      for (int i = 0; i < W; ++i) acc[i] = 0;
+      for (int kk0 = 0; kk0 < nk; kk0 += KU) {
 #pragma unroll
         for (int ku = 0; ku < KU; ++ku) {
-          if (!L.has_e) tile_load_packed<V>(L, lp + L.k_off[ku], lpre[ku]);
-          if (!R.has_e) tile_load_packed<V>(R, rp + R.k_off[ku], rpre[ku]);
+          const int kk = kk0 + ku;
+          uint32_t xv[W], yv[W];
+          if (NK > 0) {
+#pragma unroll
+            for (int i = 0; i < W; ++i) xv[i] = xw[ku][i];
+          } else {
+            tile_load_packed<V>(X, x0 + X.k_off[kk], xv);
+          }
+          if constexpr (kHoist) {
+#pragma unroll
+            for (int i = 0; i < W; ++i) yv[i] = yh[e][ku][i];
+          } else {
+            tile_load_packed<V>(Y, y0 + Y.e_off[e] + Y.k_off[kk], yv);
+          }
+#pragma unroll
+          for (int i = 0; i < W; ++i) acc[i] |= xv[i] & yv[i];
         }
       }
-#pragma unroll
-      for (int e = 0; e < NE; ++e) {
-        uint32_t acc[W];
-#pragma unroll
-        for (int i = 0; i < W; ++i) acc[i] = 0;
-        for (int kk0 = 0; kk0 < nk; kk0 += KU) {
-#pragma unroll
-          for (int ku = 0; ku < KU; ++ku) {
-            const int kk = kk0 + ku;
-            uint32_t lw[W], rw[W];
-            if (L.has_e) tile_load_packed<V>(L, lp + L.e_off[e] + L.k_off[kk], lw);
-            else if (NK > 0) {
-#pragma unroll
-              for (int i = 0; i < W; ++i) lw[i] = lpre[ku][i];
-            } else tile_load_packed<V>(L, lp + L.k_off[kk], lw);
-            if (R.has_e) tile_load_packed<V>(R, rp + R.e_off[e] + R.k_off[kk], rw);
-            else if (NK > 0) {
-#pragma unroll
-              for (int i = 0; i < W; ++i) rw[i] = rpre[ku][i];
-            } else tile_load_packed<V>(R, rp + R.k_off[kk], rw);
-#pragma unroll
-            for (int i = 0; i < W; ++i) acc[i] |= lw[i] & rw[i];
-          }
-        }
-        const uint64_t oe = oo + a.o_e[e];
-        if (a.o_contig) {
-          if constexpr (V == 16) {
-            *reinterpret_cast<uint4*>(a.out + oe) =
-                make_uint4(acc[0], acc[1 % W], acc[2 % W], acc[3 % W]);
-          } else {
-            *reinterpret_cast<uint32_t*>(a.out + oe) = acc[0];
-          }
+      const uint64_t oe = oo + a.o_e[e];
+      if (a.o_contig) {
+        if constexpr (V == 16) {
+          *reinterpret_cast<uint4*>(a.out + oe) =
+              make_uint4(acc[0], acc[1 % W], acc[2 % W], acc[3 % W]);
         } else {
-#pragma unroll
-          for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = (acc[j / 4] >> (8 * (j % 4))) & 0xff;
+          *reinterpret_cast<uint32_t*>(a.out + oe) = acc[0];
         }
+      } else {
+#pragma unroll
+        for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = (acc[j / 4] >> (8 * (j % 4))) & 0xff;
       }
     }
-  }
-  if constexpr (!kPacked) {
-    // planes outermost; the E-free operand of plane p+1 is loaded while plane p is being
-    // combined (two planes of loads in flight per thread), and reused across E values
+  } else {
+    // planes outermost; X of plane p+1 is loaded while plane p is combined
     constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
-    VT lcur[KU][V], rcur[KU][V], lnxt[KU][V], rnxt[KU][V];
-    auto preload = [&](int p, VT (&lb)[KU][V], VT (&rb)[KU][V]) {
-      const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
-      const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
+    constexpr bool kHoist = NK > 0 && NE * KU * V * sizeof(VT) <= 128;
+    const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
+    const int leaves = X.leaf + Y.leaf;
+    VT xcur[KU][V], xnxt[KU][V];
+    auto preload = [&](int p, VT (&xb)[KU][V]) {
+      const uint64_t xp = x0 + (X.leaf ? 0 : p * X.plane);
 #pragma unroll
-      for (int ku = 0; ku < KU; ++ku) {
-        if (!L.has_e) tile_load<T, VT, V>(L, lp + L.k_off[ku], lb[ku]);
-        if (!R.has_e) tile_load<T, VT, V>(R, rp + R.k_off[ku], rb[ku]);
-      }
+      for (int ku = 0; ku < KU; ++ku) tile_load<T, VT, V>(X, xp + X.k_off[ku], xb[ku]);
     };
-    if (NK > 0) preload(0, lcur, rcur);
+    if (NK > 0) preload(0, xcur);
 #pragma unroll
     for (int p = 0; p < PP; ++p) {
       if (p >= np) break;
-      if (NK > 0 && p + 1 < np) preload(p + 1, lnxt, rnxt);
-      const uint64_t lp = xo[0] + (L.leaf ? 0 : p * L.plane);
-      const uint64_t rp = xo[1] + (R.leaf ? 0 : p * R.plane);
+      if (NK > 0 && p + 1 < np) preload(p + 1, xnxt);
+      const uint64_t xp = x0 + (X.leaf ? 0 : p * X.plane);
+      const uint64_t yp = y0 + (Y.leaf ? 0 : p * Y.plane);
+      VT yh[kHoist ? NE : 1][KU][V];
+      if constexpr (kHoist) {
+#pragma unroll
+        for (int e = 0; e < NE; ++e)
+#pragma unroll
+          for (int ku = 0; ku < KU; ++ku)
+            tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[ku], yh[e][ku]);
+      }
 #pragma unroll
       for (int e = 0; e < NE; ++e) {
         const uint64_t oe = oo + a.o_e[e];
@@ -423,23 +423,25 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
 #pragma unroll
           for (int ku = 0; ku < KU; ++ku) {
             const int kk = kk0 + ku;
-            VT lv[V], rv[V];
-            if (L.has_e) tile_load<T, VT, V>(L, lp + L.e_off[e] + L.k_off[kk], lv);
-            else if (NK > 0) {
+            VT xv[V], yv[V];
+            if (NK > 0) {
 #pragma unroll
-              for (int j = 0; j < V; ++j) lv[j] = lcur[ku][j];
-            } else tile_load<T, VT, V>(L, lp + L.k_off[kk], lv);
-            if (R.has_e) tile_load<T, VT, V>(R, rp + R.e_off[e] + R.k_off[kk], rv);
-            else if (NK > 0) {
+              for (int j = 0; j < V; ++j) xv[j] = xcur[ku][j];
+            } else {
+              tile_load<T, VT, V>(X, xp + X.k_off[kk], xv);
+            }
+            if constexpr (kHoist) {
 #pragma unroll
-              for (int j = 0; j < V; ++j) rv[j] = rcur[ku][j];
-            } else tile_load<T, VT, V>(R, rp + R.k_off[kk], rv);
+              for (int j = 0; j < V; ++j) yv[j] = yh[e][ku][j];
+            } else {
+              tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[kk], yv);
+            }
 #pragma unroll
             for (int j = 0; j < V; ++j) {
               if constexpr (kRing == TSG_RING_OR_AND) {
-                acc[j] |= lv[j] & rv[j];
+                acc[j] |= xv[j] & yv[j];
               } else {
-                acc[j] += (AT)lv[j] * (AT)rv[j];
+                acc[j] += (AT)xv[j] * (AT)yv[j];
               }
             }
             if constexpr (kRing == TSG_RING_MODP) {
@@ -484,13 +486,29 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
 #pragma unroll
         for (int ku = 0; ku < KU; ++ku)
 #pragma unroll
-          for (int j = 0; j < V; ++j) {
-            lcur[ku][j] = lnxt[ku][j];
-            rcur[ku][j] = rnxt[ku][j];
-          }
+          for (int j = 0; j < V; ++j) xcur[ku][j] = xnxt[ku][j];
       }
     }
   }
+}
+
+template <int kRing, int V, int NE, int NK>
+__global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
+  const uint32_t g = blockIdx.y;
+  const uint32_t f_hi = blockIdx.x << a.tile_bits;
+  const uint32_t f_lo = threadIdx.x * (uint32_t)V;
+  uint64_t xo[2];
+#pragma unroll
+  for (int o = 0; o < 2; ++o) {
+    const TileOperand& op = a.op[o];
+    xo[o] = op.base + scatter_bits(op.g, g) + scatter32(op.f_hi, f_hi) + scatter32(op.f_lo, f_lo);
+  }
+  const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
+  // at most one operand carries E bits (the other is the one E was chosen against)
+  if (!a.op[0].has_e)
+    tile_thread<kRing, V, NE, NK>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo);
+  else
+    tile_thread<kRing, V, NE, NK>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo);
 }
 
 // ------------------------------------------------------------------------------------
