@@ -160,6 +160,10 @@ constexpr int kModeGather = 0;
 constexpr int kModeContig = 1;
 constexpr int kModeBcast = 2;
 constexpr int kModePair = 3;  // two distinct offsets: 0 and tab[3]; pair_sel picks per position
+// OR-AND, 16 byte positions of which the operand carries c <= 3 of the 4 index bits: the
+// 2^c distinct bytes (offsets dtab) are packed into two words and spread over the four
+// output words with byte permutes (selectors psel)
+constexpr int kModePerm = 4;
 constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
 constexpr int kMaxK = 16;  // summed combinations kept in tables (k <= 4)
 
@@ -179,10 +183,13 @@ struct TileOperand {
   uint32_t tab[16];       // offsets of the V consecutive F positions
   uint32_t e_off[kMaxE];  // offsets of the E combinations
   uint32_t k_off[kMaxK];  // offsets of the summed combinations
-  int32_t mode;           // kModeContig / kModeBcast / kModePair / kModeGather
+  int32_t mode;           // kModeContig / kModeBcast / kModePair / kModeGather / kModePerm
   int32_t pair_sel;       // kModePair: bit j set when position j reads offset tab[3]
   int32_t has_e;          // carries E bits (reloaded per E combination)
   int32_t leaf;           // uint8 leaf (widened on load)
+  int32_t pn;             // kModePerm: distinct values (2, 4 or 8)
+  uint32_t dtab[8];       // kModePerm: their offsets
+  uint32_t psel[4];       // kModePerm: __byte_perm selector of each output word
 };
 
 struct TileArgs {
@@ -300,6 +307,18 @@ __device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t
 #pragma unroll
     for (int j = 0; j < 4; ++j) r |= (((op.pair_sel >> j) & 1) ? x1 : x0) << (8 * j);
     w[0] = r;
+  } else if (V == 16 && op.mode == kModePerm) {
+    uint32_t w0 = 0, w1 = 0;
+#pragma unroll
+    for (int d = 0; d < 8; ++d) {
+      if (d < op.pn) {
+        const uint32_t b = base[off + op.dtab[d]];
+        if (d < 4) w0 |= b << (8 * d);
+        else w1 |= b << (8 * (d - 4));
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < V / 4; ++i) w[i] = __byte_perm(w0, w1, op.psel[i]);
   } else {
 #pragma unroll
     for (int i = 0; i < V / 4; ++i) {
@@ -1195,20 +1214,22 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   const int nf = (int)fbits.size();
   int v = nf >= 2 ? 4 : 1;
   if (ring == TSG_RING_OR_AND && nf >= 4) {
-    // 16 byte-wide positions when every operand and the output take the 4 fastest F bits
-    // as their own 4 fastest bits (vector load) or not at all (broadcast)
+    // 16 byte-wide positions when the output takes the 4 fastest F bits as its 4 fastest
+    // bits and every operand carries them as its own 4 fastest bits (vector load), at most
+    // 3 of them (byte permutes of <= 8 distinct values) or none (broadcast)
     bool ok16 = true;
     for (int b = 0; b < 4 && ok16; ++b) ok16 = fbits[b] == b;
     for (int o = 0; o < 2 && ok16; ++o) {
       int carried = 0;
+      bool ident = true;
       for (int b = 0; b < 4; ++b) {
         const int p = st.pos[o][fbits[b]];
         if (p >= 0) {
           carried++;
-          ok16 = ok16 && p == b;
+          ident = ident && p == b;
         }
       }
-      ok16 = ok16 && (carried == 0 || carried == 4) && (carried == 0 || (d[o].base & 15) == 0);
+      if (carried == 4) ok16 = ident && (d[o].base & 15) == 0;
     }
     if (ok16) v = 16;
   }
@@ -1289,6 +1310,35 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
       if (pair) {
         op.mode = kModePair;
         op.pair_sel = sel;
+      }
+    }
+    if (op.mode == kModeGather && v == 16) {
+      // carried fast F bits (F index, operand bit), ascending F index: distinct value d
+      // has bit k of d = carried bit k of the position
+      std::vector<std::pair<int, int>> cb;
+      for (const auto& pr : lo)
+        if (pr.first < 4) cb.push_back(pr);
+      if (cb.empty() || cb.size() > 3) {
+        *ok = false;  // excluded by the choice of V above
+        return TSG_OK;
+      }
+      op.mode = kModePerm;
+      op.pn = 1 << cb.size();
+      for (int dd = 0; dd < op.pn; ++dd) {
+        uint32_t off = 0;
+        for (size_t k = 0; k < cb.size(); ++k)
+          if ((dd >> k) & 1) off |= 1u << cb[k].second;
+        op.dtab[dd] = off;
+      }
+      for (int i = 0; i < 4; ++i) {
+        uint32_t sel = 0;
+        for (int t = 0; t < 4; ++t) {
+          const int j = 4 * i + t;
+          uint32_t dd = 0;
+          for (size_t k = 0; k < cb.size(); ++k) dd |= (uint32_t)((j >> cb[k].first) & 1) << k;
+          sel |= dd << (4 * t);
+        }
+        op.psel[i] = sel;
       }
     }
     op.has_e = ep.empty() ? 0 : 1;
