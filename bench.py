@@ -199,6 +199,23 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def dominant_traffic(ring: str, step: int, group: int):
+    """DRAM bytes (read + write) of one launch of tree step `step` in `ring`, from the ncu
+    launch list committed under profiles/ for this workload, or None when that capture
+    does not hold this step at this group size."""
+    path = ROOT / "profiles" / "tree_steps_n60_dram.txt"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        parts = line.split("#")[0].split()
+        if len(parts) == 5 and parts[0] == ring and parts[1] == str(step) and parts[2] == str(group):
+            try:
+                return float(parts[4])
+            except ValueError:
+                return None
+    return None
+
+
 def workload_config(args, contraction, group: int) -> dict:
     st = contraction.stats()
     return {
@@ -297,20 +314,31 @@ def run_gb300(args) -> None:
     value = world * args.steps * group / ns / elapsed
     launches_per_step = (npl.launch_count(*slice_range(0), group) * 2)
 
-    # roofline: algorithmic bytes of the step kernels / step time
+    # Roofline of the dominant launch: one more pass over the next slice group with a CUDA
+    # event after every launch (tsg_plan_run_timed); the tree step with the largest device
+    # time in either ring is the dominant launch, and its algorithmic bytes (operands read
+    # once, result written once, x the slices of the group) / its event time is `achieved`.
     sp = contraction.sliced_plan
-    bytes_count = sp.bytes_per_slice(4, NUM_PRIMES) * group
-    bytes_sat = sp.bytes_per_slice(1, 1) * group
     step_s = elapsed / args.steps
     peak, peak_kind = measured_peaks()
-    achieved = (bytes_count + bytes_sat) / step_s / 1e9
-    traffic = None
-    tfile = ROOT / "profiles" / "traffic_n60.json"
-    if tfile.exists():
-        try:
-            traffic = json.loads(tfile.read_text()).get("dram_bytes_per_step_scaled")
-        except Exception:
-            traffic = None
+    b, e = slice_range(args.warmup + args.steps)
+    timing_passes = 2
+    acc_ms = {"modp": None, "or_and": None}
+    for _ in range(timing_passes):
+        for name, ring, pr, ws, res in (("modp", _native.TSG_RING_MODP, primes, ws_count, res_count),
+                                        ("or_and", _native.TSG_RING_OR_AND, (), ws_sat, res_sat)):
+            ms = npl.run_timed(ring, pr, pool_dev, b, e, group, ws, res, False, sh)
+            acc_ms[name] = ms if acc_ms[name] is None else [x + y for x, y in zip(acc_ms[name], ms)]
+    step_bytes = {"modp": sp.step_bytes_per_slice(4, NUM_PRIMES), "or_and": sp.step_bytes_per_slice(1, 1)}
+    nsteps = len(step_bytes["modp"])
+    ring_name, dom = max(((r, s) for r in acc_ms for s in range(nsteps)),
+                         key=lambda rs: acc_ms[rs[0]][rs[1]])
+    dom_ms = acc_ms[ring_name][dom] / timing_passes
+    dom_bytes = step_bytes[ring_name][dom] * group
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    step_total_ms = sum(sum(v) for v in acc_ms.values()) / timing_passes
+    traffic = dominant_traffic(ring_name, dom, group)
+    step_roofline = (sp.bytes_per_slice(4, NUM_PRIMES) + sp.bytes_per_slice(1, 1)) * group / step_s / 1e9
 
     # end to end through the public API: host leaves in, host results out, every step
     e2e_times = []
@@ -347,7 +375,11 @@ def run_gb300(args) -> None:
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_kind,
-                         "kernel": "tree_step_kernel (all steps of a slice group)"},
+                         "kernel": f"tree step {dom} of the {ring_name} run (the launch with the "
+                                   f"largest device time, {dom_ms:.2f} ms of "
+                                   f"{step_total_ms:.1f} ms per step)",
+                         "algorithmic_bytes": dom_bytes,
+                         "step_achieved": step_roofline},
             "cpu_baseline": cpu,
             "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                      "d2h_bytes_per_step": d2h} if e2e_value is not None else None),

@@ -167,6 +167,18 @@ TSG_API tsg_status tsg_plan_run(const tsg_plan* plan, int32_t ring, int32_t num_
                         void* workspace_dev, int64_t workspace_bytes, void* result_dev,
                         int32_t accumulate, void* stream);
 
+/* tsg_plan_run that also measures: a CUDA event is recorded on `stream` before the first
+ * launch and after every launch, and on return (the call waits for the run to finish)
+ * step_ms[s] holds the device time of tree step s summed over the slice groups of the
+ * call, step_ms[num_steps] that of the root reductions (caller array of num_steps + 1
+ * floats). For profiling: the events add a few microseconds per launch. No counterpart
+ * in the reference, which has no device execution to time. */
+TSG_API tsg_status tsg_plan_run_timed(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                              const uint32_t* primes, const uint8_t* leaf_pool_dev,
+                              int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                              void* workspace_dev, int64_t workspace_bytes, void* result_dev,
+                              int32_t accumulate, void* stream, float* step_ms);
+
 /* Builds every launch tsg_plan_run would issue for these arguments and checks, on the
  * host, that each operand offset stays inside its leaf or workspace buffer. Touches no
  * device memory and needs no GPU. */

@@ -43,6 +43,7 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_root_bits",
     "tsg_plan_launch_count",
     "tsg_plan_run",
+    "tsg_plan_run_timed",
     "tsg_plan_validate",
     "tsg_take_device_error",
     "tsg_static_scratch_bytes",
@@ -106,6 +107,10 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_run.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_void_p,
                                  c_int64, c_int64, c_int64, c_void_p, c_int64, c_void_p,
                                  c_int32, c_void_p]
+    lib.tsg_plan_run_timed.restype = c_int32
+    lib.tsg_plan_run_timed.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_void_p,
+                                       c_int64, c_int64, c_int64, c_void_p, c_int64, c_void_p,
+                                       c_int32, c_void_p, POINTER(ctypes.c_float)]
     lib.tsg_take_device_error.restype = c_int32
     lib.tsg_take_device_error.argtypes = [c_void_p]
     lib.tsg_static_scratch_bytes.restype = c_int64

@@ -242,6 +242,23 @@ class NativePlan:
         )
         _native.check(st)
 
+    def run_timed(self, ring: int, primes: Sequence[int], pool: torch.Tensor, begin: int,
+                  end: int, group: int, workspace: torch.Tensor, result: torch.Tensor,
+                  accumulate: bool, stream: int) -> list[float]:
+        """:meth:`run` with CUDA events around every launch; waits for the run and returns
+        the device milliseconds of each tree step (summed over slice groups), followed by
+        those of the root reductions."""
+        parr = (_native.c_uint32 * max(1, len(primes)))(*primes)
+        n = len(self._arrs["step_out_bits"])
+        ms = (_native.ctypes.c_float * (n + 1))()
+        st = self._lib.tsg_plan_run_timed(
+            self.handle, ring, len(primes), parr, pool.data_ptr(), begin, end, group,
+            workspace.data_ptr(), workspace.numel(), result.data_ptr(), int(bool(accumulate)),
+            stream, ms,
+        )
+        _native.check(st)
+        return list(ms)
+
     def __del__(self) -> None:
         h = getattr(self, "handle", None)
         if h is not None and h.value:

@@ -1713,14 +1713,44 @@ tsg_status check_range(const tsg_plan* plan, int64_t slice_begin, int64_t slice_
 namespace tsg {
 namespace {
 
-// Shared body of tsg_plan_run and tsg_plan_validate. With dry == true no pointer is
-// dereferenced and nothing is launched: every launch's arguments are built and
-// bounds-checked only.
+// Per-launch device times of one run (tsg_plan_run_timed): an event is recorded on the
+// run's stream before the first launch and after every launch; launch i took
+// elapsed(ev[i], ev[i + 1]) and belongs to step ids[i] (num_steps: root reduction).
+struct RunTimer {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ids;
+  ~RunTimer() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+  tsg_status record(cudaStream_t stream, int id) {
+    cudaEvent_t e;
+    TSG_CUDA_TRY(cudaEventCreate(&e));
+    ev.push_back(e);
+    if (id >= 0) ids.push_back(id);
+    TSG_CUDA_TRY(cudaEventRecord(e, stream));
+    return TSG_OK;
+  }
+  tsg_status collect(int num_steps, float* step_ms) {
+    for (int s = 0; s <= num_steps; ++s) step_ms[s] = 0.f;
+    if (ev.empty()) return TSG_OK;
+    TSG_CUDA_TRY(cudaEventSynchronize(ev.back()));
+    for (size_t i = 0; i + 1 < ev.size(); ++i) {
+      float ms = 0.f;
+      TSG_CUDA_TRY(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+      step_ms[ids[i]] += ms;
+    }
+    return TSG_OK;
+  }
+};
+
+// Shared body of tsg_plan_run, tsg_plan_run_timed and tsg_plan_validate. With dry == true
+// no pointer is dereferenced and nothing is launched: every launch's arguments are built
+// and bounds-checked only. With a timer, every launch is followed by an event record.
 tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
                     const uint32_t* primes, const uint8_t* pool, int64_t slice_begin,
                     int64_t slice_end, int64_t group_size, void* workspace,
                     int64_t workspace_bytes, void* result_dev, int32_t accumulate,
-                    cudaStream_t stream, bool dry) {
+                    cudaStream_t stream, bool dry, RunTimer* timer = nullptr) {
   TSG_TRY(check_range(plan, slice_begin, slice_end, group_size));
   int64_t eb;
   int planes;
@@ -1761,23 +1791,33 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
   c.g_bits = 0;
   while ((int64_t(1) << c.g_bits) < group_size) c.g_bits++;
   const int ns = (int)plan->steps.size();
+  if (timer && !dry) TSG_TRY(timer->record(stream, -1));
+  auto timed = [&](int id) -> tsg_status {
+    return (timer && !dry) ? timer->record(stream, id) : TSG_OK;
+  };
   auto step = [&](int s, int64_t base, int64_t cnt) -> tsg_status {
-    if (!dry) return launch_step(c, s, base, cnt);
-    LaunchArgs la;
-    return build_step(c, s, base, cnt, &la);
+    if (dry) {
+      LaunchArgs la;
+      return build_step(c, s, base, cnt, &la);
+    }
+    TSG_TRY(launch_step(c, s, base, cnt));
+    return timed(s);
+  };
+  auto reduce = [&](int64_t cnt, uint8_t* result, int acc) -> tsg_status {
+    if (dry) return TSG_OK;
+    TSG_TRY(launch_reduce(c, cnt, result, acc));
+    return timed(ns);
   };
   for (int s = 0; s < ns; ++s)
     if (!plan->steps[s].dep) TSG_TRY(step(s, 0, 1));
   uint8_t* result = (uint8_t*)result_dev;
-  if (!plan->steps.back().dep) {
-    return dry ? TSG_OK : launch_reduce(c, 1, result, accumulate);
-  }
+  if (!plan->steps.back().dep) return reduce(1, result, accumulate);
   bool first = true;
   for (int64_t base = slice_begin; base < slice_end; base += group_size) {
     const int64_t cnt = std::min<int64_t>(group_size, slice_end - base);
     for (int s = 0; s < ns; ++s)
       if (plan->steps[s].dep) TSG_TRY(step(s, base, cnt));
-    if (!dry) TSG_TRY(launch_reduce(c, cnt, result, first ? accumulate : 1));
+    TSG_TRY(reduce(cnt, result, first ? accumulate : 1));
     first = false;
   }
   return TSG_OK;
@@ -1974,6 +2014,20 @@ tsg_status tsg_plan_run(const tsg_plan* plan, int32_t ring, int32_t num_primes,
   return run_impl(plan, ring, num_primes, primes, leaf_pool_dev, slice_begin, slice_end,
                   group_size, workspace_dev, workspace_bytes, result_dev, accumulate,
                   (cudaStream_t)stream, /*dry=*/false);
+}
+
+tsg_status tsg_plan_run_timed(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                              const uint32_t* primes, const uint8_t* leaf_pool_dev,
+                              int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                              void* workspace_dev, int64_t workspace_bytes, void* result_dev,
+                              int32_t accumulate, void* stream, float* step_ms) {
+  if (!plan || !leaf_pool_dev || !result_dev || !step_ms)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run_timed: null pointer");
+  RunTimer timer;
+  TSG_TRY(run_impl(plan, ring, num_primes, primes, leaf_pool_dev, slice_begin, slice_end,
+                   group_size, workspace_dev, workspace_bytes, result_dev, accumulate,
+                   (cudaStream_t)stream, /*dry=*/false, &timer));
+  return timer.collect((int)plan->steps.size(), step_ms);
 }
 
 tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_primes,

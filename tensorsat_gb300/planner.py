@@ -460,18 +460,25 @@ class SlicedPlan:
             "step_rhs_pos": np.ascontiguousarray(pos[1]),
         }
 
-    def bytes_per_slice(self, elem_bytes: int, planes: int = 1) -> float:
-        """Algorithmic HBM bytes of one slice: each step reads both operands once and
-        writes its result once (leaves are uint8, other tensors elem_bytes * planes)."""
+    def step_bytes_per_slice(self, elem_bytes: int, planes: int = 1) -> list[float]:
+        """Algorithmic HBM bytes of each step for one slice: the step reads both operands
+        once and writes its result once (leaves are uint8, other tensors elem_bytes *
+        planes)."""
         t = self.tree
         L = t.num_leaves
         sl = frozenset(self.sliced)
-        tot = 0.0
+        out = []
         for s, (a, b) in enumerate(t.steps):
+            tot = 0.0
             for x in (a, b):
                 if x < L:
                     tot += 2.0 ** len(t.node_wires[x] - sl)
                 else:
                     tot += 2.0 ** len(t.node_wires[x] - sl) * elem_bytes * planes
             tot += 2.0 ** len(t.node_wires[L + s] - sl) * elem_bytes * planes
-        return tot
+            out.append(tot)
+        return out
+
+    def bytes_per_slice(self, elem_bytes: int, planes: int = 1) -> float:
+        """Algorithmic HBM bytes of one slice, all steps (see step_bytes_per_slice)."""
+        return float(sum(self.step_bytes_per_slice(elem_bytes, planes)))

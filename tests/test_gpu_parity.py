@@ -267,3 +267,28 @@ def test_sliced_count_properties(cuda, n, m, seed, target):
     fixed = {w: (sid >> j) & 1 for j, w in enumerate(sl)}
     assert int(r.cpu().numpy().view(np.uint64)[0]) * c1.discard_factor == orc.cnf_count_by_tree(
         n, cnf.clauses, c1.tree.steps, fixed=fixed)
+
+
+def test_timed_run_matches_plain_run(cuda):
+    """tsg_plan_run_timed gives the results of tsg_plan_run (integers: equality) and one
+    non-negative device time per tree step plus the root reductions."""
+    cnf = CNFInstance.random(3, 30, 128, rng=4)
+    d = cnf.clause_diagram()
+    c = GpuContraction(CudaRel, d.wiring, target_bits=14, trials=2)
+    npl = c.native_plan()
+    ns = c.num_slices
+    group = min(8, ns)
+    pool = c.leaf_pool(d)
+    stream = torch.cuda.current_stream().cuda_stream
+    for ring, primes, nres, dt in [(_native.TSG_RING_MODP, PRIMES_31[:3], 3, torch.int32),
+                                   (_native.TSG_RING_OR_AND, (), 1, torch.uint8)]:
+        ws = torch.empty(npl.workspace_bytes(ring, max(1, len(primes)), group),
+                         dtype=torch.uint8, device=cuda)
+        plain = torch.zeros(nres, dtype=dt, device=cuda)
+        timed = torch.zeros(nres, dtype=dt, device=cuda)
+        npl.run(ring, primes, pool, 0, ns, group, ws, plain, False, stream)
+        ms = npl.run_timed(ring, primes, pool, 0, ns, group, ws, timed, False, stream)
+        torch.cuda.synchronize()
+        assert torch.equal(plain, timed)
+        assert len(ms) == len(c.tree.steps) + 1
+        assert all(x >= 0 for x in ms) and sum(ms) > 0
