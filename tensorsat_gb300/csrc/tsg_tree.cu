@@ -72,6 +72,27 @@ __device__ __forceinline__ uint32_t mont_finish(uint64_t acc, int leaves, const 
   return mont_redc(acc, ring.p[p], ring.pinv[p]);
 }
 
+// One plane's constants, selected from the kernel parameters without dynamic indexing
+// (which would copy the parameter block to local memory).
+struct PlaneConst {
+  uint32_t p, pinv, r1;
+};
+
+__device__ __forceinline__ PlaneConst plane_const(const RingArgs& ring, int p) {
+  PlaneConst c{ring.p[0], ring.pinv[0], ring.r1[0]};
+#pragma unroll
+  for (int i = 1; i < TSG_MAX_PRIMES; ++i)
+    if (p == i) c = PlaneConst{ring.p[i], ring.pinv[i], ring.r1[i]};
+  return c;
+}
+
+// mont_finish with the plane's constants in registers.
+__device__ __forceinline__ uint32_t mont_finish_c(uint64_t acc, int leaves, const PlaneConst& c) {
+  if (leaves == 2) return small_mod(acc * c.r1, c.p);
+  if (leaves == 1) return small_mod(acc, c.p);
+  return mont_redc(acc, c.p, c.pinv);
+}
+
 __device__ __forceinline__ uint64_t scatter_bits(const BitMap& m, uint64_t x) {
   uint64_t r = 0;
 #pragma unroll 1
@@ -348,7 +369,7 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
   constexpr int KU = NK > 0 ? NK : 1;
   const int nk = NK > 0 ? NK : a.n_k;
   if constexpr (kPacked) {
-    constexpr bool kHoist = NK > 0 && NE * KU * W <= 32;
+    constexpr bool kHoist = NK > 0 && NE * KU * W <= 16;  // more spills registers
     uint32_t xw[KU][W];
     uint32_t yh[kHoist ? NE : 1][KU][W];
     if (NK > 0) {
@@ -404,7 +425,7 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
   } else {
     // planes outermost; X of plane p+1 is loaded while plane p is combined
     constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
-    constexpr bool kHoist = NK > 0 && NE * KU * V * sizeof(VT) <= 128;
+    constexpr bool kHoist = NK > 0 && NE * KU * V * sizeof(VT) <= 64;  // more spills registers
     const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
     const int leaves = X.leaf + Y.leaf;
     VT xcur[KU][V], xnxt[KU][V];
@@ -532,17 +553,26 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
 
 // ------------------------------------------------------------------------------------
 // Streaming kernel for the large steps (the bulk of the HBM traffic). Persistent blocks
-// walk the (tile, slice) work items; thread 0 stages the E-free operand's tile for the
-// next item (every residue plane and summed combination: contiguous 4 KB chunks) into
-// shared memory with TMA bulk copies (cp.async.bulk ... mbarrier::complete_tx) while the
-// block combines the current item from the other stage. The other operand (small, cached
-// in L2) is read with ordinary loads as in the tile kernel; outputs are written from
-// registers. Every mbarrier wait is bounded: on expiry the block records an error in
-// g_device_error, waits (bounded) for its own copies in flight, and returns.
+// walk the (tile, slice) work items with a warp-specialised pipeline:
+//   * an item is one residue plane of one 1024-element tile of one slice;
+//   * a producer warp stages items into a ring of `stages` shared-memory stages with TMA
+//     bulk copies (cp.async.bulk ... mbarrier::complete_tx): the E-free operand's tile
+//     for every summed combination and, where its offsets allow (s_span > 0), the other
+//     operand's aligned blocks for the tile, plus the item's offsets in a stage header;
+//   * 8 consumer warps (4 positions per thread) combine an item from its stage, write the
+//     result from registers as 16-byte vectors, and release the stage (one arrival per
+//     warp on the stage's `empty` barrier); nothing else synchronises the block.
+// Every mbarrier wait is bounded: on expiry the thread records an error in
+// g_device_error and sets the block's bail flag; the producer then waits (bounded) for
+// the copies it has in flight and every thread returns.
 
-constexpr int kStreamTileBits = 10;                    // 256 threads x 4 positions
+constexpr int kStreamTileBits = 10;                      // 256 consumer threads x 4
 constexpr int kStreamTile = 1 << kStreamTileBits;
-constexpr long long kSpinLimit = 1ll << 24;            // try_wait polls per wait
+constexpr int kStreamConsumers = 256;
+constexpr int kStreamThreads = kStreamConsumers + 32;    // + the producer warp
+constexpr int kStreamMaxStages = 8;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;         // one bounded wait: 2 s
+constexpr uint32_t kSuspendHintNs = 20000;               // longest suspension per try_wait
 
 __device__ int g_device_error = 0;  // 0 = ok, else TSG_ERR_TIMEOUT
 
@@ -561,6 +591,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -573,11 +607,45 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for phase `parity` of `bar`; false when the limit expired.
+// try_wait that may suspend the thread in hardware for up to kSuspendHintNs while the
+// phase is incomplete, instead of returning at once (no issue slots spent polling).
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendHintNs)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for phase `parity` of `bar`: false when kWaitLimitNs of wall-clock time
+// (the global nanosecond timer) passed without the phase completing.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (long long i = 0; i < kSpinLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
+  if (mbar_try_wait_suspend(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait_suspend(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+// Warp-uniform bounded wait (every lane of the warp calls it): lane 0 polls, the outcome
+// is broadcast, and on success every lane observes the completed phase itself (acquire).
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity) {
+  int ok = 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  if (ok) (void)mbar_try_wait(bar, parity);
+  return ok != 0;
 }
 
 __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes,
@@ -596,6 +664,15 @@ struct StreamArgs {
   uint32_t chunk_bytes;  // one (plane, summed combination) chunk of the staged operand
   uint32_t s_span;       // elements of one staged chunk of the other operand per (plane, E
                          // combination, summed combination); 0: read from global memory
+  uint32_t stage_bytes;  // one stage: the item's chunks of both operands
+  int32_t stages;        // stages in the ring (2 .. kStreamMaxStages)
+};
+
+// Offsets of one staged item, written by the producer next to its stage.
+struct StreamItem {
+  uint64_t so;  // the other operand's offset for the tile and plane (positions excluded)
+  uint64_t oo;  // output offset for the tile and plane (positions excluded)
+  int32_t p;    // residue plane
 };
 
 // Loads the V values of the other operand from its staged chunk: `p` points at the
@@ -632,142 +709,176 @@ __device__ __forceinline__ void smem_load(const TileOperand& op, const T* p, T (
 }
 
 template <int kRing, int NE, int NK>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kStreamThreads, 3)
     tree_step_stream_kernel(TileArgs a, RingArgs ring, StreamArgs sa) {
   using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
-  using VT = T;
   constexpr int V = 4;
-  constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
   constexpr int KU = NK;  // NK in {1, 2}
   extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bars[2];
-  __shared__ int bail;
+  __shared__ __align__(8) uint64_t full[kStreamMaxStages], empty[kStreamMaxStages];
+  __shared__ StreamItem head[kStreamMaxStages];
+  __shared__ volatile int bail;
   const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
   const TileOperand& B = a.op[sa.big];
   const TileOperand& S = a.op[1 - sa.big];
-  const int leaves = a.op[0].leaf + a.op[1].leaf;
   const bool s_staged = sa.s_span != 0;
-  const uint32_t b_bytes = (uint32_t)(np * KU) * sa.chunk_bytes;
+  const uint32_t b_bytes = (uint32_t)KU * sa.chunk_bytes;
   const uint32_t s_chunk = sa.s_span * (uint32_t)sizeof(T);
-  const uint32_t stage_bytes = b_bytes + (s_staged ? (uint32_t)(np * NE * KU) * s_chunk : 0u);
-  const uint32_t f_lo = threadIdx.x * V;
-  const uint64_t s_lo = scatter32(S.f_lo, f_lo);
-  const uint64_t o_lo = scatter32(a.of_lo, f_lo);
+  const int nst = sa.stages;
+  const uint64_t items = sa.work * (uint64_t)np;  // (tile, slice, residue plane)
   const int lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int s = 0; s < nst; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kStreamConsumers / 32);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     bail = 0;
   }
   __syncthreads();
 
-  // so: the other operand's offset for the tile, without the thread's own positions
-  auto item_offsets = [&](uint64_t w, uint64_t* bo, uint64_t* so, uint64_t* oo) {
-    const uint32_t g = (uint32_t)(w / sa.tiles);
-    const uint32_t f_hi = (uint32_t)(w % sa.tiles) << kStreamTileBits;
-    *bo = B.base + scatter_bits(B.g, g) + scatter32(B.f_hi, f_hi);
-    *so = S.base + scatter_bits(S.g, g) + scatter32(S.f_hi, f_hi);
-    *oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + o_lo;
-  };
-  // Run by warp 0: lane 0 arms the stage's barrier with the byte count, then the lanes
-  // issue the bulk copies (np x KU tiles of B, np x NE x KU chunks of the other operand).
-  auto issue = [&](uint64_t w, int stage) {
-    uint64_t bo, so, oo;
-    item_offsets(w, &bo, &so, &oo);
-    uint8_t* dst = smem + stage * stage_bytes;
-    if (lane == 0) mbar_expect_tx(&bars[stage], stage_bytes);
-    __syncwarp();
+  if (threadIdx.x >= kStreamConsumers) {
+    // producer warp: lane 0 writes the item's offsets into the stage header and arms the
+    // stage's barrier with the byte count (its arrival releases the header), then the
+    // lanes issue the bulk copies (KU tiles of B, NE x KU blocks of the other operand)
     const T* bsrc = reinterpret_cast<const T*>(B.ptr);
     const T* ssrc = reinterpret_cast<const T*>(S.ptr);
-    const int nb = np * KU;
-    const int ncopies = nb + (s_staged ? np * NE * KU : 0);
-    for (int i = lane; i < ncopies; i += 32) {
-      if (i < nb) {
-        const int p = i / KU, ku = i % KU;
-        tma_load_1d(dst + i * sa.chunk_bytes, bsrc + bo + p * B.plane + B.k_off[ku],
-                    sa.chunk_bytes, &bars[stage]);
-      } else {
-        const int j = i - nb;
-        const int p = j / (NE * KU), e = (j / KU) % NE, ku = j % KU;
-        tma_load_1d(dst + b_bytes + j * s_chunk,
-                    ssrc + so + p * S.plane + S.e_off[e] + S.k_off[ku], s_chunk, &bars[stage]);
+    const int ncopies = KU + (s_staged ? NE * KU : 0);
+    const uint64_t stride = gridDim.x;
+    uint64_t i = 0;  // items issued by this block
+    bool stop = false;
+    for (uint64_t w0 = blockIdx.x; w0 < items && !stop; w0 += 32 * stride) {
+      // lane L computes the offsets of the block's item w0 + L * stride
+      const uint64_t wl = w0 + (uint64_t)lane * stride;
+      uint64_t l_bo = 0, l_so = 0, l_oo = 0;
+      int l_p = 0;
+      if (wl < items) {
+        l_p = (int)(wl % np);
+        const uint64_t tw = wl / np;
+        const uint32_t g = (uint32_t)(tw / sa.tiles);
+        const uint32_t f_hi = (uint32_t)(tw % sa.tiles) << kStreamTileBits;
+        l_bo = B.base + scatter_bits(B.g, g) + scatter32(B.f_hi, f_hi) + l_p * B.plane;
+        l_so = S.base + scatter_bits(S.g, g) + scatter32(S.f_hi, f_hi) + (S.leaf ? 0 : l_p * S.plane);
+        l_oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + l_p * a.o_plane;
+      }
+      const uint64_t left = (items - w0 + stride - 1) / stride;
+      const int nb = (int)(left < 32 ? left : 32);
+      for (int k = 0; k < nb; ++k, ++i) {
+        const int s = (int)(i % nst);
+        const uint32_t round = (uint32_t)(i / nst);
+        const uint64_t bo = __shfl_sync(0xffffffffu, l_bo, k);
+        const uint64_t so = __shfl_sync(0xffffffffu, l_so, k);
+        const uint64_t oo = __shfl_sync(0xffffffffu, l_oo, k);
+        const int p = __shfl_sync(0xffffffffu, l_p, k);
+        if (__shfl_sync(0xffffffffu, (int)bail, 0)) {
+          stop = true;
+          break;
+        }
+        if (round > 0 && !mbar_wait_warp(&empty[s], (round - 1) & 1)) {
+          if (lane == 0) {
+            atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
+            bail = 1;
+          }
+          stop = true;
+          break;
+        }
+        uint8_t* dst = smem + (size_t)s * sa.stage_bytes;
+        if (lane == 0) {
+          head[s].so = so;
+          head[s].oo = oo;
+          head[s].p = p;
+          mbar_expect_tx(&full[s], sa.stage_bytes);
+        }
+        __syncwarp();
+        for (int c = lane; c < ncopies; c += 32) {
+          if (c < KU) {
+            tma_load_1d(dst + c * sa.chunk_bytes, bsrc + bo + B.k_off[c], sa.chunk_bytes, &full[s]);
+          } else {
+            const int j = c - KU;
+            const int e = j / KU, ku = j % KU;
+            tma_load_1d(dst + b_bytes + j * s_chunk, ssrc + so + S.e_off[e] + S.k_off[ku], s_chunk,
+                        &full[s]);
+          }
+        }
       }
     }
-  };
-
-  uint64_t w = blockIdx.x;
-  if (threadIdx.x < 32 && w < sa.work) issue(w, 0);
-  uint32_t phase[2] = {0, 0};
-  for (int it = 0; w < sa.work; ++it, w += gridDim.x) {
-    const int stage = it & 1;
-    const uint64_t wn = w + gridDim.x;
-    if (threadIdx.x < 32 && wn < sa.work) issue(wn, stage ^ 1);
-    if (!mbar_wait_bounded(&bars[stage], phase[stage])) {
-      atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
-      bail = 1;
+    // the copies of the last (up to) nst items may still be in flight: wait for them
+    if (lane == 0) {
+      const uint64_t first = i > (uint64_t)nst ? i - nst : 0;
+      for (uint64_t j = first; j < i; ++j)
+        (void)mbar_wait_bounded(&full[j % nst], (uint32_t)((j / nst) & 1));
     }
-    phase[stage] ^= 1;
-    __syncthreads();
-    if (bail) {
-      // drain: the copies issued for the other stage must land before the block exits
-      if (threadIdx.x == 0 && wn < sa.work) (void)mbar_wait_bounded(&bars[stage ^ 1], phase[stage ^ 1]);
+    return;
+  }
+
+  // consumer warps: one residue plane of one tile per item
+  const int leaves = a.op[0].leaf + a.op[1].leaf;
+  const uint32_t f_lo = threadIdx.x * V;
+  const uint64_t s_lo = scatter32(S.f_lo, f_lo);
+  const uint64_t o_lo = scatter32(a.of_lo, f_lo);
+  uint64_t i = 0;
+  for (uint64_t w = blockIdx.x; w < items; w += gridDim.x, ++i) {
+    const int s = (int)(i % nst);
+    if (__shfl_sync(0xffffffffu, (int)bail, 0)) return;
+    if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
+      if (lane == 0) {
+        atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
+        bail = 1;
+      }
       return;
     }
-    uint64_t bo, so, oo;
-    item_offsets(w, &bo, &so, &oo);
-    const uint8_t* st = smem + stage * stage_bytes;
+    const uint64_t so = head[s].so;
+    const uint64_t oo = head[s].oo + o_lo;
+    const PlaneConst pc = plane_const(ring, head[s].p);
+    const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
+    T bv[KU][V];
 #pragma unroll
-    for (int p = 0; p < PP; ++p) {
-      if (p >= np) break;
-      VT bv[KU][V];
-#pragma unroll
-      for (int ku = 0; ku < KU; ++ku) {
-        const T* src = reinterpret_cast<const T*>(st + (p * KU + ku) * sa.chunk_bytes) + f_lo;
-        if constexpr (sizeof(T) == 4) {
-          const uint4 x = *reinterpret_cast<const uint4*>(src);
-          bv[ku][0] = x.x;
-          bv[ku][1] = x.y;
-          bv[ku][2] = x.z;
-          bv[ku][3] = x.w;
-        } else {
-          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
-          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
-          bv[ku][0] = x0.x;
-          bv[ku][1] = x0.y;
-          bv[ku][2] = x1.x;
-          bv[ku][3] = x1.y;
-        }
-      }
-      const uint64_t sp = so + s_lo + (S.leaf ? 0 : p * S.plane);
-      const T* ss = reinterpret_cast<const T*>(st + b_bytes) + (uint64_t)p * NE * KU * sa.s_span + s_lo;
-#pragma unroll
-      for (int e = 0; e < NE; ++e) {
-        uint64_t acc[V] = {0, 0, 0, 0};
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku) {
-          VT sv[V];
-          if (s_staged) smem_load<T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
-          else tile_load<T, VT, V>(S, sp + S.e_off[e] + S.k_off[ku], sv);
-#pragma unroll
-          for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
-        }
-        const uint64_t oe = oo + a.o_e[e];
-        if constexpr (kRing == TSG_RING_U64) {
-          uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
-          reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[0], acc[1]);
-          reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[2], acc[3]);
-        } else {
-          uint32_t r[V];
-#pragma unroll
-          for (int j = 0; j < V; ++j) r[j] = mont_finish(acc[j], leaves, ring, p);
-          *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane + oe) =
-              make_uint4(r[0], r[1], r[2], r[3]);
-        }
+    for (int ku = 0; ku < KU; ++ku) {
+      const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
+      if constexpr (sizeof(T) == 4) {
+        const uint4 x = *reinterpret_cast<const uint4*>(src);
+        bv[ku][0] = x.x;
+        bv[ku][1] = x.y;
+        bv[ku][2] = x.z;
+        bv[ku][3] = x.w;
+      } else {
+        const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
+        const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
+        bv[ku][0] = x0.x;
+        bv[ku][1] = x0.y;
+        bv[ku][2] = x1.x;
+        bv[ku][3] = x1.y;
       }
     }
-    __syncthreads();  // the stage is refilled two items later
+    const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      uint64_t acc[V] = {0, 0, 0, 0};
+#pragma unroll
+      for (int ku = 0; ku < KU; ++ku) {
+        T sv[V];
+        if (s_staged) smem_load<T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
+        else tile_load<T, T, V>(S, so + s_lo + S.e_off[e] + S.k_off[ku], sv);
+#pragma unroll
+        for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
+      }
+      const uint64_t oe = oo + a.o_e[e];
+      if constexpr (kRing == TSG_RING_U64) {
+        uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
+        reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[0], acc[1]);
+        reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[2], acc[3]);
+      } else {
+        uint32_t r[V];
+#pragma unroll
+        for (int j = 0; j < V; ++j) r[j] = mont_finish_c(acc[j], leaves, pc);
+        *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
+            make_uint4(r[0], r[1], r[2], r[3]);
+      }
+    }
+    // release the stage: every lane of the warp is done reading it
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
   }
 }
 
@@ -1434,13 +1545,14 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
 // as whole 1024-element tiles: its first 10 F bits are its own bits 0-9, every other
 // offset term is a multiple of 1024 elements (so each chunk is contiguous and 16-byte
 // aligned for TMA), and the tile kernel would use 256 threads x 4 positions.
-// Shared memory of one streaming block, both stages, when the other operand is staged as
-// well: three blocks per SM.
-constexpr uint64_t kStreamSmemBudget = 72 * 1024;
+// Dynamic shared memory of one streaming block (its ring of stages): three blocks per SM.
+constexpr uint64_t kStreamBlockSmem = 72 * 1024;
+constexpr int kStreamBlocksPerSm = 3;
 
-uint64_t stream_smem_bytes(int np, int ne, int nk, uint32_t chunk_bytes, uint32_t span,
-                           uint32_t esize) {
-  return 2ull * np * ((uint64_t)nk * chunk_bytes + (uint64_t)ne * nk * span * esize);
+// Bytes of one stage (one residue plane of one tile): the staged operand's tile per
+// summed combination and, with span > 0, the other operand's blocks.
+uint64_t stream_stage_bytes(int ne, int nk, uint32_t chunk_bytes, uint32_t span, uint32_t esize) {
+  return (uint64_t)nk * chunk_bytes + (uint64_t)ne * nk * span * esize;
 }
 
 // Span of the staged chunks of the other operand of a streamed step, or 0 (plain loads).
@@ -1475,8 +1587,8 @@ uint32_t stream_span(const LaunchArgs& la, int np, uint32_t esize, uint64_t exte
   const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
   const uint64_t end = s.base + scatter_max(s.g, gbits) + narrow_max(s.f_hi, nbits) + eo + ko + span;
   ok = ok && end <= extent;
-  ok = ok && stream_smem_bytes(np, sh.ne, sh.nk, la.stream.chunk_bytes, span, esize) <=
-                 kStreamSmemBudget;
+  ok = ok && 2 * stream_stage_bytes(sh.ne, sh.nk, la.stream.chunk_bytes, span, esize) <=
+                 kStreamBlockSmem;
   return ok ? span : 0;
 }
 
@@ -1512,6 +1624,11 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   la.stream.work = sh.tiles * la.cnt;
   la.stream.chunk_bytes = kStreamTile * esize;
   la.stream.s_span = stream_span(la, np, esize, extent[1 - big]);
+  const uint64_t stage = stream_stage_bytes(sh.ne, sh.nk, la.stream.chunk_bytes,
+                                            la.stream.s_span, esize);
+  if (2 * stage > kStreamBlockSmem) return;  // fewer than two stages fit
+  la.stream.stage_bytes = (uint32_t)stage;
+  la.stream.stages = (int)std::min<uint64_t>(kStreamMaxStages, kStreamBlockSmem / stage);
   la.streamed = true;
 }
 
@@ -1592,21 +1709,22 @@ void launch_tile_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st)
 template <int kRing, int NE, int NK>
 tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
   auto kernel = tree_step_stream_kernel<kRing, NE, NK>;
-  const int np = kRing == TSG_RING_MODP ? ra.np : 1;
-  const size_t smem = stream_smem_bytes(np, NE, NK, la.stream.chunk_bytes, la.stream.s_span,
-                                        kRing == TSG_RING_U64 ? 8 : 4);
+  const size_t smem = (size_t)la.stream.stages * la.stream.stage_bytes;
+  if (la.stream.stages < 2 || la.stream.stages > kStreamMaxStages || smem > kStreamBlockSmem)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "stream kernel: stage ring outside its limits");
   static bool configured[64] = {};  // one attribute call per instantiation and device
   int dev = 0;
   TSG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(TSG_ERR_UNSUPPORTED, "device ordinal outside 0..63");
   if (!configured[dev]) {
-    const int max_smem = 2 * TSG_MAX_PRIMES * 2 * kStreamTile * 8;
     TSG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      max_smem));
+                                      (int)kStreamBlockSmem));
     configured[dev] = true;
   }
-  const uint64_t blocks = std::min<uint64_t>(la.stream.work, (uint64_t)device_sm_count() * 3);
-  kernel<<<(unsigned)blocks, kThreads, smem, st>>>(la.t, ra, la.stream);
+  const int np = kRing == TSG_RING_MODP ? ra.np : 1;
+  const uint64_t blocks = std::min<uint64_t>(la.stream.work * np,
+                                             (uint64_t)device_sm_count() * kStreamBlocksPerSm);
+  kernel<<<(unsigned)blocks, kStreamThreads, smem, st>>>(la.t, ra, la.stream);
   return TSG_OK;
 }
 
