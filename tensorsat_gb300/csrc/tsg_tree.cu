@@ -676,10 +676,13 @@ struct StreamItem {
 };
 
 // Loads the V values of the other operand from its staged chunk: `p` points at the
-// thread's first position, the tile's positions sit at the operand's tab offsets.
-template <typename T, int V>
-__device__ __forceinline__ void smem_load(const TileOperand& op, const T* p, T (&out)[V]) {
-  if (op.mode == kModeContig) {
+// thread's first position, the tile's positions sit at the operand's tab offsets. The
+// load mode is a template parameter (the streaming consumer is specialised on it).
+constexpr int kModeGlobal = -1;  // the streaming kernel's other operand is not staged
+
+template <int kMode, typename T, int V>
+__device__ __forceinline__ void stage_load(const TileOperand& op, const T* p, T (&out)[V]) {
+  if constexpr (kMode == kModeContig) {
     if constexpr (sizeof(T) == 4) {
       const uint4 x = *reinterpret_cast<const uint4*>(p);
       out[0] = x.x;
@@ -694,11 +697,11 @@ __device__ __forceinline__ void smem_load(const TileOperand& op, const T* p, T (
       out[2 % V] = x1.x;
       out[3 % V] = x1.y;
     }
-  } else if (op.mode == kModeBcast) {
+  } else if constexpr (kMode == kModeBcast) {
     const T x = p[0];
 #pragma unroll
     for (int j = 0; j < V; ++j) out[j] = x;
-  } else if (op.mode == kModePair) {
+  } else if constexpr (kMode == kModePair) {
     const T x0 = p[0], x1 = p[op.tab[3]];
 #pragma unroll
     for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
@@ -812,74 +815,88 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
     return;
   }
 
-  // consumer warps: one residue plane of one tile per item
-  const int leaves = a.op[0].leaf + a.op[1].leaf;
+  // consumer warps: one residue plane of one tile per item; the loop is specialised on how
+  // the other operand is read (its staged load mode, or global loads when not staged)
   const uint32_t f_lo = threadIdx.x * V;
   const uint64_t s_lo = scatter32(S.f_lo, f_lo);
   const uint64_t o_lo = scatter32(a.of_lo, f_lo);
-  uint64_t i = 0;
-  for (uint64_t w = blockIdx.x; w < items; w += gridDim.x, ++i) {
-    const int s = (int)(i % nst);
-    if (__shfl_sync(0xffffffffu, (int)bail, 0)) return;
-    if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
-      if (lane == 0) {
-        atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
-        bail = 1;
+  auto consume = [&](auto mode_c) {
+    constexpr int kSMode = decltype(mode_c)::value;  // kModeGlobal: not staged
+    // staged operands are intermediates, so only a global operand can be a leaf
+    const int leaves = kSMode == kModeGlobal ? S.leaf : 0;
+    uint64_t i = 0;
+    for (uint64_t w = blockIdx.x; w < items; w += gridDim.x, ++i) {
+      const int s = (int)(i % nst);
+      if (__shfl_sync(0xffffffffu, (int)bail, 0)) return;
+      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
+        if (lane == 0) {
+          atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
+          bail = 1;
+        }
+        return;
       }
-      return;
-    }
-    const uint64_t so = head[s].so;
-    const uint64_t oo = head[s].oo + o_lo;
-    const PlaneConst pc = plane_const(ring, head[s].p);
-    const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
-    T bv[KU][V];
-#pragma unroll
-    for (int ku = 0; ku < KU; ++ku) {
-      const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
-      if constexpr (sizeof(T) == 4) {
-        const uint4 x = *reinterpret_cast<const uint4*>(src);
-        bv[ku][0] = x.x;
-        bv[ku][1] = x.y;
-        bv[ku][2] = x.z;
-        bv[ku][3] = x.w;
-      } else {
-        const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
-        const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
-        bv[ku][0] = x0.x;
-        bv[ku][1] = x0.y;
-        bv[ku][2] = x1.x;
-        bv[ku][3] = x1.y;
-      }
-    }
-    const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
-#pragma unroll
-    for (int e = 0; e < NE; ++e) {
-      uint64_t acc[V] = {0, 0, 0, 0};
+      const uint64_t so = head[s].so;
+      const uint64_t oo = head[s].oo + o_lo;
+      const PlaneConst pc = plane_const(ring, head[s].p);
+      const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
+      T bv[KU][V];
 #pragma unroll
       for (int ku = 0; ku < KU; ++ku) {
-        T sv[V];
-        if (s_staged) smem_load<T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
-        else tile_load<T, T, V>(S, so + s_lo + S.e_off[e] + S.k_off[ku], sv);
-#pragma unroll
-        for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
+        const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
+        if constexpr (sizeof(T) == 4) {
+          const uint4 x = *reinterpret_cast<const uint4*>(src);
+          bv[ku][0] = x.x;
+          bv[ku][1] = x.y;
+          bv[ku][2] = x.z;
+          bv[ku][3] = x.w;
+        } else {
+          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
+          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
+          bv[ku][0] = x0.x;
+          bv[ku][1] = x0.y;
+          bv[ku][2] = x1.x;
+          bv[ku][3] = x1.y;
+        }
       }
-      const uint64_t oe = oo + a.o_e[e];
-      if constexpr (kRing == TSG_RING_U64) {
-        uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
-        reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[0], acc[1]);
-        reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[2], acc[3]);
-      } else {
-        uint32_t r[V];
+      const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
 #pragma unroll
-        for (int j = 0; j < V; ++j) r[j] = mont_finish_c(acc[j], leaves, pc);
-        *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
-            make_uint4(r[0], r[1], r[2], r[3]);
+      for (int e = 0; e < NE; ++e) {
+        uint64_t acc[V] = {0, 0, 0, 0};
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku) {
+          T sv[V];
+          if constexpr (kSMode == kModeGlobal)
+            tile_load<T, T, V>(S, so + s_lo + S.e_off[e] + S.k_off[ku], sv);
+          else
+            stage_load<kSMode, T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
+#pragma unroll
+          for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
+        }
+        const uint64_t oe = oo + a.o_e[e];
+        if constexpr (kRing == TSG_RING_U64) {
+          uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
+          reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[0], acc[1]);
+          reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[2], acc[3]);
+        } else {
+          uint32_t r[V];
+#pragma unroll
+          for (int j = 0; j < V; ++j)
+            r[j] = kSMode == kModeGlobal ? mont_finish_c(acc[j], leaves, pc)
+                                         : mont_redc(acc[j], pc.p, pc.pinv);
+          *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
+              make_uint4(r[0], r[1], r[2], r[3]);
+        }
       }
+      // release the stage: every lane of the warp is done reading it
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
     }
-    // release the stage: every lane of the warp is done reading it
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
-  }
+  };
+  if (!s_staged) consume(std::integral_constant<int, kModeGlobal>{});
+  else if (S.mode == kModeContig) consume(std::integral_constant<int, kModeContig>{});
+  else if (S.mode == kModeBcast) consume(std::integral_constant<int, kModeBcast>{});
+  else if (S.mode == kModePair) consume(std::integral_constant<int, kModePair>{});
+  else consume(std::integral_constant<int, kModeGather>{});
 }
 
 // Combines the root tensors of `cnt` slices (layout [plane][cnt][E]) into result[E]
