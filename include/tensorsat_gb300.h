@@ -167,6 +167,25 @@ TSG_API tsg_status tsg_plan_run(const tsg_plan* plan, int32_t ring, int32_t num_
                         void* workspace_dev, int64_t workspace_bytes, void* result_dev,
                         int32_t accumulate, void* stream);
 
+/* Batched runs of many instances (for example a batch of random CNF instances of uneven
+ * sizes, each with its own plan). Instance i contracts all 2^num_sliced slices of plans[i]
+ * over its leaf pool leaf_pools[i] in groups of group_sizes[i] and overwrites results[i]
+ * (layout as in tsg_plan_run). The instances run one after another on `stream` and share
+ * one workspace of at least tsg_batch_workspace_bytes. Every instance's arguments and
+ * every launch are checked on the host before the first launch, so a bad instance fails
+ * the call with nothing launched. The call neither allocates nor synchronises: it can be
+ * captured into a CUDA graph and replayed (make one uncaptured call first, which sets
+ * up per-kernel attributes). No counterpart in the reference, which contracts one
+ * instance per call (tensorsat/contractions/abc.py:92, Contraction.contract). */
+TSG_API tsg_status tsg_batch_workspace_bytes(int32_t num_instances, const tsg_plan* const* plans,
+                                     int32_t ring, int32_t num_primes,
+                                     const int64_t* group_sizes, int64_t* bytes_out);
+TSG_API tsg_status tsg_batch_run(int32_t num_instances, const tsg_plan* const* plans,
+                         int32_t ring, int32_t num_primes, const uint32_t* primes,
+                         const uint8_t* const* leaf_pools, const int64_t* group_sizes,
+                         void* workspace_dev, int64_t workspace_bytes,
+                         void* const* results_dev, void* stream);
+
 /* tsg_plan_run that also measures: a CUDA event is recorded on `stream` before the first
  * launch and after every launch, and on return (the call waits for the run to finish)
  * step_ms[s] holds the device time of tree step s summed over the slice groups of the

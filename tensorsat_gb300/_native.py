@@ -44,6 +44,8 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_launch_count",
     "tsg_plan_run",
     "tsg_plan_run_timed",
+    "tsg_batch_workspace_bytes",
+    "tsg_batch_run",
     "tsg_plan_validate",
     "tsg_take_device_error",
     "tsg_static_scratch_bytes",
@@ -111,6 +113,13 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_run_timed.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_void_p,
                                        c_int64, c_int64, c_int64, c_void_p, c_int64, c_void_p,
                                        c_int32, c_void_p, POINTER(ctypes.c_float)]
+    lib.tsg_batch_workspace_bytes.restype = c_int32
+    lib.tsg_batch_workspace_bytes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32, _i64p,
+                                              _i64p]
+    lib.tsg_batch_run.restype = c_int32
+    lib.tsg_batch_run.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32, POINTER(c_uint32),
+                                  POINTER(c_void_p), _i64p, c_void_p, c_int64, POINTER(c_void_p),
+                                  c_void_p]
     lib.tsg_take_device_error.restype = c_int32
     lib.tsg_take_device_error.argtypes = [c_void_p]
     lib.tsg_static_scratch_bytes.restype = c_int64

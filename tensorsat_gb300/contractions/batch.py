@@ -1,0 +1,222 @@
+"""Batched contraction of many networks in one native call (``tsg_batch_run``).
+
+The reference contracts one diagram per ``Contraction.contract`` call
+(``tensorsat/contractions/abc.py:92``). A batch of networks of uneven sizes (for example
+random CNF instances with different variable and clause counts) is planned network by
+network (one :class:`~tensorsat_gb300.contractions.gpu.GpuContraction` each), then run
+by one C call. That call checks every instance and every launch on the host, then issues
+all kernels of all instances on one stream with one shared workspace. It neither
+allocates nor synchronises, so :meth:`BatchContraction.capture` records it into a CUDA
+graph, and each replay reruns the whole batch with a single launch from the host.
+
+Results are the same as running each network through its own
+:class:`~tensorsat_gb300.contractions.gpu.GpuContraction`: SAT bits in the OR-AND
+semiring, exact model counts modulo 31-bit primes recombined by CRT.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from collections.abc import Sequence
+from typing import Any
+
+import numpy as np
+import torch
+
+from .. import _device, _native
+from ..diagrams import Diagram
+from ..lang.cuda_rel import CudaRel, leaf_array
+from .gpu import PRIMES_31, GpuContraction, count_bound_bits, crt
+
+__all__ = ["BatchContraction", "BatchGraph"]
+
+
+def _ptr_array(values: Sequence[int]) -> Any:
+    return (ctypes.c_void_p * max(1, len(values)))(*values)
+
+
+class BatchGraph:
+    """A captured batch run: :meth:`replay` reruns every instance of the batch into the
+    same result buffers with one graph launch."""
+
+    def __init__(self, graph: torch.cuda.CUDAGraph, results: list[torch.Tensor],
+                 keep: list[Any]) -> None:
+        self._graph = graph
+        self.results = results
+        self._keep = keep  # workspace, pools and argument arrays the graph points to
+
+    def replay(self) -> list[torch.Tensor]:
+        self._graph.replay()
+        return self.results
+
+
+class BatchContraction:
+    """Plans a batch of flat diagrams (each closed or with open outputs) and contracts them
+    together: :meth:`contract` gives one result box per diagram, :meth:`count` one exact
+    model count per diagram."""
+
+    def __init__(self, box_class: type[CudaRel], diagrams: Sequence[Diagram], *,
+                 target_bits: int | None = 26, trials: int = 2, seed: int = 0) -> None:
+        if not diagrams:
+            raise ValueError("A batch needs at least one diagram.")
+        self._diagrams = list(diagrams)
+        self._contractions = [GpuContraction(box_class, d.wiring, target_bits=target_bits,
+                                             trials=trials, seed=seed)
+                              for d in self._diagrams]
+        for c, d in zip(self._contractions, self._diagrams):
+            c.validate(d)
+        self._pools: list[torch.Tensor] | None = None
+
+    @property
+    def contractions(self) -> list[GpuContraction]:
+        return self._contractions
+
+    def __len__(self) -> int:
+        return len(self._contractions)
+
+    # -- native arguments -------------------------------------------------------------
+
+    def pools(self) -> list[torch.Tensor]:
+        """Device leaf pools of every instance (uploaded once)."""
+        if self._pools is None:
+            self._pools = [c.leaf_pool(d, cache=False)
+                           for c, d in zip(self._contractions, self._diagrams)]
+        return self._pools
+
+    def groups(self, ring: int, planes: int, budget_bytes: int | None = None) -> list[int]:
+        """Slice group per instance: the largest power of two whose workspace fits the
+        budget (default: 40% of free device memory); the batch shares one workspace, so
+        the budget bounds every instance."""
+        if budget_bytes is None:
+            free, _ = torch.cuda.mem_get_info()
+            budget_bytes = int(free * 0.4)
+        return [c.choose_group(ring, planes, budget_bytes) for c in self._contractions]
+
+    def workspace_bytes(self, ring: int, planes: int, groups: Sequence[int]) -> int:
+        lib = _native.lib()
+        handles = _ptr_array([c.native_plan().handle.value for c in self._contractions])
+        out = ctypes.c_int64()
+        _native.check(lib.tsg_batch_workspace_bytes(
+            len(self), handles, ring, planes, _native.i64_array(list(groups)), ctypes.byref(out)))
+        return int(out.value)
+
+    def _results(self, ring: int, planes: int) -> list[torch.Tensor]:
+        dev = _device.require_cuda()
+        res = []
+        for c in self._contractions:
+            entries = 1 << len(c._leaves.out_unique)
+            if ring == _native.TSG_RING_OR_AND:
+                res.append(torch.zeros(entries, dtype=torch.uint8, device=dev))
+            elif ring == _native.TSG_RING_U64:
+                res.append(torch.zeros(entries, dtype=torch.int64, device=dev))
+            else:
+                res.append(torch.zeros(planes * entries, dtype=torch.int32, device=dev))
+        return res
+
+    def _call(self, ring: int, primes: Sequence[int], groups: Sequence[int],
+              workspace: torch.Tensor, results: Sequence[torch.Tensor], stream: int) -> list:
+        lib = _native.lib()
+        pools = self.pools()
+        args = [
+            _ptr_array([c.native_plan().handle.value for c in self._contractions]),
+            (_native.c_uint32 * max(1, len(primes)))(*primes),
+            _ptr_array([p.data_ptr() for p in pools]),
+            _native.i64_array(list(groups)),
+            _ptr_array([r.data_ptr() for r in results]),
+        ]
+        st = lib.tsg_batch_run(len(self), args[0], ring, len(primes), args[1], args[2],
+                               args[3], workspace.data_ptr(), workspace.numel(), args[4],
+                               stream)
+        _native.check(st)
+        return args
+
+    def run(self, ring: int, primes: Sequence[int] = (),
+            groups: Sequence[int] | None = None) -> list[torch.Tensor]:
+        """One ``tsg_batch_run`` call over every instance; returns each instance's device
+        result (layout as :meth:`GpuContraction.run`)."""
+        dev = _device.require_cuda()
+        planes = len(primes) if ring == _native.TSG_RING_MODP else 1
+        if groups is None:
+            groups = self.groups(ring, planes)
+        ws = torch.empty(max(1, self.workspace_bytes(ring, planes, groups)), dtype=torch.uint8,
+                         device=dev)
+        results = self._results(ring, planes)
+        self._call(ring, primes, groups, ws, results, _device.stream_handle())
+        GpuContraction.check_device()
+        return results
+
+    def capture(self, ring: int, primes: Sequence[int] = (),
+                groups: Sequence[int] | None = None) -> BatchGraph:
+        """Records one batch run into a CUDA graph (after one uncaptured run, which sets up
+        the kernels' attributes); :meth:`BatchGraph.replay` reruns it."""
+        dev = _device.require_cuda()
+        planes = len(primes) if ring == _native.TSG_RING_MODP else 1
+        if groups is None:
+            groups = self.groups(ring, planes)
+        ws = torch.empty(max(1, self.workspace_bytes(ring, planes, groups)), dtype=torch.uint8,
+                         device=dev)
+        results = self._results(ring, planes)
+        self._call(ring, primes, groups, ws, results, _device.stream_handle())
+        torch.cuda.synchronize(dev)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            args = self._call(ring, primes, groups, ws, results,
+                              torch.cuda.current_stream(dev).cuda_stream)
+        return BatchGraph(graph, results, [ws, self.pools(), args, list(groups), list(primes)])
+
+    # -- answers ----------------------------------------------------------------------
+
+    def contract(self, groups: Sequence[int] | None = None) -> list[CudaRel]:
+        """OR-AND contraction of every diagram: one result box per diagram (a scalar box
+        for a SAT network: ``bool(box)`` is its SAT bit)."""
+        res = self.run(_native.TSG_RING_OR_AND, groups=groups)
+        return [c._box_from_root(r) for c, r in zip(self._contractions, res)]
+
+    def count_bounds(self) -> list[float]:
+        """log2 upper bound on each diagram's model count (free variables of its oriented
+        gate network)."""
+        bounds = []
+        for c, d in zip(self._contractions, self._diagrams):
+            arrays = []
+            for blk in d.blocks:
+                try:
+                    arrays.append(leaf_array(blk))
+                except TypeError:
+                    arrays.append(np.zeros((), dtype=np.uint8))
+            bounds.append(count_bound_bits(c._wiring, arrays))
+        return bounds
+
+    def primes_needed(self) -> int:
+        bound = max(self.count_bounds())
+        n = 1
+        while sum(math.log2(p) for p in PRIMES_31[:n]) <= bound:
+            n += 1
+        return n
+
+    def count(self, num_primes: int | None = None,
+              groups: Sequence[int] | None = None) -> list[Any]:
+        """Exact model count of every diagram (``int`` for closed networks, a numpy object
+        array over the out wires otherwise), from one batched run modulo ``num_primes``
+        31-bit primes (default: as many as the largest count bound of the batch needs, at
+        most 4 per run)."""
+        need = self.primes_needed()
+        if num_primes is None:
+            num_primes = need
+        if num_primes < need:
+            raise OverflowError(f"the batch's count bounds need {need} 31-bit primes")
+        if num_primes > _native.TSG_MAX_PRIMES:
+            raise OverflowError(
+                f"the batch needs {num_primes} primes; one batched run carries at most "
+                f"{_native.TSG_MAX_PRIMES} (count such networks with GpuContraction.count)")
+        primes = PRIMES_31[:num_primes]
+        res = self.run(_native.TSG_RING_MODP, primes, groups=groups)
+        out = []
+        for c, r in zip(self._contractions, res):
+            planes = r.cpu().numpy().view(np.uint32).reshape(num_primes, -1)
+            counts = crt([planes[p] for p in range(num_primes)], primes)
+            out.append(c._counts_from_root(counts))
+        return out
+
+    def __repr__(self) -> str:
+        return f"<BatchContraction of {len(self)} networks>"

@@ -486,6 +486,10 @@ class GpuContraction(Contraction):
         res = self.run(diagram, _native.TSG_RING_OR_AND, group=group, slice_range=slice_range,
                        cache_leaves=cache_leaves)
         self.check_device()
+        return self._box_from_root(res)
+
+    def _box_from_root(self, res: torch.Tensor) -> CudaRel:
+        """Result box from the OR-AND root entries (over the distinct out wires)."""
         lw = self._leaves
         k = len(lw.out_unique)
         box = CudaRel._new(res.reshape((2,) * k))
@@ -546,6 +550,11 @@ class GpuContraction(Contraction):
             counts = crt(residues, primes)
         else:
             raise ValueError(f"unknown count ring {ring!r}")
+        return self._counts_from_root(counts)
+
+    def _counts_from_root(self, counts: np.ndarray) -> Any:
+        """Counts (``int`` for a closed network, an object array over the out wires
+        otherwise) from the exact root entries of a run (discarded wires excluded)."""
         lw = self._leaves
         counts = counts * lw.discard_factor
         k = len(lw.out_unique)

@@ -2173,6 +2173,50 @@ tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_pri
                   nullptr, 0, nullptr, 0, nullptr, /*dry=*/true);
 }
 
+tsg_status tsg_batch_workspace_bytes(int32_t num_instances, const tsg_plan* const* plans,
+                                     int32_t ring, int32_t num_primes,
+                                     const int64_t* group_sizes, int64_t* bytes_out) {
+  if (num_instances < 0 || (num_instances > 0 && (!plans || !group_sizes)) || !bytes_out)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_workspace_bytes: null pointer or negative count");
+  int64_t most = 0;
+  for (int32_t i = 0; i < num_instances; ++i) {
+    if (!plans[i]) return fail(TSG_ERR_INVALID_ARGUMENT, "batch_workspace_bytes: null plan");
+    int64_t b = 0;
+    TSG_TRY(tsg_plan_workspace_bytes(plans[i], ring, num_primes, group_sizes[i], &b));
+    most = std::max(most, b);
+  }
+  *bytes_out = most;
+  return TSG_OK;
+}
+
+tsg_status tsg_batch_run(int32_t num_instances, const tsg_plan* const* plans, int32_t ring,
+                         int32_t num_primes, const uint32_t* primes,
+                         const uint8_t* const* leaf_pools, const int64_t* group_sizes,
+                         void* workspace_dev, int64_t workspace_bytes, void* const* results_dev,
+                         void* stream) {
+  if (num_instances < 0 ||
+      (num_instances > 0 && (!plans || !leaf_pools || !group_sizes || !results_dev)))
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_run: null pointer or negative count");
+  // every instance is checked (arguments, bounds of every launch) before anything runs
+  for (int32_t i = 0; i < num_instances; ++i) {
+    if (!plans[i] || !leaf_pools[i] || !results_dev[i])
+      return fail(TSG_ERR_INVALID_ARGUMENT,
+                  "batch_run: null plan, pool or result of instance " + std::to_string(i));
+    const int64_t ns = int64_t(1) << plans[i]->num_sliced;
+    tsg_status st = run_impl(plans[i], ring, num_primes, primes, nullptr, 0, ns,
+                             group_sizes[i], nullptr, 0, nullptr, 0, nullptr, /*dry=*/true);
+    if (st != TSG_OK)
+      return fail(st, "batch_run: instance " + std::to_string(i) + ": " + tsg_last_error());
+  }
+  for (int32_t i = 0; i < num_instances; ++i) {
+    const int64_t ns = int64_t(1) << plans[i]->num_sliced;
+    TSG_TRY(run_impl(plans[i], ring, num_primes, primes, leaf_pools[i], 0, ns, group_sizes[i],
+                     workspace_dev, workspace_bytes, results_dev[i], 0, (cudaStream_t)stream,
+                     /*dry=*/false));
+  }
+  return TSG_OK;
+}
+
 int64_t tsg_static_scratch_bytes(void) { return kStaticScratchBytes; }
 
 tsg_status tsg_take_device_error(void* stream) {

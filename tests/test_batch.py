@@ -1,0 +1,110 @@
+"""Batched runs of many networks (tsg_batch_run, BatchContraction).
+
+CPU tests call the C ABI without a GPU: the shared workspace is the largest per-instance
+workspace, and a batch with one bad instance is rejected by the host checks before
+anything is launched. GPU tests compare a ragged batch of random 3-SAT instances (uneven
+variable and clause counts, several of them sliced) with brute force and with per-instance
+contractions, and replays of a captured CUDA graph with the uncaptured run. Counts and SAT
+bits are integers: the tolerance is equality.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import finrel_oracle as orc
+from tensorsat_gb300 import _native
+from tensorsat_gb300.contractions.batch import BatchContraction
+from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+from tensorsat_gb300.lang.cuda_rel import CudaRel
+from tensorsat_gb300.lib.sat import CNFInstance
+
+
+def ragged_instances(count: int, n_lo: int, n_hi: int, seed: int = 0) -> list[CNFInstance]:
+    """Random 3-SAT instances with n uniform in [n_lo, n_hi] and clause ratio uniform in
+    [3.5, 5.0], one generator per instance (seeded by its index)."""
+    out = []
+    for i in range(count):
+        g = np.random.default_rng(seed * 100_003 + i)
+        n = int(g.integers(n_lo, n_hi + 1))
+        m = round(float(g.uniform(3.5, 5.0)) * n)
+        out.append(CNFInstance.random(3, n, m, rng=g))
+    return out
+
+
+def _plans(instances, target_bits):
+    return [GpuContraction(CudaRel, cnf.clause_diagram().wiring, target_bits=target_bits,
+                           trials=1).native_plan() for cnf in instances]
+
+
+def test_batch_workspace_is_the_largest_instance_workspace():
+    plans = _plans(ragged_instances(6, 10, 20), target_bits=8)
+    lib = _native.lib()
+    groups = [1, 2, 4, 1, 2, 1]
+    out = ctypes.c_int64()
+    handles = (ctypes.c_void_p * len(plans))(*[p.handle.value for p in plans])
+    for ring, planes in [(_native.TSG_RING_OR_AND, 1), (_native.TSG_RING_MODP, 3),
+                         (_native.TSG_RING_U64, 1)]:
+        _native.check(lib.tsg_batch_workspace_bytes(len(plans), handles, ring, planes,
+                                                    _native.i64_array(groups), ctypes.byref(out)))
+        assert out.value == max(p.workspace_bytes(ring, planes, g) for p, g in zip(plans, groups))
+
+
+def test_batch_rejects_a_bad_instance_before_launching():
+    """Instance 2 has a group size that is not a power of two: the call fails in the host
+    checks (the pointers are never dereferenced, so placeholders suffice)."""
+    plans = _plans(ragged_instances(4, 10, 16, seed=1), target_bits=6)
+    lib = _native.lib()
+    n = len(plans)
+    handles = (ctypes.c_void_p * n)(*[p.handle.value for p in plans])
+    fake = (ctypes.c_void_p * n)(*([256] * n))
+    groups = _native.i64_array([1, 1, 3, 1])
+    st = lib.tsg_batch_run(n, handles, _native.TSG_RING_OR_AND, 0, None, fake, groups, None, 0,
+                           fake, None)
+    assert st == _native.TSG_ERR_INVALID_ARGUMENT
+    assert "instance 2" in lib.tsg_last_error().decode()
+    assert lib.tsg_batch_run(-1, None, 0, 0, None, None, None, None, 0, None, None) \
+        == _native.TSG_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.gpu
+def test_ragged_batch_counts_and_sat_bits_match_brute_force(cuda):
+    instances = ragged_instances(12, 12, 22, seed=2)
+    diagrams = [cnf.clause_diagram() for cnf in instances]
+    batch = BatchContraction(CudaRel, diagrams, target_bits=9, trials=1)
+    assert any(c.num_slices > 1 for c in batch.contractions)
+    expected = [orc.brute_force_count(cnf.num_vars, cnf.clauses) for cnf in instances]
+    assert batch.count() == expected
+    assert batch.count(num_primes=3) == expected
+    bits = [bool(box) for box in batch.contract()]
+    assert bits == [e > 0 for e in expected]
+    # the same as contracting each network on its own
+    for c, d, e in zip(batch.contractions, diagrams, expected):
+        assert c.count(d, ring="modp", num_primes=2) == e
+
+
+@pytest.mark.gpu
+def test_batch_graph_replay_matches_uncaptured_run(cuda):
+    instances = ragged_instances(8, 14, 24, seed=3)
+    batch = BatchContraction(CudaRel, [cnf.clause_diagram() for cnf in instances],
+                             target_bits=10, trials=1)
+    primes = PRIMES_31[:3]
+    direct = [r.clone() for r in batch.run(_native.TSG_RING_MODP, primes)]
+    sat_direct = [r.clone() for r in batch.run(_native.TSG_RING_OR_AND)]
+    g = batch.capture(_native.TSG_RING_MODP, primes)
+    gs = batch.capture(_native.TSG_RING_OR_AND)
+    for _ in range(2):
+        for r in g.results + gs.results:
+            r.fill_(7)  # replays must rewrite every result
+        g.replay()
+        gs.replay()
+        torch.cuda.synchronize()
+        for a, b in zip(g.results, direct):
+            assert torch.equal(a, b)
+        for a, b in zip(gs.results, sat_direct):
+            assert torch.equal(a, b)
+    GpuContraction.check_device()
