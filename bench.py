@@ -53,6 +53,11 @@ def parse_args():
     p.add_argument("--trials", type=int, default=8)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", default="n60", choices=["n60", "ragged"],
+                   help="n60: the single-instance headline workload; ragged: a batch of "
+                        "random instances of uneven sizes (batched runs, CUDA graphs)")
+    p.add_argument("--instances", type=int, default=512, help="ragged: batch size")
+    p.add_argument("--n-range", type=int, nargs=2, default=[30, 40], help="ragged: n bounds")
     return p.parse_args()
 
 
@@ -392,10 +397,136 @@ def run_gb300(args) -> None:
         dist.destroy_process_group()
 
 
+# --------------------------------------------------------------------------------------
+# Ragged batch: many random instances of uneven sizes
+
+
+RAGGED_METRIC = "exact instances/s (SAT bit + model count), ragged batch of random 3-SAT"
+RAGGED_CHUNK = 64  # instances per captured graph
+
+
+def ragged_instances(count: int, n_lo: int, n_hi: int):
+    """n uniform in [n_lo, n_hi], clause ratio uniform in [3.5, 5.0], one generator per
+    instance seeded by its index."""
+    import numpy as np
+
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    out = []
+    for i in range(count):
+        g = np.random.default_rng(i)
+        n = int(g.integers(n_lo, n_hi + 1))
+        m = round(float(g.uniform(3.5, 5.0)) * n)
+        out.append(CNFInstance.random(3, n, m, rng=g))
+    return out
+
+
+def run_ragged(args) -> None:
+    import torch
+
+    from tensorsat_gb300 import _native
+    from tensorsat_gb300.contractions.batch import BatchContraction
+    from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    lo, hi = args.n_range
+    instances = ragged_instances(args.instances, lo, hi)
+    diagrams = [cnf.clause_diagram() for cnf in instances]
+    primes = PRIMES_31[:NUM_PRIMES]
+    chunks = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK], target_bits=TARGET_BITS,
+                               trials=1)
+              for i in range(0, len(diagrams), RAGGED_CHUNK)]
+    # one workspace for every graph (they replay in order on one stream); slice groups
+    # sized to a fixed budget
+    budget = 8 << 30
+    plans = []
+    for b in chunks:
+        for ring, pr in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ())):
+            groups = b.groups(ring, max(1, len(pr)), budget)
+            plans.append((b, ring, pr, groups, b.workspace_bytes(ring, max(1, len(pr)), groups)))
+    ws = torch.empty(max(p[4] for p in plans), dtype=torch.uint8, device=dev)
+    graphs = [b.capture(ring, pr, groups, workspace=ws) for b, ring, pr, groups, _ in plans]
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        for g in graphs:
+            g.replay()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(0) as clocks:
+        ev[0].record(stream)
+        for k in range(args.steps):
+            step()
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    value = len(instances) * args.steps / (sum(step_ms) / 1000.0)
+    GpuContraction.check_device()
+
+    # plain form: one instance per call through the public API (count + SAT bit)
+    sample = min(len(diagrams), 64)
+    plain = [GpuContraction(CudaRel, d.wiring, target_bits=TARGET_BITS, trials=1)
+             for d in diagrams[:sample]]
+    for c, d in zip(plain[:4], diagrams[:4]):
+        c.count(d, ring="modp", num_primes=NUM_PRIMES)
+        bool(c.contract(d))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c, d in zip(plain, diagrams[:sample]):
+        c.count(d, ring="modp", num_primes=NUM_PRIMES, cache_leaves=False)
+        bool(c.contract(d, cache_leaves=False))
+    torch.cuda.synchronize()
+    plain_value = sample / (time.perf_counter() - t0)
+
+    # end to end, batched: host diagrams in (leaf upload), counts and bits out
+    fresh = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK], target_bits=TARGET_BITS,
+                              trials=1)
+             for i in range(0, len(diagrams), RAGGED_CHUNK)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h2d = 0
+    for b in fresh:
+        b.count(num_primes=NUM_PRIMES)
+        [bool(x) for x in b.contract()]
+        h2d += sum(p.numel() for p in b.pools())
+    torch.cuda.synchronize()
+    e2e_value = len(diagrams) / (time.perf_counter() - t0)
+    launches = sum(g.launches for g in graphs)
+    line = {
+        "metric": RAGGED_METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 residues mod 3 primes + u8 OR-AND",
+        "data": "synthetic (seeded CNFInstance.random per instance, no dataset)",
+        "config": {"workload": f"ragged batch of {len(instances)} random 3-SAT instances, n "
+                               f"uniform in [{lo}, {hi}], clause ratio uniform in [3.5, 5.0], "
+                               f"seeded per instance",
+                   "instances": len(instances), "n_range": [lo, hi],
+                   "graphs": len(graphs), "instances_per_graph": RAGGED_CHUNK,
+                   "l2": "not flushed: small instances are L2-resident by design"},
+        "plain": {"value": plain_value, "unit": UNIT, "sample": sample,
+                  "form": "GpuContraction.count + contract per instance"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": len(instances) * (4 * NUM_PRIMES + 1)},
+        "gpu_launches": launches * args.steps,
+        "clocks": clocks.summary(),
+        "step_ms": [round(x, 3) for x in step_ms],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ragged":
+        run_ragged(args)
     else:
         run_gb300(args)
 

@@ -41,9 +41,11 @@ class BatchGraph:
     same result buffers with one graph launch."""
 
     def __init__(self, graph: torch.cuda.CUDAGraph, results: list[torch.Tensor],
-                 keep: list[Any]) -> None:
+                 groups: list[int], launches: int, keep: list[Any]) -> None:
         self._graph = graph
         self.results = results
+        self.groups = groups      # slice group of each instance
+        self.launches = launches  # kernel launches recorded in the graph
         self._keep = keep  # workspace, pools and argument arrays the graph points to
 
     def replay(self) -> list[torch.Tensor]:
@@ -131,31 +133,39 @@ class BatchContraction:
         _native.check(st)
         return args
 
-    def run(self, ring: int, primes: Sequence[int] = (),
-            groups: Sequence[int] | None = None) -> list[torch.Tensor]:
+    def _workspace(self, ring: int, planes: int, groups: Sequence[int],
+                   workspace: torch.Tensor | None) -> torch.Tensor:
+        need = self.workspace_bytes(ring, planes, groups)
+        if workspace is not None:
+            if workspace.numel() < need:
+                raise ValueError(f"the batch needs a workspace of {need} bytes")
+            return workspace
+        return torch.empty(max(1, need), dtype=torch.uint8, device=_device.require_cuda())
+
+    def run(self, ring: int, primes: Sequence[int] = (), groups: Sequence[int] | None = None,
+            workspace: torch.Tensor | None = None) -> list[torch.Tensor]:
         """One ``tsg_batch_run`` call over every instance; returns each instance's device
-        result (layout as :meth:`GpuContraction.run`)."""
-        dev = _device.require_cuda()
+        result (layout as :meth:`GpuContraction.run`). ``workspace`` (uint8, at least
+        :meth:`workspace_bytes`) may be shared with other batches run on the same stream."""
         planes = len(primes) if ring == _native.TSG_RING_MODP else 1
         if groups is None:
             groups = self.groups(ring, planes)
-        ws = torch.empty(max(1, self.workspace_bytes(ring, planes, groups)), dtype=torch.uint8,
-                         device=dev)
+        ws = self._workspace(ring, planes, groups, workspace)
         results = self._results(ring, planes)
         self._call(ring, primes, groups, ws, results, _device.stream_handle())
         GpuContraction.check_device()
         return results
 
-    def capture(self, ring: int, primes: Sequence[int] = (),
-                groups: Sequence[int] | None = None) -> BatchGraph:
+    def capture(self, ring: int, primes: Sequence[int] = (), groups: Sequence[int] | None = None,
+                workspace: torch.Tensor | None = None) -> BatchGraph:
         """Records one batch run into a CUDA graph (after one uncaptured run, which sets up
-        the kernels' attributes); :meth:`BatchGraph.replay` reruns it."""
+        the kernels' attributes); :meth:`BatchGraph.replay` reruns it. Graphs replayed on
+        one stream may share one ``workspace``."""
         dev = _device.require_cuda()
         planes = len(primes) if ring == _native.TSG_RING_MODP else 1
         if groups is None:
             groups = self.groups(ring, planes)
-        ws = torch.empty(max(1, self.workspace_bytes(ring, planes, groups)), dtype=torch.uint8,
-                         device=dev)
+        ws = self._workspace(ring, planes, groups, workspace)
         results = self._results(ring, planes)
         self._call(ring, primes, groups, ws, results, _device.stream_handle())
         torch.cuda.synchronize(dev)
@@ -163,7 +173,10 @@ class BatchContraction:
         with torch.cuda.graph(graph):
             args = self._call(ring, primes, groups, ws, results,
                               torch.cuda.current_stream(dev).cuda_stream)
-        return BatchGraph(graph, results, [ws, self.pools(), args, list(groups), list(primes)])
+        launches = sum(c.native_plan().launch_count(0, c.num_slices, g)
+                       for c, g in zip(self._contractions, groups))
+        return BatchGraph(graph, results, list(groups), launches,
+                          [ws, self.pools(), args, list(primes)])
 
     # -- answers ----------------------------------------------------------------------
 
