@@ -716,7 +716,7 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
     tree_step_stream_kernel(TileArgs a, RingArgs ring, StreamArgs sa) {
   using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
   constexpr int V = 4;
-  constexpr int KU = NK;  // NK in {1, 2}
+  constexpr int KU = NK;  // NK in {1, 2, 4}: 2^K summed combinations
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) uint64_t full[kStreamMaxStages], empty[kStreamMaxStages];
   __shared__ StreamItem head[kStreamMaxStages];
@@ -861,7 +861,8 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
       const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
 #pragma unroll
       for (int e = 0; e < NE; ++e) {
-        uint64_t acc[V] = {0, 0, 0, 0};
+        uint64_t acc[V] = {0, 0, 0, 0};  // U64: the sum; MODP: the current pair of products
+        uint32_t done[V] = {0, 0, 0, 0};  // MODP, 4 summed combinations: first pair, reduced
 #pragma unroll
         for (int ku = 0; ku < KU; ++ku) {
           T sv[V];
@@ -871,6 +872,17 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
             stage_load<kSMode, T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
 #pragma unroll
           for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
+          if constexpr (kRing == TSG_RING_MODP && KU > 2) {
+            // two Montgomery products stay below p 2^32: reduce each pair (with a leaf
+            // operand the four products are small and are reduced once at the end)
+            if (ku == 1 && leaves == 0) {
+#pragma unroll
+              for (int j = 0; j < V; ++j) {
+                done[j] = mont_redc(acc[j], pc.p, pc.pinv);
+                acc[j] = 0;
+              }
+            }
+          }
         }
         const uint64_t oe = oo + a.o_e[e];
         if constexpr (kRing == TSG_RING_U64) {
@@ -880,9 +892,11 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
         } else {
           uint32_t r[V];
 #pragma unroll
-          for (int j = 0; j < V; ++j)
+          for (int j = 0; j < V; ++j) {
             r[j] = kSMode == kModeGlobal ? mont_finish_c(acc[j], leaves, pc)
                                          : mont_redc(acc[j], pc.p, pc.pinv);
+            if constexpr (KU > 2) r[j] = add_mod(done[j], r[j], pc.p);
+          }
           *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
               make_uint4(r[0], r[1], r[2], r[3]);
         }
@@ -1604,7 +1618,7 @@ uint32_t stream_span(const LaunchArgs& la, int np, uint32_t esize, uint64_t exte
   const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
   const uint64_t end = s.base + scatter_max(s.g, gbits) + narrow_max(s.f_hi, nbits) + eo + ko + span;
   ok = ok && end <= extent;
-  ok = ok && 2 * stream_stage_bytes(sh.ne, sh.nk, la.stream.chunk_bytes, span, esize) <=
+  ok = ok && 2 * stream_stage_bytes(sh.ne, t.n_k, la.stream.chunk_bytes, span, esize) <=
                  kStreamBlockSmem;
   return ok ? span : 0;
 }
@@ -1615,7 +1629,8 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   const TileShape& sh = la.shape;
   // the streaming kernel stores 4 consecutive outputs as one vector: only when the 4
   // positions of a thread are 4 consecutive, aligned outputs
-  if (sh.v != 4 || (sh.nk != 1 && sh.nk != 2) || t.tile_bits != kStreamTileBits || !t.o_contig)
+  if (sh.v != 4 || (t.n_k != 1 && t.n_k != 2 && t.n_k != 4) || t.tile_bits != kStreamTileBits ||
+      !t.o_contig)
     return;
   if (sh.tiles * la.cnt < (uint64_t)device_sm_count() * 8) return;  // too small to stream
   int big = -1;
@@ -1641,7 +1656,7 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   la.stream.work = sh.tiles * la.cnt;
   la.stream.chunk_bytes = kStreamTile * esize;
   la.stream.s_span = stream_span(la, np, esize, extent[1 - big]);
-  const uint64_t stage = stream_stage_bytes(sh.ne, sh.nk, la.stream.chunk_bytes,
+  const uint64_t stage = stream_stage_bytes(sh.ne, t.n_k, la.stream.chunk_bytes,
                                             la.stream.s_span, esize);
   if (2 * stage > kStreamBlockSmem) return;  // fewer than two stages fit
   la.stream.stage_bytes = (uint32_t)stage;
@@ -1747,8 +1762,11 @@ tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_
 
 template <int kRing, int NE>
 tsg_status launch_stream_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  return la.shape.nk == 1 ? launch_stream_t<kRing, NE, 1>(la, ra, st)
-                          : launch_stream_t<kRing, NE, 2>(la, ra, st);
+  switch (la.t.n_k) {
+    case 1: return launch_stream_t<kRing, NE, 1>(la, ra, st);
+    case 2: return launch_stream_t<kRing, NE, 2>(la, ra, st);
+    default: return launch_stream_t<kRing, NE, 4>(la, ra, st);
+  }
 }
 
 template <int kRing>

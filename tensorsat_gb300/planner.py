@@ -290,6 +290,142 @@ def minfill_order(net: Network, rng: random.Random, prefix: Sequence[int] = ()) 
     return order
 
 
+def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
+                sliced: frozenset[int] = frozenset(), max_bits: int | None = None
+                ) -> ContractionTree:
+    """Subtree reconfiguration. For every internal node x, the subtree below x is cut at
+    up to ``subtree_size`` inputs (expanding its most expensive steps first) and replaced
+    by the cheapest binary contraction of those inputs, found by dynamic programming over
+    subsets. A partial contraction of a subset S keeps a wire when x keeps it or an input
+    outside S carries it. Cost is the tree's index-space cost per slice: the sum over
+    steps of 2^|wires of both operands, sliced wires excluded|. With ``max_bits`` no new
+    intermediate may exceed 2^max_bits entries per slice. The root and every leaf are
+    unchanged, so the answers are too."""
+    L = tree.num_leaves
+    wires: dict[int, frozenset[int]] = dict(enumerate(tree.node_wires))
+    children: dict[int, tuple[int, int]] = {L + s: ab for s, ab in enumerate(tree.steps)}
+    root = tree.root
+    next_id = L + len(tree.steps)
+
+    def step_cost(x: int) -> float:
+        a, b = children[x]
+        return 2.0 ** len((wires[a] | wires[b]) - sliced)
+
+    for _ in range(max(0, passes)):
+        improved = False
+        todo = [root]
+        seen = []
+        while todo:  # internal nodes, root first
+            x = todo.pop()
+            seen.append(x)
+            for c in children[x]:
+                if c in children:
+                    todo.append(c)
+        for x in seen:
+            if x not in children:
+                continue  # removed by an earlier replacement
+            frontier = list(children[x])
+            internal = [x]
+            while len(frontier) < subtree_size:
+                inner = [f for f in frontier if f in children]
+                if not inner:
+                    break
+                big = max(inner, key=step_cost)
+                frontier.remove(big)
+                internal.append(big)
+                frontier.extend(children[big])
+            n = len(frontier)
+            if n < 3:
+                continue
+            old = sum(step_cost(y) for y in internal)
+            # wires as bit sets over the wires present in the subtree
+            index: dict[int, int] = {}
+            for f in frontier:
+                for w in wires[f]:
+                    index.setdefault(w, len(index))
+            bits = [sum(1 << index[w] for w in wires[f]) for f in frontier]
+            keep_x = sum(1 << index[w] for w in wires[x] if w in index)
+            live = sum(1 << i for w, i in index.items() if w not in sliced)
+            full = (1 << n) - 1
+            union = [0] * (full + 1)
+            for m in range(1, full + 1):
+                low = m & -m
+                union[m] = union[m ^ low] | bits[low.bit_length() - 1]
+            kept = [union[m] & (keep_x | union[full ^ m]) for m in range(full + 1)]
+            inf = float("inf")
+            best = [0.0] * (full + 1)
+            split = [0] * (full + 1)
+            for m in range(1, full + 1):
+                if m & (m - 1) == 0:
+                    continue
+                if m != full and max_bits is not None and (kept[m] & live).bit_count() > max_bits:
+                    best[m] = inf  # intermediate above the cap
+                    continue
+                low = m & -m
+                rest = m ^ low
+                top = inf
+                sub = rest
+                while True:  # A = low | sub (contains the lowest input), B = the rest
+                    a = low | sub
+                    b = m ^ a
+                    if b:
+                        c = best[a] + best[b] + 2.0 ** ((kept[a] | kept[b]) & live).bit_count()
+                        if c < top:
+                            top, split[m] = c, a
+                    if sub == 0:
+                        break
+                    sub = (sub - 1) & rest
+                best[m] = top
+            if not best[full] < old * (1 - 1e-9):
+                continue
+            # rebuild the subtree below x from the splits; x keeps its id and wires
+            for y in internal:
+                if y != x:
+                    del children[y]
+                    del wires[y]
+
+            def build(m: int) -> int:
+                nonlocal next_id
+                if m & (m - 1) == 0:
+                    return frontier[m.bit_length() - 1]
+                a = split[m]
+                na, nb = build(a), build(m ^ a)
+                if m == full:
+                    y = x
+                else:
+                    y = next_id
+                    next_id += 1
+                    inv = {v: k for k, v in index.items()}
+                    km = kept[m]
+                    wires[y] = frozenset(inv[i] for i in range(km.bit_length()) if km >> i & 1)
+                children[y] = (na, nb)
+                return y
+
+            build(full)
+            improved = True
+        if not improved:
+            break
+    # re-linearise in post order: leaves keep their ids, steps are numbered L + s
+    steps: list[tuple[int, int]] = []
+    node_wires = [tree.node_wires[i] for i in range(L)]
+    new_id: dict[int, int] = {i: i for i in range(L)}
+    stack = [(root, False)]
+    while stack:
+        x, done = stack.pop()
+        if x in new_id:
+            continue
+        a, b = children[x]
+        if done:
+            steps.append((new_id[a], new_id[b]))
+            new_id[x] = L + len(steps) - 1
+            node_wires.append(wires[x])
+        else:
+            stack.append((x, True))
+            stack.append((b, False))
+            stack.append((a, False))
+    return ContractionTree(L, steps, node_wires, tree.out_wires)
+
+
 def slice_tree(tree: ContractionTree, target_bits: int, forbid: frozenset[int] = frozenset()
                ) -> frozenset[int]:
     """Greedy slicing: repeatedly slice the wire of a largest intermediate that lowers the
@@ -320,10 +456,37 @@ def slice_tree(tree: ContractionTree, target_bits: int, forbid: frozenset[int] =
         sliced.add(best[1])
 
 
+def unslice(tree: ContractionTree, sliced: frozenset[int], target_bits: int) -> frozenset[int]:
+    """Drops sliced wires that are no longer needed to keep every intermediate within
+    2^target_bits entries (each dropped wire halves the number of slices)."""
+    sl = set(sliced)
+    for w in sorted(sliced):
+        if tree.cost(frozenset(sl - {w}))[1] <= target_bits:
+            sl.discard(w)
+    return frozenset(sl)
+
+
+def plan_bytes(tree: ContractionTree, sliced: frozenset[int]) -> float:
+    """Algorithmic HBM bytes of the whole contraction (every slice; 4-byte intermediates,
+    1-byte leaves): each step reads both operands and writes its result once."""
+    L = tree.num_leaves
+    tot = 0.0
+    for s, (a, b) in enumerate(tree.steps):
+        for x in (a, b):
+            tot += 2.0 ** len(tree.node_wires[x] - sliced) * (1 if x < L else 4)
+        tot += 2.0 ** len(tree.node_wires[L + s] - sliced) * 4
+    return tot * 2.0 ** len(sliced)
+
+
 def optimize(net: Network, *, target_bits: int | None = 26, trials: int = 8, seed: int = 0,
-             method: str = "minfill") -> tuple[ContractionTree, frozenset[int]]:
-    """Searches ``trials`` randomized elimination orders and returns the best
-    (tree, sliced wires) by (peak bits after slicing, log2 total cost incl. slices)."""
+             method: str = "minfill", reconf: int = 10) -> tuple[ContractionTree, frozenset[int]]:
+    """Searches ``trials`` randomized elimination orders and returns the best (tree,
+    sliced wires) by (peak bits after slicing, total bytes over all slices).
+
+    Each order's tree is improved by subtree reconfiguration (subtrees of up to ``reconf``
+    inputs; 0 turns it off), sliced to ``target_bits``, reconfigured again under that
+    slicing (no intermediate above the cap), and freed of sliced wires it no longer
+    needs."""
     rng = random.Random(seed)
     prefix = simplify_order(net)
     forbid = frozenset(net.out_wires)
@@ -336,12 +499,17 @@ def optimize(net: Network, *, target_bits: int | None = 26, trials: int = 8, see
             raise ValueError(f"unknown optimisation method {method!r}")
         order = minfill_order(net, rng, prefix)
         tree = build_tree(net, order)
+        if reconf >= 3:
+            tree = reconfigure(tree, reconf)
         if target_bits is None:
             sliced = frozenset()
         else:
             sliced = slice_tree(tree, target_bits, forbid)
-        tot, peak, _ = tree.cost(sliced)
-        key = (peak, tot + len(sliced))
+            if reconf >= 3 and sliced:
+                tree = reconfigure(tree, reconf, sliced=sliced, max_bits=target_bits)
+                sliced = unslice(tree, sliced, target_bits)
+        peak = tree.cost(sliced)[1]
+        key = (peak, plan_bytes(tree, sliced))
         if best is None or key < best[0]:
             best = (key, tree, sliced)
     return best[1], best[2]
