@@ -666,6 +666,7 @@ struct StreamArgs {
                          // combination, summed combination); 0: read from global memory
   uint32_t stage_bytes;  // one stage: the item's chunks of both operands
   int32_t stages;        // stages in the ring (2 .. kStreamMaxStages)
+  int32_t kchunks;       // stages per item: its summed combinations, 4 (NK) per stage
 };
 
 // Offsets of one staged item, written by the producer next to its stage.
@@ -767,41 +768,45 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
       }
       const uint64_t left = (items - w0 + stride - 1) / stride;
       const int nb = (int)(left < 32 ? left : 32);
-      for (int k = 0; k < nb; ++k, ++i) {
-        const int s = (int)(i % nst);
-        const uint32_t round = (uint32_t)(i / nst);
+      for (int k = 0; k < nb && !stop; ++k) {
         const uint64_t bo = __shfl_sync(0xffffffffu, l_bo, k);
         const uint64_t so = __shfl_sync(0xffffffffu, l_so, k);
         const uint64_t oo = __shfl_sync(0xffffffffu, l_oo, k);
         const int p = __shfl_sync(0xffffffffu, l_p, k);
-        if (__shfl_sync(0xffffffffu, (int)bail, 0)) {
-          stop = true;
-          break;
-        }
-        if (round > 0 && !mbar_wait_warp(&empty[s], (round - 1) & 1)) {
-          if (lane == 0) {
-            atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
-            bail = 1;
+        for (int kc = 0; kc < sa.kchunks; ++kc, ++i) {  // one stage per KU summed combinations
+          const int s = (int)(i % nst);
+          const uint32_t round = (uint32_t)(i / nst);
+          if (__shfl_sync(0xffffffffu, (int)bail, 0)) {
+            stop = true;
+            break;
           }
-          stop = true;
-          break;
-        }
-        uint8_t* dst = smem + (size_t)s * sa.stage_bytes;
-        if (lane == 0) {
-          head[s].so = so;
-          head[s].oo = oo;
-          head[s].p = p;
-          mbar_expect_tx(&full[s], sa.stage_bytes);
-        }
-        __syncwarp();
-        for (int c = lane; c < ncopies; c += 32) {
-          if (c < KU) {
-            tma_load_1d(dst + c * sa.chunk_bytes, bsrc + bo + B.k_off[c], sa.chunk_bytes, &full[s]);
-          } else {
-            const int j = c - KU;
-            const int e = j / KU, ku = j % KU;
-            tma_load_1d(dst + b_bytes + j * s_chunk, ssrc + so + S.e_off[e] + S.k_off[ku], s_chunk,
-                        &full[s]);
+          if (round > 0 && !mbar_wait_warp(&empty[s], (round - 1) & 1)) {
+            if (lane == 0) {
+              atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
+              bail = 1;
+            }
+            stop = true;
+            break;
+          }
+          uint8_t* dst = smem + (size_t)s * sa.stage_bytes;
+          if (lane == 0) {
+            head[s].so = so;
+            head[s].oo = oo;
+            head[s].p = p;
+            mbar_expect_tx(&full[s], sa.stage_bytes);
+          }
+          __syncwarp();
+          const int kb = kc * KU;
+          for (int c = lane; c < ncopies; c += 32) {
+            if (c < KU) {
+              tma_load_1d(dst + c * sa.chunk_bytes, bsrc + bo + B.k_off[kb + c], sa.chunk_bytes,
+                          &full[s]);
+            } else {
+              const int j = c - KU;
+              const int e = j / KU, ku = j % KU;
+              tma_load_1d(dst + b_bytes + j * s_chunk, ssrc + so + S.e_off[e] + S.k_off[kb + ku],
+                          s_chunk, &full[s]);
+            }
           }
         }
       }
@@ -820,12 +825,116 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
   const uint32_t f_lo = threadIdx.x * V;
   const uint64_t s_lo = scatter32(S.f_lo, f_lo);
   const uint64_t o_lo = scatter32(a.of_lo, f_lo);
+  // An item whose 2^K > 4 summed combinations span kchunks stages of KU = 4: partial sums
+  // stay in registers (MODP: pairs of products reduced and added mod p; with a leaf
+  // operand each stage's four small products are reduced at once) until the last stage.
+  auto consume_chunked = [&](uint64_t& i, int leaves, auto mode_c) -> bool {
+    constexpr int kSMode = decltype(mode_c)::value;
+    using Acc = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
+    Acc part[NE][V];
+#pragma unroll
+    for (int e = 0; e < NE; ++e)
+#pragma unroll
+      for (int j = 0; j < V; ++j) part[e][j] = 0;
+    uint64_t so = 0, oo = 0;
+    PlaneConst pc{0, 0, 0};
+    for (int kc = 0; kc < sa.kchunks; ++kc, ++i) {
+      const int s = (int)(i % nst);
+      if (__shfl_sync(0xffffffffu, (int)bail, 0)) return false;
+      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
+        if (lane == 0) {
+          atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
+          bail = 1;
+        }
+        return false;
+      }
+      if (kc == 0) {
+        so = head[s].so;
+        oo = head[s].oo + o_lo;
+        pc = plane_const(ring, head[s].p);
+      }
+      const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
+      T bv[KU][V];
+#pragma unroll
+      for (int ku = 0; ku < KU; ++ku) {
+        const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
+        if constexpr (sizeof(T) == 4) {
+          const uint4 x = *reinterpret_cast<const uint4*>(src);
+          bv[ku][0] = x.x;
+          bv[ku][1] = x.y;
+          bv[ku][2] = x.z;
+          bv[ku][3] = x.w;
+        } else {
+          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
+          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
+          bv[ku][0] = x0.x;
+          bv[ku][1] = x0.y;
+          bv[ku][2] = x1.x;
+          bv[ku][3] = x1.y;
+        }
+      }
+      const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        uint64_t acc[V] = {0, 0, 0, 0};
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku) {
+          T sv[V];
+          if constexpr (kSMode == kModeGlobal)
+            tile_load<T, T, V>(S, so + s_lo + S.e_off[e] + S.k_off[kc * KU + ku], sv);
+          else
+            stage_load<kSMode, T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
+#pragma unroll
+          for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
+          if constexpr (kRing == TSG_RING_MODP) {
+            if ((ku & 1) && leaves == 0) {
+#pragma unroll
+              for (int j = 0; j < V; ++j) {
+                part[e][j] = add_mod(part[e][j], mont_redc(acc[j], pc.p, pc.pinv), pc.p);
+                acc[j] = 0;
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < V; ++j) {
+          if constexpr (kRing == TSG_RING_U64) {
+            part[e][j] += acc[j];
+          } else {
+            if (leaves != 0) part[e][j] = add_mod(part[e][j], small_mod(acc[j], pc.p), pc.p);
+          }
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      const uint64_t oe = oo + a.o_e[e];
+      if constexpr (kRing == TSG_RING_U64) {
+        uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
+        reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(part[e][0], part[e][1]);
+        reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(part[e][2], part[e][3]);
+      } else {
+        *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
+            make_uint4(part[e][0], part[e][1], part[e][2], part[e][3]);
+      }
+    }
+    return true;
+  };
   auto consume = [&](auto mode_c) {
     constexpr int kSMode = decltype(mode_c)::value;  // kModeGlobal: not staged
     // staged operands are intermediates, so only a global operand can be a leaf
     const int leaves = kSMode == kModeGlobal ? S.leaf : 0;
-    uint64_t i = 0;
+    uint64_t i = 0;  // stages consumed
     for (uint64_t w = blockIdx.x; w < items; w += gridDim.x, ++i) {
+      if constexpr (KU == 4) {
+        if (sa.kchunks > 1) {  // the item spans kchunks stages
+          if (!consume_chunked(i, leaves, mode_c)) return;
+          --i;  // consume_chunked advanced i past the item's stages
+          continue;
+        }
+      }
       const int s = (int)(i % nst);
       if (__shfl_sync(0xffffffffu, (int)bail, 0)) return;
       if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
@@ -1618,7 +1727,7 @@ uint32_t stream_span(const LaunchArgs& la, int np, uint32_t esize, uint64_t exte
   const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
   const uint64_t end = s.base + scatter_max(s.g, gbits) + narrow_max(s.f_hi, nbits) + eo + ko + span;
   ok = ok && end <= extent;
-  ok = ok && 2 * stream_stage_bytes(sh.ne, t.n_k, la.stream.chunk_bytes, span, esize) <=
+  ok = ok && 2 * stream_stage_bytes(sh.ne, std::min(t.n_k, 4), la.stream.chunk_bytes, span, esize) <=
                  kStreamBlockSmem;
   return ok ? span : 0;
 }
@@ -1629,8 +1738,8 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   const TileShape& sh = la.shape;
   // the streaming kernel stores 4 consecutive outputs as one vector: only when the 4
   // positions of a thread are 4 consecutive, aligned outputs
-  if (sh.v != 4 || (t.n_k != 1 && t.n_k != 2 && t.n_k != 4) || t.tile_bits != kStreamTileBits ||
-      !t.o_contig)
+  // up to 16 summed combinations, at most 4 per stage (an item spans n_k / 4 stages)
+  if (sh.v != 4 || t.n_k > 16 || t.tile_bits != kStreamTileBits || !t.o_contig)
     return;
   if (sh.tiles * la.cnt < (uint64_t)device_sm_count() * 8) return;  // too small to stream
   int big = -1;
@@ -1656,11 +1765,12 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   la.stream.work = sh.tiles * la.cnt;
   la.stream.chunk_bytes = kStreamTile * esize;
   la.stream.s_span = stream_span(la, np, esize, extent[1 - big]);
-  const uint64_t stage = stream_stage_bytes(sh.ne, t.n_k, la.stream.chunk_bytes,
+  const uint64_t stage = stream_stage_bytes(sh.ne, std::min(t.n_k, 4), la.stream.chunk_bytes,
                                             la.stream.s_span, esize);
   if (2 * stage > kStreamBlockSmem) return;  // fewer than two stages fit
   la.stream.stage_bytes = (uint32_t)stage;
   la.stream.stages = (int)std::min<uint64_t>(kStreamMaxStages, kStreamBlockSmem / stage);
+  la.stream.kchunks = t.n_k > 4 ? t.n_k / 4 : 1;
   la.streamed = true;
 }
 
@@ -1762,7 +1872,7 @@ tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_
 
 template <int kRing, int NE>
 tsg_status launch_stream_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  switch (la.t.n_k) {
+  switch (std::min(la.t.n_k, 4)) {
     case 1: return launch_stream_t<kRing, NE, 1>(la, ra, st);
     case 2: return launch_stream_t<kRing, NE, 2>(la, ra, st);
     default: return launch_stream_t<kRing, NE, 4>(la, ra, st);
