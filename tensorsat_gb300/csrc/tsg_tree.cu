@@ -449,8 +449,24 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
           for (int ku = 0; ku < KU; ++ku)
             tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[ku], yh[e][ku]);
       }
+      // above the hoisting budget: double buffer over E (the next combination's values
+      // are loaded before this one's stores)
+      constexpr bool kDouble = !kHoist && NK > 0 && NE > 1;
+      VT ycur[kDouble ? KU : 1][V], ynxt[kDouble ? KU : 1][V];
+      if constexpr (kDouble) {
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku)
+          tile_load<T, VT, V>(Y, yp + Y.e_off[0] + Y.k_off[ku], ycur[ku]);
+      }
 #pragma unroll
       for (int e = 0; e < NE; ++e) {
+        if constexpr (kDouble) {
+          if (e + 1 < NE) {
+#pragma unroll
+            for (int ku = 0; ku < KU; ++ku)
+              tile_load<T, VT, V>(Y, yp + Y.e_off[e + 1] + Y.k_off[ku], ynxt[ku]);
+          }
+        }
         const uint64_t oe = oo + a.o_e[e];
         AT acc[V];
         uint32_t done[V];  // MODP: reduced chunks (Montgomery form) when more than 2 sums
@@ -473,6 +489,9 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
             if constexpr (kHoist) {
 #pragma unroll
               for (int j = 0; j < V; ++j) yv[j] = yh[e][ku][j];
+            } else if constexpr (kDouble) {
+#pragma unroll
+              for (int j = 0; j < V; ++j) yv[j] = ycur[ku][j];
             } else {
               tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[kk], yv);
             }
@@ -520,6 +539,12 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
 #pragma unroll
             for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
           }
+        }
+        if constexpr (kDouble) {
+#pragma unroll
+          for (int ku = 0; ku < KU; ++ku)
+#pragma unroll
+            for (int j = 0; j < V; ++j) ycur[ku][j] = ynxt[ku][j];
         }
       }
       if (NK > 0) {
@@ -1492,7 +1517,7 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   while (((uint64_t)1 << tile_bits) < threads * v) tile_bits++;
   shape->v = v;
   shape->ne = ne;
-  shape->nk = st.k_bits == 0 ? 1 : (st.k_bits == 1 ? 2 : 0);
+  shape->nk = st.k_bits <= 2 ? (1 << st.k_bits) : 0;  // unrolled summed combinations
   shape->threads = (unsigned)threads;
   shape->tiles = positions >> tile_bits;
   if (shape->tiles >= (1ull << 31)) {
@@ -1823,6 +1848,10 @@ void launch_tile_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
   switch (la.shape.nk) {
     case 1: launch_tile_t<kRing, V, NE, 1>(la, ra, st); break;
     case 2: launch_tile_t<kRing, V, NE, 2>(la, ra, st); break;
+    case 4:  // unrolled only for OR-AND (the count rings stream their large K = 2 steps)
+      if constexpr (kRing == TSG_RING_OR_AND) launch_tile_t<kRing, V, NE, 4>(la, ra, st);
+      else launch_tile_t<kRing, V, NE, 0>(la, ra, st);
+      break;
     default: launch_tile_t<kRing, V, NE, 0>(la, ra, st); break;
   }
 }
