@@ -25,1084 +25,30 @@
 #include <vector>
 
 #include "tsg_common.cuh"
+#include "tsg_tree_dev.cuh"
 
 namespace tsg {
+using namespace dev;
 namespace {
 
-constexpr int kMaxRuns = 64;
-constexpr int kThreads = 256;
-
-struct BitMap {
-  int32_t n;
-  uint8_t src[kMaxRuns];
-  uint8_t len[kMaxRuns];
-  uint8_t dst[kMaxRuns];
-};
-
-struct StepArgs {
-  const uint8_t* lhs;
-  const uint8_t* rhs;
-  uint8_t* out;
-  uint64_t l_base, r_base;             // constant element offsets
-  uint64_t l_plane, r_plane, o_plane;  // residue-plane strides (elements)
-  uint64_t total;                      // output entries of this launch
-  int32_t k_bits;
-  BitMap lt, lk, rt, rk;
-};
-
-// Residues mod p are kept in Montgomery form (x * 2^32 mod p) in every intermediate; the
-// root reduction converts back, so results are plain residues.
-struct RingArgs {
-  int32_t np;
-  uint32_t p[TSG_MAX_PRIMES];
-  uint64_t m[TSG_MAX_PRIMES];     // Barrett constants floor((2^64-1)/p)
-  uint32_t pinv[TSG_MAX_PRIMES];  // -p^-1 mod 2^32
-  uint32_t r1[TSG_MAX_PRIMES];    // 2^32 mod p (Montgomery form of 1)
-};
-
-// Montgomery-form value of sum_k L*R for one output and prime, from the 64-bit sum of
-// products `acc` (operands: plain 0/1 for leaves, Montgomery residues otherwise):
-//   both leaves:   acc is a plain count <= 16      -> acc * (2^32 mod p) mod p
-//   one leaf:      acc is a sum of <= 16 residues  -> reduce the small multiple
-//   no leaf:       acc < 2 p^2 (two products)      -> Montgomery reduction
-__device__ __forceinline__ uint32_t mont_finish(uint64_t acc, int leaves, const RingArgs& ring,
-                                                int p) {
-  if (leaves == 2) return small_mod(acc * ring.r1[p], ring.p[p]);
-  if (leaves == 1) return small_mod(acc, ring.p[p]);
-  return mont_redc(acc, ring.p[p], ring.pinv[p]);
-}
-
-// One plane's constants, selected from the kernel parameters without dynamic indexing
-// (which would copy the parameter block to local memory).
-struct PlaneConst {
-  uint32_t p, pinv, r1;
-};
-
-__device__ __forceinline__ PlaneConst plane_const(const RingArgs& ring, int p) {
-  PlaneConst c{ring.p[0], ring.pinv[0], ring.r1[0]};
-#pragma unroll
-  for (int i = 1; i < TSG_MAX_PRIMES; ++i)
-    if (p == i) c = PlaneConst{ring.p[i], ring.pinv[i], ring.r1[i]};
-  return c;
-}
-
-// mont_finish with the plane's constants in registers.
-__device__ __forceinline__ uint32_t mont_finish_c(uint64_t acc, int leaves, const PlaneConst& c) {
-  if (leaves == 2) return small_mod(acc * c.r1, c.p);
-  if (leaves == 1) return small_mod(acc, c.p);
-  return mont_redc(acc, c.p, c.pinv);
-}
-
-__device__ __forceinline__ uint64_t scatter_bits(const BitMap& m, uint64_t x) {
-  uint64_t r = 0;
-#pragma unroll 1
-  for (int i = 0; i < m.n; ++i)
-    r |= ((x >> m.src[i]) & ((1ull << m.len[i]) - 1ull)) << m.dst[i];
-  return r;
-}
-
-template <bool kLeaf, typename T>
-__device__ __forceinline__ T load_elem(const uint8_t* base, uint64_t off) {
-  if constexpr (kLeaf) {
-    return (T)base[off];
-  } else {
-    return reinterpret_cast<const T*>(base)[off];
-  }
-}
-
-// One pairwise contraction step: out[t] = sum_k lhs[scatter(t,k)] * rhs[scatter(t,k)] in
-// the ring kRing. kLLeaf / kRLeaf mark uint8 leaf operands (widened on load).
-template <int kRing, bool kLLeaf, bool kRLeaf>
-__global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArgs ring) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t nk = 1ull << a.k_bits;
-  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.total; t += stride) {
-    const uint64_t lo = a.l_base + scatter_bits(a.lt, t);
-    const uint64_t ro = a.r_base + scatter_bits(a.rt, t);
-    if constexpr (kRing == TSG_RING_OR_AND) {
-      uint32_t acc = 0;
-      for (uint64_t kk = 0; kk < nk; ++kk) {
-        acc |= (uint32_t)a.lhs[lo + scatter_bits(a.lk, kk)] &
-               (uint32_t)a.rhs[ro + scatter_bits(a.rk, kk)];
-      }
-      a.out[t] = acc ? 1 : 0;
-    } else if constexpr (kRing == TSG_RING_U64) {
-      uint64_t acc = 0;
-      for (uint64_t kk = 0; kk < nk; ++kk) {
-        acc += load_elem<kLLeaf, uint64_t>(a.lhs, lo + scatter_bits(a.lk, kk)) *
-               load_elem<kRLeaf, uint64_t>(a.rhs, ro + scatter_bits(a.rk, kk));
-      }
-      reinterpret_cast<uint64_t*>(a.out)[t] = acc;
-    } else {
-      // Montgomery residues; products of two residues are reduced pairwise (2 p^2 < p 2^32)
-      constexpr int leaves = (kLLeaf ? 1 : 0) + (kRLeaf ? 1 : 0);
-      uint32_t acc[TSG_MAX_PRIMES] = {0, 0, 0, 0};
-      uint64_t part[TSG_MAX_PRIMES] = {0, 0, 0, 0};
-      for (uint64_t kk = 0; kk < nk; ++kk) {
-        const uint64_t lko = lo + scatter_bits(a.lk, kk);
-        const uint64_t rko = ro + scatter_bits(a.rk, kk);
-#pragma unroll
-        for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
-          if (p < ring.np) {
-            const uint32_t l = load_elem<kLLeaf, uint32_t>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane));
-            const uint32_t r = load_elem<kRLeaf, uint32_t>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane));
-            part[p] += (uint64_t)l * r;
-            if (leaves == 0 ? (kk & 1) : ((kk & 15) == 15)) {
-              acc[p] = add_mod(acc[p], mont_finish(part[p], leaves, ring, p), ring.p[p]);
-              part[p] = 0;
-            }
-          }
-        }
-      }
-      uint32_t* out = reinterpret_cast<uint32_t*>(a.out);
-#pragma unroll
-      for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
-        if (p < ring.np)
-          out[t + p * a.o_plane] = add_mod(acc[p], mont_finish(part[p], leaves, ring, p), ring.p[p]);
-      }
-    }
-  }
-}
-
-// ------------------------------------------------------------------------------------
-// Tile kernel: the common case where a slice's tensors have < 2^32 entries and at most
-// 4 wires are summed. Output bits split into three groups:
-//   E  up to 2 "enumerated" bits, looped over inside a thread: the output bits the larger
-//      operand does not carry, so that operand is read once and reused for every E value;
-//   F  the remaining output bits; the low `tile_bits` of them index threads (V consecutive
-//      positions per thread), the rest index blocks (blockIdx.x);
-//   g  the slice slot (blockIdx.y).
-// Every operand offset is base + scatter(g) + scatter(F high) [uniform per block] +
-// scatter(F low) [once per thread] + tables for the V positions, E values and summed
-// combinations, so the per-output index work is a few table adds.
-
-constexpr int kMaxNarrowRuns = 32;
-constexpr int kModeGather = 0;
-constexpr int kModeContig = 1;
-constexpr int kModeBcast = 2;
-constexpr int kModePair = 3;  // two distinct offsets: 0 and tab[3]; pair_sel picks per position
-// OR-AND, 16 byte positions of which the operand carries c <= 3 of the 4 index bits: the
-// 2^c distinct bytes (offsets dtab) are packed into two words and spread over the four
-// output words with byte permutes (selectors psel)
-constexpr int kModePerm = 4;
-constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
-constexpr int kMaxK = 16;  // summed combinations kept in tables (k <= 4)
-
-struct NarrowMap {
-  int32_t n;
-  uint8_t src[kMaxNarrowRuns];
-  uint8_t len[kMaxNarrowRuns];
-  uint8_t dst[kMaxNarrowRuns];
-};
-
-struct TileOperand {
-  const uint8_t* ptr;
-  uint64_t base;          // constant element offset
-  uint64_t plane;         // residue-plane stride (elements); 0 for leaves
-  NarrowMap f_lo, f_hi;   // F bits below / at or above tile_bits -> operand bits
-  BitMap g;               // slice-slot bits -> operand bits
-  uint32_t tab[16];       // offsets of the V consecutive F positions
-  uint32_t e_off[kMaxE];  // offsets of the E combinations
-  uint32_t k_off[kMaxK];  // offsets of the summed combinations
-  int32_t mode;           // kModeContig / kModeBcast / kModePair / kModeGather / kModePerm
-  int32_t pair_sel;       // kModePair: bit j set when position j reads offset tab[3]
-  int32_t has_e;          // carries E bits (reloaded per E combination)
-  int32_t leaf;           // uint8 leaf (widened on load)
-  int32_t pn;             // kModePerm: distinct values (2, 4 or 8)
-  uint32_t dtab[8];       // kModePerm: their offsets
-  uint32_t psel[4];       // kModePerm: __byte_perm selector of each output word
-};
-
-struct TileArgs {
-  TileOperand op[2];
-  uint8_t* out;
-  uint64_t o_plane;
-  uint32_t n_out;          // outputs per slice
-  NarrowMap of_lo, of_hi;  // F bits -> output bit positions
-  uint32_t o_tab[16];
-  uint32_t o_e[kMaxE];
-  int32_t tile_bits;
-  int32_t n_k;             // summed combinations (2^k)
-  int32_t o_contig;        // the V positions are consecutive outputs
-};
-
-__device__ __forceinline__ uint32_t scatter32(const NarrowMap& m, uint32_t x) {
-  uint32_t r = 0;
-#pragma unroll 1
-  for (int i = 0; i < m.n; ++i) r |= ((x >> m.src[i]) & ((1u << m.len[i]) - 1u)) << m.dst[i];
-  return r;
-}
-
-// Loads the V values of one operand (residue plane already folded into `off`).
-template <typename T, typename VT, int V>
-__device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, VT (&out)[V]) {
-  const uint8_t* base = op.ptr;
-  if (op.leaf) {
-    if (V == 16 && op.mode == kModeContig) {
-      const uint4 w = *reinterpret_cast<const uint4*>(base + off);
-      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = (VT)((ws[j / 4] >> (8 * (j % 4))) & 0xff);
-    } else if (V == 4 && op.mode == kModeContig) {
-      const uint32_t w = *reinterpret_cast<const uint32_t*>(base + off);
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = (VT)((w >> (8 * j)) & 0xff);
-    } else if (op.mode == kModeBcast) {
-      const VT x = (VT)base[off];
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = x;
-    } else if (V == 4 && op.mode == kModePair) {
-      const VT x0 = (VT)base[off], x1 = (VT)base[off + op.tab[3]];
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
-    } else {
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = (VT)base[off + op.tab[j]];
-    }
-    return;
-  }
-  const T* p = reinterpret_cast<const T*>(base);
-  if (V == 16 && op.mode == kModeContig) {
-    if constexpr (sizeof(T) == 1) {
-      const uint4 w = *reinterpret_cast<const uint4*>(p + off);
-      const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = (VT)((ws[j / 4] >> (8 * (j % 4))) & 0xff);
-    }
-  } else if (V == 4 && op.mode == kModeContig) {
-    if constexpr (sizeof(T) == 1) {
-      const uint32_t w = *reinterpret_cast<const uint32_t*>(p + off);
-#pragma unroll
-      for (int j = 0; j < V; ++j) out[j] = (VT)((w >> (8 * j)) & 0xff);
-    } else if constexpr (sizeof(T) == 4) {
-      const uint4 w = *reinterpret_cast<const uint4*>(p + off);
-      out[0] = w.x;
-      out[1 % V] = w.y;
-      out[2 % V] = w.z;
-      out[3 % V] = w.w;
-    } else {
-      const ulonglong2* q = reinterpret_cast<const ulonglong2*>(p + off);
-      const ulonglong2 w0 = q[0], w1 = q[1];
-      out[0] = w0.x;
-      out[1 % V] = w0.y;
-      out[2 % V] = w1.x;
-      out[3 % V] = w1.y;
-    }
-  } else if (op.mode == kModeBcast) {
-    const VT x = (VT)p[off];
-#pragma unroll
-    for (int j = 0; j < V; ++j) out[j] = x;
-  } else if (V == 4 && op.mode == kModePair) {
-    const VT x0 = (VT)p[off], x1 = (VT)p[off + op.tab[3]];
-#pragma unroll
-    for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
-  } else {
-#pragma unroll
-    for (int j = 0; j < V; ++j) out[j] = (VT)p[off + op.tab[j]];
-  }
-}
-
-// OR-AND values are 0/1 bytes, so four positions packed in a 32-bit word combine with
-// word-wide AND / OR. Loads `V` positions (V = 4 or 16) as V/4 packed words.
-template <int V>
-__device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t off,
-                                                 uint32_t (&w)[V / 4]) {
-  const uint8_t* base = op.ptr;
-  if (op.mode == kModeContig) {
-    if constexpr (V == 16) {
-      const uint4 x = *reinterpret_cast<const uint4*>(base + off);
-      w[0] = x.x;
-      w[1 % (V / 4)] = x.y;
-      w[2 % (V / 4)] = x.z;
-      w[3 % (V / 4)] = x.w;
-    } else {
-      w[0] = *reinterpret_cast<const uint32_t*>(base + off);
-    }
-  } else if (op.mode == kModeBcast) {
-    const uint32_t x = (uint32_t)base[off] * 0x01010101u;
-#pragma unroll
-    for (int i = 0; i < V / 4; ++i) w[i] = x;
-  } else if (V == 4 && op.mode == kModePair) {
-    const uint32_t x0 = base[off], x1 = base[off + op.tab[3]];
-    uint32_t r = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) r |= (((op.pair_sel >> j) & 1) ? x1 : x0) << (8 * j);
-    w[0] = r;
-  } else if (V == 16 && op.mode == kModePerm) {
-    uint32_t w0 = 0, w1 = 0;
-#pragma unroll
-    for (int d = 0; d < 8; ++d) {
-      if (d < op.pn) {
-        const uint32_t b = base[off + op.dtab[d]];
-        if (d < 4) w0 |= b << (8 * d);
-        else w1 |= b << (8 * (d - 4));
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < V / 4; ++i) w[i] = __byte_perm(w0, w1, op.psel[i]);
-  } else {
-#pragma unroll
-    for (int i = 0; i < V / 4; ++i) {
-      uint32_t r = 0;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) r |= (uint32_t)base[off + op.tab[4 * i + j]] << (8 * j);
-      w[i] = r;
-    }
-  }
-}
-
-// One thread's work in the tile kernel. X is an operand without E bits (loaded once per
-// residue plane and reused for every E value), Y the other one; the ring products commute,
-// so the kernel passes (lhs, rhs) or (rhs, lhs). With a fixed summed count (NK > 0) the
-// thread gathers all of Y's values of a plane before its first store: loads placed after
-// a store to a possibly aliasing address would each wait out their own latency.
-template <int kRing, int V, int NE, int NK>
-__device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& ring,
-                                            const TileOperand& X, const TileOperand& Y,
-                                            uint64_t x0, uint64_t y0, uint64_t oo) {
-  using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
-            typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
-  using VT = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
-  using AT = uint64_t;
-  constexpr bool kPacked = (kRing == TSG_RING_OR_AND) && (V % 4 == 0);
-  constexpr int W = kPacked ? V / 4 : 1;  // packed words per operand (OR-AND)
-  constexpr int KU = NK > 0 ? NK : 1;
-  const int nk = NK > 0 ? NK : a.n_k;
-  if constexpr (kPacked) {
-    constexpr bool kHoist = NK > 0 && NE * KU * W <= 16;  // more spills registers
-    uint32_t xw[KU][W];
-    uint32_t yh[kHoist ? NE : 1][KU][W];
-    if (NK > 0) {
-#pragma unroll
-      for (int ku = 0; ku < KU; ++ku) tile_load_packed<V>(X, x0 + X.k_off[ku], xw[ku]);
-    }
-    if constexpr (kHoist) {
-#pragma unroll
-      for (int e = 0; e < NE; ++e)
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku)
-          tile_load_packed<V>(Y, y0 + Y.e_off[e] + Y.k_off[ku], yh[e][ku]);
-    }
-#pragma unroll
-    for (int e = 0; e < NE; ++e) {
-      uint32_t acc[W];
-#pragma unroll
-      for (int i = 0; i < W; ++i) acc[i] = 0;
-      for (int kk0 = 0; kk0 < nk; kk0 += KU) {
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku) {
-          const int kk = kk0 + ku;
-          uint32_t xv[W], yv[W];
-          if (NK > 0) {
-#pragma unroll
-            for (int i = 0; i < W; ++i) xv[i] = xw[ku][i];
-          } else {
-            tile_load_packed<V>(X, x0 + X.k_off[kk], xv);
-          }
-          if constexpr (kHoist) {
-#pragma unroll
-            for (int i = 0; i < W; ++i) yv[i] = yh[e][ku][i];
-          } else {
-            tile_load_packed<V>(Y, y0 + Y.e_off[e] + Y.k_off[kk], yv);
-          }
-#pragma unroll
-          for (int i = 0; i < W; ++i) acc[i] |= xv[i] & yv[i];
-        }
-      }
-      const uint64_t oe = oo + a.o_e[e];
-      if (a.o_contig) {
-        if constexpr (V == 16) {
-          *reinterpret_cast<uint4*>(a.out + oe) =
-              make_uint4(acc[0], acc[1 % W], acc[2 % W], acc[3 % W]);
-        } else {
-          *reinterpret_cast<uint32_t*>(a.out + oe) = acc[0];
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = (acc[j / 4] >> (8 * (j % 4))) & 0xff;
-      }
-    }
-  } else {
-    // planes outermost; X of plane p+1 is loaded while plane p is combined
-    constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
-    constexpr bool kHoist = NK > 0 && NE * KU * V * sizeof(VT) <= 64;  // more spills registers
-    const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
-    const int leaves = X.leaf + Y.leaf;
-    VT xcur[KU][V], xnxt[KU][V];
-    auto preload = [&](int p, VT (&xb)[KU][V]) {
-      const uint64_t xp = x0 + (X.leaf ? 0 : p * X.plane);
-#pragma unroll
-      for (int ku = 0; ku < KU; ++ku) tile_load<T, VT, V>(X, xp + X.k_off[ku], xb[ku]);
-    };
-    if (NK > 0) preload(0, xcur);
-#pragma unroll
-    for (int p = 0; p < PP; ++p) {
-      if (p >= np) break;
-      if (NK > 0 && p + 1 < np) preload(p + 1, xnxt);
-      const uint64_t xp = x0 + (X.leaf ? 0 : p * X.plane);
-      const uint64_t yp = y0 + (Y.leaf ? 0 : p * Y.plane);
-      VT yh[kHoist ? NE : 1][KU][V];
-      if constexpr (kHoist) {
-#pragma unroll
-        for (int e = 0; e < NE; ++e)
-#pragma unroll
-          for (int ku = 0; ku < KU; ++ku)
-            tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[ku], yh[e][ku]);
-      }
-      // above the hoisting budget: double buffer over E (the next combination's values
-      // are loaded before this one's stores)
-      constexpr bool kDouble = !kHoist && NK > 0 && NE > 1;
-      VT ycur[kDouble ? KU : 1][V], ynxt[kDouble ? KU : 1][V];
-      if constexpr (kDouble) {
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku)
-          tile_load<T, VT, V>(Y, yp + Y.e_off[0] + Y.k_off[ku], ycur[ku]);
-      }
-#pragma unroll
-      for (int e = 0; e < NE; ++e) {
-        if constexpr (kDouble) {
-          if (e + 1 < NE) {
-#pragma unroll
-            for (int ku = 0; ku < KU; ++ku)
-              tile_load<T, VT, V>(Y, yp + Y.e_off[e + 1] + Y.k_off[ku], ynxt[ku]);
-          }
-        }
-        const uint64_t oe = oo + a.o_e[e];
-        AT acc[V];
-        uint32_t done[V];  // MODP: reduced chunks (Montgomery form) when more than 2 sums
-#pragma unroll
-        for (int j = 0; j < V; ++j) {
-          acc[j] = 0;
-          done[j] = 0;
-        }
-        for (int kk0 = 0; kk0 < nk; kk0 += KU) {
-#pragma unroll
-          for (int ku = 0; ku < KU; ++ku) {
-            const int kk = kk0 + ku;
-            VT xv[V], yv[V];
-            if (NK > 0) {
-#pragma unroll
-              for (int j = 0; j < V; ++j) xv[j] = xcur[ku][j];
-            } else {
-              tile_load<T, VT, V>(X, xp + X.k_off[kk], xv);
-            }
-            if constexpr (kHoist) {
-#pragma unroll
-              for (int j = 0; j < V; ++j) yv[j] = yh[e][ku][j];
-            } else if constexpr (kDouble) {
-#pragma unroll
-              for (int j = 0; j < V; ++j) yv[j] = ycur[ku][j];
-            } else {
-              tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[kk], yv);
-            }
-#pragma unroll
-            for (int j = 0; j < V; ++j) {
-              if constexpr (kRing == TSG_RING_OR_AND) {
-                acc[j] |= xv[j] & yv[j];
-              } else {
-                acc[j] += (AT)xv[j] * (AT)yv[j];
-              }
-            }
-            if constexpr (kRing == TSG_RING_MODP) {
-              // two Montgomery products stay below p 2^32: reduce every pair of sums
-              if (leaves == 0 && (kk & 1) && kk + 1 < nk) {
-#pragma unroll
-                for (int j = 0; j < V; ++j) {
-                  done[j] = add_mod(done[j], mont_redc(acc[j], ring.p[p], ring.pinv[p]), ring.p[p]);
-                  acc[j] = 0;
-                }
-              }
-            }
-          }
-        }
-        if constexpr (kRing == TSG_RING_OR_AND) {
-#pragma unroll
-          for (int j = 0; j < V; ++j) a.out[oe + a.o_tab[j]] = acc[j] ? 1 : 0;
-        } else if constexpr (kRing == TSG_RING_U64) {
-          uint64_t* out = reinterpret_cast<uint64_t*>(a.out);
-          if (V == 4 && a.o_contig) {
-            reinterpret_cast<ulonglong2*>(out + oe)[0] = make_ulonglong2(acc[0], acc[1 % V]);
-            reinterpret_cast<ulonglong2*>(out + oe)[1] = make_ulonglong2(acc[2 % V], acc[3 % V]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = acc[j];
-          }
-        } else {
-          uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane;
-          uint32_t r[V];
-#pragma unroll
-          for (int j = 0; j < V; ++j)
-            r[j] = add_mod(done[j], mont_finish(acc[j], leaves, ring, p), ring.p[p]);
-          if (V == 4 && a.o_contig) {
-            *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1 % V], r[2 % V], r[3 % V]);
-          } else {
-#pragma unroll
-            for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
-          }
-        }
-        if constexpr (kDouble) {
-#pragma unroll
-          for (int ku = 0; ku < KU; ++ku)
-#pragma unroll
-            for (int j = 0; j < V; ++j) ycur[ku][j] = ynxt[ku][j];
-        }
-      }
-      if (NK > 0) {
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku)
-#pragma unroll
-          for (int j = 0; j < V; ++j) xcur[ku][j] = xnxt[ku][j];
-      }
-    }
-  }
-}
-
-template <int kRing, int V, int NE, int NK>
-__global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a, RingArgs ring) {
-  const uint32_t g = blockIdx.y;
-  const uint32_t f_hi = blockIdx.x << a.tile_bits;
-  const uint32_t f_lo = threadIdx.x * (uint32_t)V;
-  uint64_t xo[2];
-#pragma unroll
-  for (int o = 0; o < 2; ++o) {
-    const TileOperand& op = a.op[o];
-    xo[o] = op.base + scatter_bits(op.g, g) + scatter32(op.f_hi, f_hi) + scatter32(op.f_lo, f_lo);
-  }
-  const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
-  // at most one operand carries E bits (the other is the one E was chosen against)
-  if (!a.op[0].has_e)
-    tile_thread<kRing, V, NE, NK>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo);
-  else
-    tile_thread<kRing, V, NE, NK>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo);
-}
-
-// ------------------------------------------------------------------------------------
-// Streaming kernel for the large steps (the bulk of the HBM traffic). Persistent blocks
-// walk the (tile, slice) work items with a warp-specialised pipeline:
-//   * an item is one residue plane of one 1024-element tile of one slice;
-//   * a producer warp stages items into a ring of `stages` shared-memory stages with TMA
-//     bulk copies (cp.async.bulk ... mbarrier::complete_tx): the E-free operand's tile
-//     for every summed combination and, where its offsets allow (s_span > 0), the other
-//     operand's aligned blocks for the tile, plus the item's offsets in a stage header;
-//   * 8 consumer warps (4 positions per thread) combine an item from its stage, write the
-//     result from registers as 16-byte vectors, and release the stage (one arrival per
-//     warp on the stage's `empty` barrier); nothing else synchronises the block.
-// Every mbarrier wait is bounded: on expiry the thread records an error in
-// g_device_error and sets the block's bail flag; the producer then waits (bounded) for
-// the copies it has in flight and every thread returns.
-
-constexpr int kStreamTileBits = 10;                      // 256 consumer threads x 4
-constexpr int kStreamTile = 1 << kStreamTileBits;
-constexpr int kStreamConsumers = 256;
-constexpr int kStreamThreads = kStreamConsumers + 32;    // + the producer warp
-constexpr int kStreamMaxStages = 8;
-constexpr uint64_t kWaitLimitNs = 2000000000ull;         // one bounded wait: 2 s
-constexpr uint32_t kSuspendHintNs = 20000;               // longest suspension per try_wait
-
+// Device-side failure record of the streaming kernels (they receive its address).
 __device__ int g_device_error = 0;  // 0 = ok, else TSG_ERR_TIMEOUT
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
-               : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n.reg .pred p;\n"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      "selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// try_wait that may suspend the thread in hardware for up to kSuspendHintNs while the
-// phase is incomplete, instead of returning at once (no issue slots spent polling).
-__device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n.reg .pred p;\n"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
-      "selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendHintNs)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t global_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-// Bounded wait for phase `parity` of `bar`: false when kWaitLimitNs of wall-clock time
-// (the global nanosecond timer) passed without the phase completing.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  if (mbar_try_wait_suspend(bar, parity)) return true;
-  const uint64_t t0 = global_ns();
-  for (;;) {
-    if (mbar_try_wait_suspend(bar, parity)) return true;
-    if (global_ns() - t0 > kWaitLimitNs) return false;
+// Address of g_device_error on the current device (looked up once per device).
+tsg_status device_error_address(int** out) {
+  static std::mutex mu;
+  static int* addr[64] = {};
+  int dev = 0;
+  TSG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(TSG_ERR_UNSUPPORTED, "device ordinal outside 0..63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    TSG_CUDA_TRY(cudaGetSymbolAddress(&p, g_device_error));
+    addr[dev] = static_cast<int*>(p);
   }
-}
-
-// Warp-uniform bounded wait (every lane of the warp calls it): lane 0 polls, the outcome
-// is broadcast, and on success every lane observes the completed phase itself (acquire).
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity) {
-  int ok = 0;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity) ? 1 : 0;
-  ok = __shfl_sync(0xffffffffu, ok, 0);
-  if (ok) (void)mbar_try_wait(bar, parity);
-  return ok != 0;
-}
-
-__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes,
-                                            uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
-          "r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-
-struct StreamArgs {
-  int32_t big;           // operand staged through shared memory (0 = lhs, 1 = rhs)
-  uint32_t tiles;        // tiles per slice
-  uint64_t work;         // tiles * slices
-  uint32_t chunk_bytes;  // one (plane, summed combination) chunk of the staged operand
-  uint32_t s_span;       // elements of one staged chunk of the other operand per (plane, E
-                         // combination, summed combination); 0: read from global memory
-  uint32_t stage_bytes;  // one stage: the item's chunks of both operands
-  int32_t stages;        // stages in the ring (2 .. kStreamMaxStages)
-  int32_t kchunks;       // stages per item: its summed combinations, 4 (NK) per stage
-};
-
-// Offsets of one staged item, written by the producer next to its stage.
-struct StreamItem {
-  uint64_t so;  // the other operand's offset for the tile and plane (positions excluded)
-  uint64_t oo;  // output offset for the tile and plane (positions excluded)
-  int32_t p;    // residue plane
-};
-
-// Loads the V values of the other operand from its staged chunk: `p` points at the
-// thread's first position, the tile's positions sit at the operand's tab offsets. The
-// load mode is a template parameter (the streaming consumer is specialised on it).
-constexpr int kModeGlobal = -1;  // the streaming kernel's other operand is not staged
-
-template <int kMode, typename T, int V>
-__device__ __forceinline__ void stage_load(const TileOperand& op, const T* p, T (&out)[V]) {
-  if constexpr (kMode == kModeContig) {
-    if constexpr (sizeof(T) == 4) {
-      const uint4 x = *reinterpret_cast<const uint4*>(p);
-      out[0] = x.x;
-      out[1 % V] = x.y;
-      out[2 % V] = x.z;
-      out[3 % V] = x.w;
-    } else {
-      const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(p)[0];
-      const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(p)[1];
-      out[0] = x0.x;
-      out[1 % V] = x0.y;
-      out[2 % V] = x1.x;
-      out[3 % V] = x1.y;
-    }
-  } else if constexpr (kMode == kModeBcast) {
-    const T x = p[0];
-#pragma unroll
-    for (int j = 0; j < V; ++j) out[j] = x;
-  } else if constexpr (kMode == kModePair) {
-    const T x0 = p[0], x1 = p[op.tab[3]];
-#pragma unroll
-    for (int j = 0; j < V; ++j) out[j] = ((op.pair_sel >> j) & 1) ? x1 : x0;
-  } else {
-#pragma unroll
-    for (int j = 0; j < V; ++j) out[j] = p[op.tab[j]];
-  }
-}
-
-template <int kRing, int NE, int NK>
-__global__ void __launch_bounds__(kStreamThreads, 3)
-    tree_step_stream_kernel(TileArgs a, RingArgs ring, StreamArgs sa) {
-  using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
-  constexpr int V = 4;
-  constexpr int KU = NK;  // NK in {1, 2, 4}: 2^K summed combinations
-  extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ __align__(8) uint64_t full[kStreamMaxStages], empty[kStreamMaxStages];
-  __shared__ StreamItem head[kStreamMaxStages];
-  __shared__ volatile int bail;
-  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
-  const TileOperand& B = a.op[sa.big];
-  const TileOperand& S = a.op[1 - sa.big];
-  const bool s_staged = sa.s_span != 0;
-  const uint32_t b_bytes = (uint32_t)KU * sa.chunk_bytes;
-  const uint32_t s_chunk = sa.s_span * (uint32_t)sizeof(T);
-  const int nst = sa.stages;
-  const uint64_t items = sa.work * (uint64_t)np;  // (tile, slice, residue plane)
-  const int lane = threadIdx.x & 31;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < nst; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], kStreamConsumers / 32);
-    }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    bail = 0;
-  }
-  __syncthreads();
-
-  if (threadIdx.x >= kStreamConsumers) {
-    // producer warp: lane 0 writes the item's offsets into the stage header and arms the
-    // stage's barrier with the byte count (its arrival releases the header), then the
-    // lanes issue the bulk copies (KU tiles of B, NE x KU blocks of the other operand)
-    const T* bsrc = reinterpret_cast<const T*>(B.ptr);
-    const T* ssrc = reinterpret_cast<const T*>(S.ptr);
-    const int ncopies = KU + (s_staged ? NE * KU : 0);
-    const uint64_t stride = gridDim.x;
-    uint64_t i = 0;  // items issued by this block
-    bool stop = false;
-    for (uint64_t w0 = blockIdx.x; w0 < items && !stop; w0 += 32 * stride) {
-      // lane L computes the offsets of the block's item w0 + L * stride
-      const uint64_t wl = w0 + (uint64_t)lane * stride;
-      uint64_t l_bo = 0, l_so = 0, l_oo = 0;
-      int l_p = 0;
-      if (wl < items) {
-        l_p = (int)(wl % np);
-        const uint64_t tw = wl / np;
-        const uint32_t g = (uint32_t)(tw / sa.tiles);
-        const uint32_t f_hi = (uint32_t)(tw % sa.tiles) << kStreamTileBits;
-        l_bo = B.base + scatter_bits(B.g, g) + scatter32(B.f_hi, f_hi) + l_p * B.plane;
-        l_so = S.base + scatter_bits(S.g, g) + scatter32(S.f_hi, f_hi) + (S.leaf ? 0 : l_p * S.plane);
-        l_oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + l_p * a.o_plane;
-      }
-      const uint64_t left = (items - w0 + stride - 1) / stride;
-      const int nb = (int)(left < 32 ? left : 32);
-      for (int k = 0; k < nb && !stop; ++k) {
-        const uint64_t bo = __shfl_sync(0xffffffffu, l_bo, k);
-        const uint64_t so = __shfl_sync(0xffffffffu, l_so, k);
-        const uint64_t oo = __shfl_sync(0xffffffffu, l_oo, k);
-        const int p = __shfl_sync(0xffffffffu, l_p, k);
-        for (int kc = 0; kc < sa.kchunks; ++kc, ++i) {  // one stage per KU summed combinations
-          const int s = (int)(i % nst);
-          const uint32_t round = (uint32_t)(i / nst);
-          if (__shfl_sync(0xffffffffu, (int)bail, 0)) {
-            stop = true;
-            break;
-          }
-          if (round > 0 && !mbar_wait_warp(&empty[s], (round - 1) & 1)) {
-            if (lane == 0) {
-              atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
-              bail = 1;
-            }
-            stop = true;
-            break;
-          }
-          uint8_t* dst = smem + (size_t)s * sa.stage_bytes;
-          if (lane == 0) {
-            head[s].so = so;
-            head[s].oo = oo;
-            head[s].p = p;
-            mbar_expect_tx(&full[s], sa.stage_bytes);
-          }
-          __syncwarp();
-          const int kb = kc * KU;
-          for (int c = lane; c < ncopies; c += 32) {
-            if (c < KU) {
-              tma_load_1d(dst + c * sa.chunk_bytes, bsrc + bo + B.k_off[kb + c], sa.chunk_bytes,
-                          &full[s]);
-            } else {
-              const int j = c - KU;
-              const int e = j / KU, ku = j % KU;
-              tma_load_1d(dst + b_bytes + j * s_chunk, ssrc + so + S.e_off[e] + S.k_off[kb + ku],
-                          s_chunk, &full[s]);
-            }
-          }
-        }
-      }
-    }
-    // the copies of the last (up to) nst items may still be in flight: wait for them
-    if (lane == 0) {
-      const uint64_t first = i > (uint64_t)nst ? i - nst : 0;
-      for (uint64_t j = first; j < i; ++j)
-        (void)mbar_wait_bounded(&full[j % nst], (uint32_t)((j / nst) & 1));
-    }
-    return;
-  }
-
-  // consumer warps: one residue plane of one tile per item; the loop is specialised on how
-  // the other operand is read (its staged load mode, or global loads when not staged)
-  const uint32_t f_lo = threadIdx.x * V;
-  const uint64_t s_lo = scatter32(S.f_lo, f_lo);
-  const uint64_t o_lo = scatter32(a.of_lo, f_lo);
-  // An item whose 2^K > 4 summed combinations span kchunks stages of KU = 4: partial sums
-  // stay in registers (MODP: pairs of products reduced and added mod p; with a leaf
-  // operand each stage's four small products are reduced at once) until the last stage.
-  auto consume_chunked = [&](uint64_t& i, int leaves, auto mode_c) -> bool {
-    constexpr int kSMode = decltype(mode_c)::value;
-    using Acc = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
-    Acc part[NE][V];
-#pragma unroll
-    for (int e = 0; e < NE; ++e)
-#pragma unroll
-      for (int j = 0; j < V; ++j) part[e][j] = 0;
-    uint64_t so = 0, oo = 0;
-    PlaneConst pc{0, 0, 0};
-    for (int kc = 0; kc < sa.kchunks; ++kc, ++i) {
-      const int s = (int)(i % nst);
-      if (__shfl_sync(0xffffffffu, (int)bail, 0)) return false;
-      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
-        if (lane == 0) {
-          atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
-          bail = 1;
-        }
-        return false;
-      }
-      if (kc == 0) {
-        so = head[s].so;
-        oo = head[s].oo + o_lo;
-        pc = plane_const(ring, head[s].p);
-      }
-      const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
-      T bv[KU][V];
-#pragma unroll
-      for (int ku = 0; ku < KU; ++ku) {
-        const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
-        if constexpr (sizeof(T) == 4) {
-          const uint4 x = *reinterpret_cast<const uint4*>(src);
-          bv[ku][0] = x.x;
-          bv[ku][1] = x.y;
-          bv[ku][2] = x.z;
-          bv[ku][3] = x.w;
-        } else {
-          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
-          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
-          bv[ku][0] = x0.x;
-          bv[ku][1] = x0.y;
-          bv[ku][2] = x1.x;
-          bv[ku][3] = x1.y;
-        }
-      }
-      const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
-#pragma unroll
-      for (int e = 0; e < NE; ++e) {
-        uint64_t acc[V] = {0, 0, 0, 0};
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku) {
-          T sv[V];
-          if constexpr (kSMode == kModeGlobal)
-            tile_load<T, T, V>(S, so + s_lo + S.e_off[e] + S.k_off[kc * KU + ku], sv);
-          else
-            stage_load<kSMode, T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
-#pragma unroll
-          for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
-          if constexpr (kRing == TSG_RING_MODP) {
-            if ((ku & 1) && leaves == 0) {
-#pragma unroll
-              for (int j = 0; j < V; ++j) {
-                part[e][j] = add_mod(part[e][j], mont_redc(acc[j], pc.p, pc.pinv), pc.p);
-                acc[j] = 0;
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < V; ++j) {
-          if constexpr (kRing == TSG_RING_U64) {
-            part[e][j] += acc[j];
-          } else {
-            if (leaves != 0) part[e][j] = add_mod(part[e][j], small_mod(acc[j], pc.p), pc.p);
-          }
-        }
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[s]);
-    }
-#pragma unroll
-    for (int e = 0; e < NE; ++e) {
-      const uint64_t oe = oo + a.o_e[e];
-      if constexpr (kRing == TSG_RING_U64) {
-        uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
-        reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(part[e][0], part[e][1]);
-        reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(part[e][2], part[e][3]);
-      } else {
-        *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
-            make_uint4(part[e][0], part[e][1], part[e][2], part[e][3]);
-      }
-    }
-    return true;
-  };
-  auto consume = [&](auto mode_c) {
-    constexpr int kSMode = decltype(mode_c)::value;  // kModeGlobal: not staged
-    // staged operands are intermediates, so only a global operand can be a leaf
-    const int leaves = kSMode == kModeGlobal ? S.leaf : 0;
-    uint64_t i = 0;  // stages consumed
-    for (uint64_t w = blockIdx.x; w < items; w += gridDim.x, ++i) {
-      if constexpr (KU == 4) {
-        if (sa.kchunks > 1) {  // the item spans kchunks stages
-          if (!consume_chunked(i, leaves, mode_c)) return;
-          --i;  // consume_chunked advanced i past the item's stages
-          continue;
-        }
-      }
-      const int s = (int)(i % nst);
-      if (__shfl_sync(0xffffffffu, (int)bail, 0)) return;
-      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
-        if (lane == 0) {
-          atomicExch(&g_device_error, TSG_ERR_TIMEOUT);
-          bail = 1;
-        }
-        return;
-      }
-      const uint64_t so = head[s].so;
-      const uint64_t oo = head[s].oo + o_lo;
-      const PlaneConst pc = plane_const(ring, head[s].p);
-      const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
-      T bv[KU][V];
-#pragma unroll
-      for (int ku = 0; ku < KU; ++ku) {
-        const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
-        if constexpr (sizeof(T) == 4) {
-          const uint4 x = *reinterpret_cast<const uint4*>(src);
-          bv[ku][0] = x.x;
-          bv[ku][1] = x.y;
-          bv[ku][2] = x.z;
-          bv[ku][3] = x.w;
-        } else {
-          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
-          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
-          bv[ku][0] = x0.x;
-          bv[ku][1] = x0.y;
-          bv[ku][2] = x1.x;
-          bv[ku][3] = x1.y;
-        }
-      }
-      const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
-#pragma unroll
-      for (int e = 0; e < NE; ++e) {
-        uint64_t acc[V] = {0, 0, 0, 0};  // U64: the sum; MODP: the current pair of products
-        uint32_t done[V] = {0, 0, 0, 0};  // MODP, 4 summed combinations: first pair, reduced
-#pragma unroll
-        for (int ku = 0; ku < KU; ++ku) {
-          T sv[V];
-          if constexpr (kSMode == kModeGlobal)
-            tile_load<T, T, V>(S, so + s_lo + S.e_off[e] + S.k_off[ku], sv);
-          else
-            stage_load<kSMode, T, V>(S, ss + (e * KU + ku) * sa.s_span, sv);
-#pragma unroll
-          for (int j = 0; j < V; ++j) acc[j] += (uint64_t)bv[ku][j] * (uint64_t)sv[j];
-          if constexpr (kRing == TSG_RING_MODP && KU > 2) {
-            // two Montgomery products stay below p 2^32: reduce each pair (with a leaf
-            // operand the four products are small and are reduced once at the end)
-            if (ku == 1 && leaves == 0) {
-#pragma unroll
-              for (int j = 0; j < V; ++j) {
-                done[j] = mont_redc(acc[j], pc.p, pc.pinv);
-                acc[j] = 0;
-              }
-            }
-          }
-        }
-        const uint64_t oe = oo + a.o_e[e];
-        if constexpr (kRing == TSG_RING_U64) {
-          uint64_t* out = reinterpret_cast<uint64_t*>(a.out) + oe;
-          reinterpret_cast<ulonglong2*>(out)[0] = make_ulonglong2(acc[0], acc[1]);
-          reinterpret_cast<ulonglong2*>(out)[1] = make_ulonglong2(acc[2], acc[3]);
-        } else {
-          uint32_t r[V];
-#pragma unroll
-          for (int j = 0; j < V; ++j) {
-            r[j] = kSMode == kModeGlobal ? mont_finish_c(acc[j], leaves, pc)
-                                         : mont_redc(acc[j], pc.p, pc.pinv);
-            if constexpr (KU > 2) r[j] = add_mod(done[j], r[j], pc.p);
-          }
-          *reinterpret_cast<uint4*>(reinterpret_cast<uint32_t*>(a.out) + oe) =
-              make_uint4(r[0], r[1], r[2], r[3]);
-        }
-      }
-      // release the stage: every lane of the warp is done reading it
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[s]);
-    }
-  };
-  if (!s_staged) consume(std::integral_constant<int, kModeGlobal>{});
-  else if (S.mode == kModeContig) consume(std::integral_constant<int, kModeContig>{});
-  else if (S.mode == kModeBcast) consume(std::integral_constant<int, kModeBcast>{});
-  else if (S.mode == kModePair) consume(std::integral_constant<int, kModePair>{});
-  else consume(std::integral_constant<int, kModeGather>{});
-}
-
-// Combines the root tensors of `cnt` slices (layout [plane][cnt][E]) into result[E]
-// (OR for OR_AND, sum mod 2^64 for U64, sum mod p per plane for MODP). One block per root
-// entry; threads stride over slices, then a shared-memory tree reduction.
-template <int kRing>
-__global__ void __launch_bounds__(kThreads)
-    root_reduce_kernel(const uint8_t* root, uint64_t cnt, uint64_t entries, uint64_t plane,
-                       uint8_t* result, int accumulate, RingArgs ring) {
-  __shared__ uint64_t red[kThreads];
-  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
-  for (uint64_t e = blockIdx.x; e < entries; e += gridDim.x) {
-    for (int p = 0; p < np; ++p) {
-      uint64_t part = 0;
-      for (uint64_t g = threadIdx.x; g < cnt; g += blockDim.x) {
-        const uint64_t idx = p * plane + g * entries + e;
-        if constexpr (kRing == TSG_RING_OR_AND) {
-          part |= root[idx];
-        } else if constexpr (kRing == TSG_RING_U64) {
-          part += reinterpret_cast<const uint64_t*>(root)[idx];
-        } else {
-          // residues < 2^31 summed over at most 2^32 slices per thread stay below 2^63
-          part += reinterpret_cast<const uint32_t*>(root)[idx];
-        }
-      }
-      if constexpr (kRing == TSG_RING_MODP) part = barrett_reduce(part, ring.p[p], ring.m[p]);
-      red[threadIdx.x] = part;
-      __syncthreads();
-      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if ((int)threadIdx.x < s) {
-          if constexpr (kRing == TSG_RING_OR_AND) {
-            red[threadIdx.x] |= red[threadIdx.x + s];
-          } else {
-            red[threadIdx.x] += red[threadIdx.x + s];  // MODP: each term < 2^31, 256 terms
-          }
-        }
-        __syncthreads();
-      }
-      if (threadIdx.x == 0) {
-        uint64_t v = red[0];
-        if constexpr (kRing == TSG_RING_OR_AND) {
-          if (accumulate) v |= result[e];
-          result[e] = v ? 1 : 0;
-        } else if constexpr (kRing == TSG_RING_U64) {
-          uint64_t* r = reinterpret_cast<uint64_t*>(result);
-          r[e] = accumulate ? r[e] + v : v;
-        } else {
-          // v < 256 p: reduce, then leave Montgomery form (REDC of x < p is x R^-1 mod p)
-          uint32_t* r = reinterpret_cast<uint32_t*>(result) + p * entries;
-          uint64_t plain = mont_redc(barrett_reduce(v, ring.p[p], ring.m[p]), ring.p[p],
-                                     ring.pinv[p]);
-          if (accumulate) plain += r[e];
-          r[e] = barrett_reduce(plain, ring.p[p], ring.m[p]);
-        }
-      }
-      __syncthreads();
-    }
-  }
+  *out = addr[dev];
+  return TSG_OK;
 }
 
 // ------------------------------------------------------------------------------------
@@ -1448,22 +394,6 @@ uint64_t scatter_pairs(const std::vector<std::pair<int, int>>& pairs, uint64_t x
   return r;
 }
 
-struct TileShape {
-  int v, ne, nk;      // template parameters (nk 0: runtime summed count)
-  unsigned threads;
-  uint64_t tiles;
-};
-
-struct LaunchArgs {
-  StepArgs a;       // general form (also used for the bounds check)
-  TileArgs t;       // tile form, valid when `tile`
-  TileShape shape;
-  StreamArgs stream;
-  bool tile;
-  bool streamed;    // run by the streaming (TMA-staged) kernel
-  bool is_leaf[2];
-  uint64_t cnt;     // slices of this launch
-};
 
 // Builds the tile form of step s from the operand descriptions; sets *ok = false when the
 // step is outside what the tile kernel handles (it then runs the general kernel).
@@ -1710,9 +640,6 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
 // as whole 1024-element tiles: its first 10 F bits are its own bits 0-9, every other
 // offset term is a multiple of 1024 elements (so each chunk is contiguous and 16-byte
 // aligned for TMA), and the tile kernel would use 256 threads x 4 positions.
-// Dynamic shared memory of one streaming block (its ring of stages): three blocks per SM.
-constexpr uint64_t kStreamBlockSmem = 72 * 1024;
-constexpr int kStreamBlocksPerSm = 3;
 
 // Bytes of one stage (one residue plane of one tile): the staged operand's tile per
 // summed combination and, with span > 0, the other operand's blocks.
@@ -1837,105 +764,26 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   return TSG_OK;
 }
 
-template <int kRing, int V, int NE, int NK>
-void launch_tile_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  dim3 grid((unsigned)la.shape.tiles, (unsigned)la.cnt);
-  tree_step_tile_kernel<kRing, V, NE, NK><<<grid, la.shape.threads, 0, st>>>(la.t, ra);
-}
-
-template <int kRing, int V, int NE>
-void launch_tile_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  switch (la.shape.nk) {
-    case 1: launch_tile_t<kRing, V, NE, 1>(la, ra, st); break;
-    case 2: launch_tile_t<kRing, V, NE, 2>(la, ra, st); break;
-    case 4:  // unrolled only for OR-AND (the count rings stream their large K = 2 steps)
-      if constexpr (kRing == TSG_RING_OR_AND) launch_tile_t<kRing, V, NE, 4>(la, ra, st);
-      else launch_tile_t<kRing, V, NE, 0>(la, ra, st);
-      break;
-    default: launch_tile_t<kRing, V, NE, 0>(la, ra, st); break;
-  }
-}
-
-template <int kRing, int V>
-void launch_tile_ne(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  switch (la.shape.ne) {
-    case 1: launch_tile_nk<kRing, V, 1>(la, ra, st); break;
-    case 2: launch_tile_nk<kRing, V, 2>(la, ra, st); break;
-    default: launch_tile_nk<kRing, V, 4>(la, ra, st); break;
-  }
-}
-
-template <int kRing>
-void launch_tile_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  if constexpr (kRing == TSG_RING_OR_AND) {
-    if (la.shape.v == 16) {
-      launch_tile_ne<kRing, 16>(la, ra, st);
-      return;
-    }
-  }
-  if (la.shape.v == 4) launch_tile_ne<kRing, 4>(la, ra, st);
-  else launch_tile_ne<kRing, 1>(la, ra, st);
-}
-
-template <int kRing, int NE, int NK>
-tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  auto kernel = tree_step_stream_kernel<kRing, NE, NK>;
-  const size_t smem = (size_t)la.stream.stages * la.stream.stage_bytes;
-  if (la.stream.stages < 2 || la.stream.stages > kStreamMaxStages || smem > kStreamBlockSmem)
-    return fail(TSG_ERR_INVALID_ARGUMENT, "stream kernel: stage ring outside its limits");
-  static bool configured[64] = {};  // one attribute call per instantiation and device
-  int dev = 0;
-  TSG_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return fail(TSG_ERR_UNSUPPORTED, "device ordinal outside 0..63");
-  if (!configured[dev]) {
-    TSG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)kStreamBlockSmem));
-    configured[dev] = true;
-  }
-  const int np = kRing == TSG_RING_MODP ? ra.np : 1;
-  const uint64_t blocks = std::min<uint64_t>(la.stream.work * np,
-                                             (uint64_t)device_sm_count() * kStreamBlocksPerSm);
-  kernel<<<(unsigned)blocks, kStreamThreads, smem, st>>>(la.t, ra, la.stream);
-  return TSG_OK;
-}
-
-template <int kRing, int NE>
-tsg_status launch_stream_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  switch (std::min(la.t.n_k, 4)) {
-    case 1: return launch_stream_t<kRing, NE, 1>(la, ra, st);
-    case 2: return launch_stream_t<kRing, NE, 2>(la, ra, st);
-    default: return launch_stream_t<kRing, NE, 4>(la, ra, st);
-  }
-}
-
-template <int kRing>
-tsg_status launch_stream_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  switch (la.shape.ne) {
-    case 1: return launch_stream_nk<kRing, 1>(la, ra, st);
-    case 2: return launch_stream_nk<kRing, 2>(la, ra, st);
-    default: return launch_stream_nk<kRing, 4>(la, ra, st);
-  }
-}
-
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   LaunchArgs la;
   TSG_TRY(build_step(c, s, base, cnt, &la));
   if (la.streamed) {
-    if (c.ring == TSG_RING_U64) TSG_TRY(launch_stream_ring<TSG_RING_U64>(la, c.ra, c.stream));
-    else TSG_TRY(launch_stream_ring<TSG_RING_MODP>(la, c.ra, c.stream));
+    TSG_TRY(device_error_address(&la.stream.error));
+    if (c.ring == TSG_RING_U64) TSG_TRY(launch_stream_u64(la, c.ra, c.stream));
+    else TSG_TRY(launch_stream_modp(la, c.ra, c.stream));
     TSG_CUDA_TRY(cudaGetLastError());
     return TSG_OK;
   }
   if (la.tile) {
     switch (c.ring) {
       case TSG_RING_OR_AND:
-        launch_tile_ring<TSG_RING_OR_AND>(la, c.ra, c.stream);
+        TSG_TRY(launch_tile_or_and(la, c.ra, c.stream));
         break;
       case TSG_RING_U64:
-        launch_tile_ring<TSG_RING_U64>(la, c.ra, c.stream);
+        TSG_TRY(launch_tile_u64(la, c.ra, c.stream));
         break;
       default:
-        launch_tile_ring<TSG_RING_MODP>(la, c.ra, c.stream);
+        TSG_TRY(launch_tile_modp(la, c.ra, c.stream));
         break;
     }
     TSG_CUDA_TRY(cudaGetLastError());
