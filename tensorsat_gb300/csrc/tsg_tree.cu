@@ -518,6 +518,10 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
         op.pair_sel = sel;
       }
     }
+    if (op.mode == kModeGather && v == 4 && !op.leaf && ring != TSG_RING_OR_AND &&
+        op.tab[0] == 0 && op.tab[1] == 1 && op.tab[2] != 0 && op.tab[3] == op.tab[2] + 1 &&
+        (op.tab[2] & 1) == 0 && (op.base & 1) == 0)
+      op.mode = kModeDual;  // alignment of the pairs is proven in check_tile_bounds
     if (op.mode == kModeGather && v == 16) {
       // carried fast F bits (F index, operand bit), ascending F index: distinct value d
       // has bit k of d = carried bit k of the position
@@ -618,6 +622,23 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
     for (int e = 0; e < sh.ne; ++e) ok = ok && (op.e_off[e] & vmask) == 0;
     for (int kk = 0; kk < t.n_k; ++kk) ok = ok && (op.k_off[kk] & vmask) == 0;
     if (!ok) return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: vector load not aligned");
+  }
+  // Two-element vector loads (kModeDual): every offset term but the first position bit
+  // must be even.
+  for (int o = 0; o < 2 && sh.v == 4; ++o) {
+    const TileOperand& op = t.op[o];
+    if (op.mode != kModeDual) continue;
+    auto map1 = [](const NarrowMap& m) {
+      for (int i = 0; i < m.n; ++i)
+        if (m.dst[i] < 1 && m.src[i] >= 1) return false;
+      return true;
+    };
+    bool ok = (op.base & 1) == 0 && (op.plane & 1) == 0 && (op.tab[2] & 1) == 0 &&
+              op.tab[1] == 1 && map1(op.f_hi) && map1(op.f_lo);
+    for (int i = 0; i < op.g.n; ++i) ok = ok && op.g.dst[i] >= 1;
+    for (int e = 0; e < sh.ne; ++e) ok = ok && (op.e_off[e] & 1) == 0;
+    for (int kk = 0; kk < t.n_k; ++kk) ok = ok && (op.k_off[kk] & 1) == 0;
+    if (!ok) return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: paired vector load not aligned");
   }
   if (t.o_contig && sh.v > 1) {
     bool ok = (t.n_out & vmask) == 0 && (la.a.o_plane & vmask) == 0 && map_ok(t.of_hi) &&

@@ -171,6 +171,9 @@ constexpr int kModePair = 3;  // two distinct offsets: 0 and tab[3]; pair_sel pi
 // 2^c distinct bytes (offsets dtab) are packed into two words and spread over the four
 // output words with byte permutes (selectors psel)
 constexpr int kModePerm = 4;
+// V = 4, count rings: positions at offsets {0, 1, d, d + 1} (two adjacent pairs), read as
+// two 2-element vector loads
+constexpr int kModeDual = 5;
 constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
 constexpr int kMaxK = 16;  // summed combinations kept in tables (k <= 4)
 
@@ -278,6 +281,22 @@ __device__ __forceinline__ void tile_load(const TileOperand& op, uint64_t off, V
     const VT x = (VT)p[off];
 #pragma unroll
     for (int j = 0; j < V; ++j) out[j] = x;
+  } else if (V == 4 && sizeof(T) >= 4 && op.mode == kModeDual) {
+    if constexpr (sizeof(T) == 4) {
+      const uint2 x0 = *reinterpret_cast<const uint2*>(p + off);
+      const uint2 x1 = *reinterpret_cast<const uint2*>(p + off + op.tab[2]);
+      out[0] = x0.x;
+      out[1 % V] = x0.y;
+      out[2 % V] = x1.x;
+      out[3 % V] = x1.y;
+    } else if constexpr (sizeof(T) == 8) {
+      const ulonglong2 x0 = *reinterpret_cast<const ulonglong2*>(p + off);
+      const ulonglong2 x1 = *reinterpret_cast<const ulonglong2*>(p + off + op.tab[2]);
+      out[0] = x0.x;
+      out[1 % V] = x0.y;
+      out[2 % V] = x1.x;
+      out[3 % V] = x1.y;
+    }
   } else if (V == 4 && op.mode == kModePair) {
     const VT x0 = (VT)p[off], x1 = (VT)p[off + op.tab[3]];
 #pragma unroll
