@@ -20,11 +20,14 @@ Restated functions (paths relative to the tensorsat project root):
   (the unclamped einsum of the #SAT prototype notebook,
   notebooks/prototypes/2025-02-13-#sat-tensor-contraction.ipynb cells 9-12)
 * :func:`brute_force_count` enumeration of all assignments (C, ``oracle/brute.c``)
+* :func:`dpll_count`       exact model counting by DPLL search with unit propagation (C,
+  ``oracle/dpll.c``), for instances beyond brute force
 
 Parity status: SAT bits are pinned against the reference's own known-answer tests and
 against outputs of the reference itself (fixtures in ``tests/golden``); per-step results
 are pinned against ``FinRel._contract2`` outputs; model counts are pinned by brute force
-(the reference has no counting API).
+and, beyond its reach, by the DPLL counter, itself checked against brute force (the
+reference has no counting API).
 """
 
 from __future__ import annotations
@@ -242,14 +245,17 @@ def tree_contract(arrays: Sequence[np.ndarray], leaf_wires: Sequence[Sequence[in
 
 
 def build_oracle(force: bool = False) -> Path:
-    """Compiles oracle/brute.c into oracle/_build/libts_oracle.so with gcc."""
-    src = ORACLE_DIR / "brute.c"
-    if BRUTE_LIB.exists() and not force and BRUTE_LIB.stat().st_mtime >= src.stat().st_mtime:
+    """Compiles oracle/brute.c and oracle/dpll.c into oracle/_build/libts_oracle.so with
+    gcc."""
+    srcs = [ORACLE_DIR / "brute.c", ORACLE_DIR / "dpll.c"]
+    if BRUTE_LIB.exists() and not force and \
+            BRUTE_LIB.stat().st_mtime >= max(src.stat().st_mtime for src in srcs):
         return BRUTE_LIB
     BUILD_DIR.mkdir(exist_ok=True)
     cc = os.environ.get("CC", "gcc")
     tmp = BRUTE_LIB.with_suffix(".so.tmp")
-    subprocess.run([cc, "-O2", "-shared", "-fPIC", "-o", str(tmp), str(src)], check=True)
+    subprocess.run([cc, "-O2", "-shared", "-fPIC", "-o", str(tmp)] + [str(x) for x in srcs],
+                   check=True)
     os.replace(tmp, BRUTE_LIB)
     return BRUTE_LIB
 
@@ -278,6 +284,44 @@ def brute_force_count(num_vars: int, clauses: Sequence[Sequence[int]]) -> int:
     if res < 0:
         raise ValueError("brute force supports at most 40 variables")
     return int(res)
+
+
+def _clause_arrays(clauses: Sequence[Sequence[int]]):
+    offsets = [0]
+    lits: list[int] = []
+    for c in clauses:
+        lits.extend(c)
+        offsets.append(len(lits))
+    return ((ctypes.c_int32 * len(offsets))(*offsets),
+            (ctypes.c_int32 * max(1, len(lits)))(*lits))
+
+
+def dpll_count(num_vars: int, clauses: Sequence[Sequence[int]],
+               node_limit: int = 50_000_000) -> tuple[int, int]:
+    """(number of assignments of variables 1..num_vars satisfying every clause, search
+    nodes visited), by DPLL search with unit propagation (C, ``oracle/dpll.c``), exact
+    below 2^128. Raises RuntimeError when the search exceeds ``node_limit`` or the count
+    reaches 2^128."""
+    lib = ctypes.CDLL(str(build_oracle()))
+    fn = lib.ts_oracle_dpll_count
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32),
+                   ctypes.POINTER(ctypes.c_int32), ctypes.c_uint64,
+                   ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                   ctypes.POINTER(ctypes.c_uint64)]
+    off, lt = _clause_arrays(clauses)
+    hi, lo, nodes = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+    st = fn(num_vars, len(clauses), off, lt, node_limit, ctypes.byref(hi), ctypes.byref(lo),
+            ctypes.byref(nodes))
+    if st == -1:
+        raise ValueError("bad DPLL arguments (variable count or literal out of range)")
+    if st == -2:
+        raise RuntimeError(f"DPLL search exceeded {node_limit} nodes")
+    if st == -4:
+        raise RuntimeError("model count is 2^128 or more")
+    if st != 0:
+        raise RuntimeError(f"DPLL counter failed with status {st}")
+    return (hi.value << 64) | lo.value, nodes.value
 
 
 # --------------------------------------------------------------------------------------

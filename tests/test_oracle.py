@@ -66,6 +66,43 @@ def test_brute_force_edge_cases():
     assert orc.brute_force_count(8, [(8,)]) == 128
 
 
+def test_dpll_counter_matches_brute_force():
+    cases = [(3, n, round(r * n), s) for n in (10, 14, 18, 22) for r in (1.5, 3.0, 4.3)
+             for s in range(3)]
+    cases += [(5, n, round(r * n), s) for n in (8, 14, 20, 24) for r in (5.0, 12.0, 21.0)
+              for s in range(2)]
+    cases += [(4, 16, 100, 0), (2, 20, 15, 1), (7, 22, 300, 0)]
+    for k, n, m, s in cases:
+        cnf = CNFInstance.random(k, n, m, rng=s)
+        assert orc.dpll_count(n, cnf.clauses)[0] == orc.brute_force_count(n, cnf.clauses), \
+            (k, n, m, s)
+
+
+def test_dpll_counter_edge_cases():
+    assert orc.dpll_count(0, [])[0] == 1
+    assert orc.dpll_count(3, [])[0] == 8
+    assert orc.dpll_count(100, [])[0] == 2**100  # beyond 64 bits
+    with pytest.raises(RuntimeError):
+        orc.dpll_count(128, [])
+    assert orc.dpll_count(1, [(1,), (-1,)])[0] == 0
+    assert orc.dpll_count(7, [(1, -1)])[0] == 128  # tautology
+    assert orc.dpll_count(8, [(8,)])[0] == 128
+    assert orc.dpll_count(4, [(2, 2, -3)])[0] == orc.brute_force_count(4, [(2, 2, -3)])
+    assert orc.dpll_count(4, [()])[0] == 0  # the empty clause
+    with pytest.raises(ValueError):
+        orc.dpll_count(3, [(4,)])
+    with pytest.raises(RuntimeError):
+        orc.dpll_count(40, CNFInstance.random(3, 40, 60, rng=0).clauses, node_limit=3)
+
+
+@pytest.mark.parametrize("case", _json("kissat.json"), ids=lambda c: c["test"])
+def test_dpll_counter_kissat_known_answers(case):
+    n, clauses = case["num_vars"], [tuple(c) for c in case["clauses"]]
+    count = orc.dpll_count(n, clauses)[0]
+    assert count == int(case["count"])
+    assert (count > 0) == case["expected"]
+
+
 def test_oracle_counts_are_tree_independent():
     cnf = CNFInstance.random(3, 16, 64, rng=3)
     exp = orc.brute_force_count(16, cnf.clauses)

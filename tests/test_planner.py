@@ -100,3 +100,72 @@ def test_slicing_never_touches_output_wires():
     d = cnf.clause_diagram("_" * 4 + "?" * 8)
     c = GpuContraction(CudaRel, d.wiring, target_bits=5, trials=1)
     assert not set(c.sliced_wires) & set(d.wiring.out_wires)
+
+
+def _primal_degeneracy(num_vars: int, clauses) -> int:
+    """Degeneracy of the primal graph (variables adjacent when they share a clause): the
+    largest minimum degree met while repeatedly deleting a minimum-degree vertex. It is a
+    lower bound on the graph's treewidth."""
+    adj = {v: set() for v in range(num_vars)}
+    for c in clauses:
+        vs = {abs(l) - 1 for l in c}
+        for v in vs:
+            adj[v] |= vs - {v}
+    deg = 0
+    while adj:
+        v = min(adj, key=lambda x: len(adj[x]))
+        deg = max(deg, len(adj[v]))
+        for u in adj.pop(v):
+            adj[u].discard(v)
+    return deg
+
+
+def test_5sat_n100_m2100_admits_no_tree_under_the_2_30_cap():
+    """Uniform random 5-SAT with n=100, m=2100, sliced over 8 wires, cannot keep every
+    intermediate at 2^30 entries or fewer, whatever the tree.
+
+    The wire sets of a tree's steps (both operands' wires together) are the bags of a tree
+    decomposition of the primal graph, so some step spans at least treewidth + 1 wires,
+    and one of its two operands carries at least half of them. Slicing 8 wires deletes 8
+    vertices, which lowers the treewidth by at most 8. The treewidth is at least the
+    degeneracy, 94 here, so some operand of every sliced tree has at least
+    ceil((94 - 8 + 1) / 2) = 44 > 30 wires."""
+    cnf = CNFInstance.random(5, 100, 2100, rng=0)
+    deg = _primal_degeneracy(100, cnf.clauses)
+    assert deg >= 94
+    assert -(-(deg - 8 + 1) // 2) > 30
+    d = cnf.clause_diagram()
+    net = planner.Network([tuple(ws) for ws in d.wiring.slot_wires_list],
+                          {w: 2 for w in range(d.wiring.num_wires)}, ())
+    tree, _ = planner.optimize(net, target_bits=None, trials=1, seed=0, reconf=0)
+    assert tree.cost(frozenset())[1] >= deg  # min-fill: 97 wires at the peak
+
+
+def test_5sat_largest_instance_under_the_cap_plans_to_256_slices():
+    """At clause ratio 21, n=39 (m=819) is where the planner's 5-SAT trees reach the 2^30
+    cap with 8 sliced wires (256 slices); every launch of that plan passes the host
+    bounds checks in every ring."""
+    from tensorsat_gb300 import _native
+    from tensorsat_gb300.contractions.gpu import PRIMES_31
+
+    cnf = CNFInstance.random(5, 39, 819, rng=0)
+    c = GpuContraction(CudaRel, cnf.clause_diagram().wiring, target_bits=30, trials=2)
+    assert c.num_slices == 256 and c.stats()["peak_bits"] == 30
+    npl = c.native_plan()
+    for ring, primes in [(_native.TSG_RING_OR_AND, ()), (_native.TSG_RING_U64, ()),
+                         (_native.TSG_RING_MODP, PRIMES_31[:3])]:
+        npl.validate(ring, primes, 0, c.num_slices, 2)
+    assert npl.workspace_bytes(_native.TSG_RING_MODP, 3, 2) < 80 * 2**30
+
+
+@pytest.mark.parametrize("n,m,seed,target", [(12, 200, 0, 6), (14, 294, 1, 6), (16, 336, 2, 8)])
+def test_emulated_5sat_sliced_plan_counts(n, m, seed, target):
+    cnf = CNFInstance.random(5, n, m, rng=seed)
+    exp = orc.brute_force_count(n, cnf.clauses)
+    d = cnf.clause_diagram()
+    c = GpuContraction(CudaRel, d.wiring, target_bits=target, trials=1, seed=seed)
+    assert c.num_slices > 1
+    arrs = c.sliced_plan.native_arrays()
+    leaves = _leaves(d, c)
+    assert int(emulate_all(arrs, leaves, "count")[0]) * c.discard_factor == exp
+    assert int(emulate_all(arrs, leaves, "or_and")[0]) == int(exp > 0)
