@@ -9,6 +9,12 @@ all kernels of all instances on one stream with one shared workspace. It neither
 allocates nor synchronises, so :meth:`BatchContraction.capture` records it into a CUDA
 graph, and each replay reruns the whole batch with a single launch from the host.
 
+Serving form: :meth:`BatchContraction.count` and :meth:`BatchContraction.contract` with
+``graph=True`` capture their run once and replay it on later calls, and
+:meth:`BatchContraction.load` copies the leaves of new diagrams with the same wirings into
+the captured leaf pools in place, so a stream of inputs pays one host-to-device copy, one
+graph launch and one read-back per batch.
+
 Results are the same as running each network through its own
 :class:`~tensorsat_gb300.contractions.gpu.GpuContraction`: SAT bits in the OR-AND
 semiring, exact model counts modulo 31-bit primes recombined by CRT.
@@ -69,6 +75,9 @@ class BatchContraction:
         for c, d in zip(self._contractions, self._diagrams):
             c.validate(d)
         self._pools: list[torch.Tensor] | None = None
+        self._graphs: dict[tuple, BatchGraph] = {}
+        self._staging: torch.Tensor | None = None    # pinned host copy of the leaf pools
+        self._staged: torch.cuda.Event | None = None  # the staging buffer's last copies
 
     @property
     def contractions(self) -> list[GpuContraction]:
@@ -85,6 +94,41 @@ class BatchContraction:
             self._pools = [c.leaf_pool(d, cache=False)
                            for c, d in zip(self._contractions, self._diagrams)]
         return self._pools
+
+    def load(self, diagrams: Sequence[Diagram] | None = None) -> int:
+        """Copies the leaves of ``diagrams`` (the batch's wirings, in order; default: the
+        batch's own diagrams) into the batch's device leaf pools in place and returns the
+        bytes copied. Later runs, and replays of graphs captured from this batch, contract
+        the new leaves. Host leaves go through one pinned staging buffer (one asynchronous
+        copy per instance on the current stream); device leaves are copied on the device.
+        """
+        if diagrams is not None:
+            diagrams = list(diagrams)
+            if len(diagrams) != len(self):
+                raise ValueError(f"expected {len(self)} diagrams, got {len(diagrams)}")
+            for c, d in zip(self._contractions, diagrams):
+                c.validate(d)
+            self._diagrams = diagrams
+        if self._pools is None:
+            return sum(p.numel() for p in self.pools())
+        parts = [c._host_pool(d) for c, d in zip(self._contractions, self._diagrams)]
+        total = sum(host.size for host, _ in parts)
+        if self._staged is not None:
+            self._staged.synchronize()  # the previous copies have read the staging buffer
+        if self._staging is None or self._staging.numel() < total:
+            self._staging = torch.empty(max(1, total), dtype=torch.uint8, pin_memory=True)
+        stage = self._staging.numpy()
+        off = 0
+        for c, pool, (host, device_leaves) in zip(self._contractions, self._pools, parts):
+            if pool.numel() != host.size:
+                raise RuntimeError("leaf pool size changed")
+            stage[off: off + host.size] = host
+            pool.copy_(self._staging[off: off + host.size], non_blocking=True)
+            c._finish_pool(pool, device_leaves)
+            off += host.size
+        self._staged = torch.cuda.Event()
+        self._staged.record()
+        return total
 
     def groups(self, ring: int, planes: int, budget_bytes: int | None = None) -> list[int]:
         """Slice group per instance: the largest power of two whose workspace fits the
@@ -178,12 +222,32 @@ class BatchContraction:
         return BatchGraph(graph, results, list(groups), launches,
                           [ws, self.pools(), args, list(primes)])
 
+    def _replay(self, ring: int, primes: Sequence[int], groups: Sequence[int] | None,
+                workspace: torch.Tensor | None) -> list[torch.Tensor]:
+        """Replays this batch's cached graph for (ring, primes, groups), capturing it on
+        first use (with ``workspace``, which the graph keeps); returns its result buffers,
+        which the next replay overwrites."""
+        key = (ring, tuple(primes), None if groups is None else tuple(groups))
+        g = self._graphs.get(key)
+        if g is None:
+            g = self.capture(ring, primes, groups, workspace)
+            self._graphs[key] = g
+        res = g.replay()
+        GpuContraction.check_device()
+        return res
+
     # -- answers ----------------------------------------------------------------------
 
-    def contract(self, groups: Sequence[int] | None = None) -> list[CudaRel]:
+    def contract(self, groups: Sequence[int] | None = None, *, graph: bool = False,
+                 workspace: torch.Tensor | None = None) -> list[CudaRel]:
         """OR-AND contraction of every diagram: one result box per diagram (a scalar box
-        for a SAT network: ``bool(box)`` is its SAT bit)."""
-        res = self.run(_native.TSG_RING_OR_AND, groups=groups)
+        for a SAT network: ``bool(box)`` is its SAT bit). ``graph=True`` replays a graph
+        captured on the first such call (see :meth:`load` for new inputs)."""
+        if graph:
+            res = [r.clone() for r in self._replay(_native.TSG_RING_OR_AND, (), groups,
+                                                   workspace)]
+        else:
+            res = self.run(_native.TSG_RING_OR_AND, groups=groups, workspace=workspace)
         return [c._box_from_root(r) for c, r in zip(self._contractions, res)]
 
     def count_bounds(self) -> list[float]:
@@ -208,11 +272,13 @@ class BatchContraction:
         return n
 
     def count(self, num_primes: int | None = None,
-              groups: Sequence[int] | None = None) -> list[Any]:
+              groups: Sequence[int] | None = None, *, graph: bool = False,
+              workspace: torch.Tensor | None = None) -> list[Any]:
         """Exact model count of every diagram (``int`` for closed networks, a numpy object
         array over the out wires otherwise), from one batched run modulo ``num_primes``
         31-bit primes (default: as many as the largest count bound of the batch needs, at
-        most 4 per run)."""
+        most 4 per run). ``graph=True`` replays a graph captured on the first such call
+        (see :meth:`load` for new inputs)."""
         need = self.primes_needed()
         if num_primes is None:
             num_primes = need
@@ -223,7 +289,10 @@ class BatchContraction:
                 f"the batch needs {num_primes} primes; one batched run carries at most "
                 f"{_native.TSG_MAX_PRIMES} (count such networks with GpuContraction.count)")
         primes = PRIMES_31[:num_primes]
-        res = self.run(_native.TSG_RING_MODP, primes, groups=groups)
+        if graph:
+            res = self._replay(_native.TSG_RING_MODP, primes, groups, workspace)
+        else:
+            res = self.run(_native.TSG_RING_MODP, primes, groups=groups, workspace=workspace)
         out = []
         for c, r in zip(self._contractions, res):
             planes = r.cpu().numpy().view(np.uint32).reshape(num_primes, -1)

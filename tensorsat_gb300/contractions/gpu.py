@@ -376,6 +376,17 @@ class GpuContraction(Contraction):
         if cache and self._pool_cache is not None and self._pool_cache[0] == id(diagram):
             return self._pool_cache[1]
         dev = _device.require_cuda()
+        host, device_leaves = self._host_pool(diagram)
+        pool = torch.from_numpy(host).to(dev, non_blocking=False)
+        self._finish_pool(pool, device_leaves)
+        if cache:
+            self._pool_cache = (id(diagram), pool)
+        return pool
+
+    def _host_pool(self, diagram: Diagram) -> tuple[np.ndarray, list[tuple[int, Any]]]:
+        """The host part of the leaf pool (host leaves and synthetic leaves at their
+        offsets, zeros elsewhere) and the leaves that :meth:`_finish_pool` writes on the
+        device (device-resident boxes and slots with repeated wires)."""
         npl = self.native_plan()
         lw = self._leaves
         host = np.zeros(npl.pool_bytes, dtype=np.uint8)
@@ -394,7 +405,14 @@ class GpuContraction(Contraction):
             arr = (box._tensor.numpy() if isinstance(box, CudaRel) else leaf_array(box))
             arr = arr.reshape(-1)
             host[off: off + arr.size] = arr
-        pool = torch.from_numpy(host).to(dev, non_blocking=False)
+        return host, device_leaves
+
+    def _finish_pool(self, pool: torch.Tensor, device_leaves: list[tuple[int, Any]]) -> None:
+        """Writes the device leaves of :meth:`_host_pool` into a device pool that already
+        holds the host part (on the current stream)."""
+        dev = _device.require_cuda()
+        npl = self.native_plan()
+        lw = self._leaves
         stream = _device.stream_handle()
         for l, box in device_leaves:
             off = int(npl.leaf_offsets[l])
@@ -412,9 +430,6 @@ class GpuContraction(Contraction):
                 _native.check(st)
             else:
                 pool[off: off + t.numel()].copy_(t.reshape(-1))
-        if cache:
-            self._pool_cache = (id(diagram), pool)
-        return pool
 
     # -- execution --------------------------------------------------------------------
 

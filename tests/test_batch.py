@@ -108,3 +108,27 @@ def test_batch_graph_replay_matches_uncaptured_run(cuda):
         for a, b in zip(gs.results, sat_direct):
             assert torch.equal(a, b)
     GpuContraction.check_device()
+
+
+@pytest.mark.gpu
+def test_batch_serving_graphs_follow_loaded_leaves(cuda):
+    """count/contract with graph=True capture one graph per ring on first use and replay
+    it afterwards; load() copies the leaves of new diagrams with the same wirings into the
+    captured pools. Here the inputs fix variable 1 to 1, then to 0, then to 1 again (a unit
+    slot whose box changes while the wiring stays), and every replay must answer for the
+    leaves loaded last."""
+    instances = ragged_instances(6, 12, 18, seed=4)
+    one = [cnf.clause_diagram("1" + "?" * (cnf.num_vars - 1)) for cnf in instances]
+    zero = [cnf.clause_diagram("0" + "?" * (cnf.num_vars - 1)) for cnf in instances]
+    exp1 = [orc.brute_force_count(c.num_vars, list(c.clauses) + [(1,)]) for c in instances]
+    exp0 = [orc.brute_force_count(c.num_vars, list(c.clauses) + [(-1,)]) for c in instances]
+    assert exp1 != exp0
+    batch = BatchContraction(CudaRel, one, target_bits=8, trials=1)
+    assert any(c.num_slices > 1 for c in batch.contractions)
+    for diagrams, exp in ((one, exp1), (zero, exp0), (one, exp1)):
+        assert batch.load(diagrams) > 0
+        assert batch.count(num_primes=3, graph=True) == exp
+        assert [bool(b) for b in batch.contract(graph=True)] == [e > 0 for e in exp]
+    assert len(batch._graphs) == 2  # one capture per ring, replayed ever since
+    with pytest.raises(ValueError):
+        batch.load(one[:-1])
