@@ -421,7 +421,24 @@ def ragged_instances(count: int, n_lo: int, n_hi: int):
     return out
 
 
+def _plan_instance(args):
+    num_vars, clauses = args
+    from tensorsat_gb300.contractions.gpu import plan_tree
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    return plan_tree(CNFInstance(num_vars, clauses).clause_diagram().wiring,
+                     target_bits=TARGET_BITS, trials=1)
+
+
 def run_ragged(args) -> None:
+    lo, hi = args.n_range
+    instances = ragged_instances(args.instances, lo, hi)
+    # planning is host work (about 0.4 s per instance here): spread it over the host cores
+    # in spawned processes, before this process touches CUDA
+    with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
+        trees = pool.map(_plan_instance, [(c.num_vars, c.clauses) for c in instances],
+                         chunksize=4)
+
     import torch
 
     from tensorsat_gb300 import _native
@@ -431,12 +448,10 @@ def run_ragged(args) -> None:
 
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
-    lo, hi = args.n_range
-    instances = ragged_instances(args.instances, lo, hi)
     diagrams = [cnf.clause_diagram() for cnf in instances]
     primes = PRIMES_31[:NUM_PRIMES]
-    chunks = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK], target_bits=TARGET_BITS,
-                               trials=1)
+    chunks = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK],
+                               trees=trees[i: i + RAGGED_CHUNK])
               for i in range(0, len(diagrams), RAGGED_CHUNK)]
     # one workspace for every graph (they replay in order on one stream); slice groups
     # sized to a fixed budget
@@ -471,8 +486,8 @@ def run_ragged(args) -> None:
 
     # plain form: one instance per call through the public API (count + SAT bit)
     sample = min(len(diagrams), 64)
-    plain = [GpuContraction(CudaRel, d.wiring, target_bits=TARGET_BITS, trials=1)
-             for d in diagrams[:sample]]
+    plain = [GpuContraction(CudaRel, d.wiring, tree=t[0], sliced=t[1])
+             for d, t in zip(diagrams[:sample], trees)]
     for c, d in zip(plain[:4], diagrams[:4]):
         c.count(d, ring="modp", num_primes=NUM_PRIMES)
         bool(c.contract(d))
@@ -484,15 +499,13 @@ def run_ragged(args) -> None:
     torch.cuda.synchronize()
     plain_value = sample / (time.perf_counter() - t0)
 
-    # end to end, batched, uncaptured: host diagrams in (leaf upload), one tsg_batch_run
+    # end to end, batched, uncaptured: host leaves in (uploaded again), one tsg_batch_run
     # per chunk and ring, counts and bits out
-    fresh = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK], target_bits=TARGET_BITS,
-                              trials=1)
-             for i in range(0, len(diagrams), RAGGED_CHUNK)]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     answers = []
-    for b in fresh:
+    for b, i in zip(chunks, range(0, len(diagrams), RAGGED_CHUNK)):
+        b.load(diagrams[i: i + RAGGED_CHUNK])
         answers.append((b.count(num_primes=NUM_PRIMES), [bool(x) for x in b.contract()]))
     torch.cuda.synchronize()
     uncaptured_value = len(diagrams) / (time.perf_counter() - t0)
@@ -500,9 +513,7 @@ def run_ragged(args) -> None:
     # end to end, serving form: every chunk captures one graph per ring on its first call
     # (set-up, like planning); each timed pass copies every instance's host leaves into the
     # captured pools (pinned staging), replays the graphs and reads counts and bits back
-    serve = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK], target_bits=TARGET_BITS,
-                              trials=1)
-             for i in range(0, len(diagrams), RAGGED_CHUNK)]
+    serve = chunks
     serve_groups = []
     for b in serve:
         gm = b.groups(_native.TSG_RING_MODP, NUM_PRIMES, budget)

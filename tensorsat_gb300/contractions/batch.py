@@ -65,13 +65,23 @@ class BatchContraction:
     model count per diagram."""
 
     def __init__(self, box_class: type[CudaRel], diagrams: Sequence[Diagram], *,
-                 target_bits: int | None = 26, trials: int = 2, seed: int = 0) -> None:
+                 target_bits: int | None = 26, trials: int = 2, seed: int = 0,
+                 trees: Sequence[tuple[Any, Sequence[int]]] | None = None) -> None:
+        """``trees`` optionally gives each diagram's (tree, sliced wires), for example from
+        :func:`~tensorsat_gb300.contractions.gpu.plan_tree` run in worker processes;
+        otherwise every diagram is planned here with ``target_bits``, ``trials`` and
+        ``seed``."""
         if not diagrams:
             raise ValueError("A batch needs at least one diagram.")
         self._diagrams = list(diagrams)
-        self._contractions = [GpuContraction(box_class, d.wiring, target_bits=target_bits,
-                                             trials=trials, seed=seed)
-                              for d in self._diagrams]
+        if trees is not None and len(trees) != len(self._diagrams):
+            raise ValueError(f"expected {len(self._diagrams)} trees, got {len(trees)}")
+        self._contractions = [
+            GpuContraction(box_class, d.wiring, target_bits=target_bits, trials=trials,
+                           seed=seed)
+            if trees is None else
+            GpuContraction(box_class, d.wiring, tree=trees[i][0], sliced=trees[i][1])
+            for i, d in enumerate(self._diagrams)]
         for c, d in zip(self._contractions, self._diagrams):
             c.validate(d)
         self._pools: list[torch.Tensor] | None = None

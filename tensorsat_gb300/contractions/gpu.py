@@ -113,6 +113,29 @@ def _prepare(wiring: Wiring) -> _Leaves:
                    tuple(dict.fromkeys(wiring.out_wires)), dims)
 
 
+def _network(lw: _Leaves) -> planner.Network:
+    """The bit network the planner sees (one tensor per prepared leaf)."""
+    if any(d != 2 for w, d in lw.wire_dims.items()
+           if any(w in ws for ws in lw.leaf_wires) or w in lw.out_unique):
+        raise NotImplementedError(
+            "GpuContraction executes bit networks: every connected wire must have"
+            " dimension 2"
+        )
+    return planner.Network(lw.leaf_wires, {w: 2 for ws in lw.leaf_wires for w in ws},
+                           lw.out_unique)
+
+
+def plan_tree(wiring: Wiring, target_bits: int | None = 26, trials: int = 8,
+              seed: int = 0) -> tuple[planner.ContractionTree, tuple[int, ...]]:
+    """The (tree, sliced wires) that ``GpuContraction(box_class, wiring,
+    target_bits=..., trials=..., seed=...)`` plans (``target_bits=None``: no slicing),
+    computed without building the contraction (host only, so planning can run in worker
+    processes and the result can be passed back as ``tree=`` / ``sliced=``)."""
+    tree, sl = planner.optimize(_network(_prepare(wiring)), target_bits=target_bits,
+                                trials=trials, seed=seed)
+    return tree, tuple(sorted(sl))
+
+
 def _functional_ports(t: np.ndarray) -> list[int]:
     """Ports whose value is a function of the other ports (exactly one 1 per assignment of
     the others), last port first (gates put their output last)."""
@@ -303,14 +326,7 @@ class GpuContraction(Contraction):
         self._optimize = optimize
         self._leaves = _prepare(wiring)
         lw = self._leaves
-        if any(d != 2 for w, d in lw.wire_dims.items()
-               if any(w in ws for ws in lw.leaf_wires) or w in lw.out_unique):
-            raise NotImplementedError(
-                "GpuContraction executes bit networks: every connected wire must have"
-                " dimension 2"
-            )
-        net = planner.Network(lw.leaf_wires, {w: 2 for ws in lw.leaf_wires for w in ws},
-                              lw.out_unique)
+        net = _network(lw)
         self._network = net
         if tree is None:
             tree, sl = planner.optimize(net, target_bits=target_bits, trials=trials, seed=seed)

@@ -19,7 +19,7 @@ import torch
 from oracle import finrel_oracle as orc
 from tensorsat_gb300 import _native
 from tensorsat_gb300.contractions.batch import BatchContraction
-from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction, plan_tree
 from tensorsat_gb300.lang.cuda_rel import CudaRel
 from tensorsat_gb300.lib.sat import CNFInstance
 
@@ -69,6 +69,21 @@ def test_batch_rejects_a_bad_instance_before_launching():
     assert "instance 2" in lib.tsg_last_error().decode()
     assert lib.tsg_batch_run(-1, None, 0, 0, None, None, None, None, 0, None, None) \
         == _native.TSG_ERR_INVALID_ARGUMENT
+
+
+def test_batch_accepts_trees_planned_elsewhere():
+    """plan_tree gives the tree GpuContraction would plan, so trees planned in worker
+    processes can be handed to a batch."""
+    instances = ragged_instances(4, 10, 16, seed=5)
+    diagrams = [cnf.clause_diagram() for cnf in instances]
+    trees = [plan_tree(d.wiring, target_bits=6, trials=1) for d in diagrams]
+    planned = BatchContraction(CudaRel, diagrams, target_bits=6, trials=1)
+    given = BatchContraction(CudaRel, diagrams, trees=trees)
+    for a, b in zip(planned.contractions, given.contractions):
+        assert a.tree.steps == b.tree.steps and a.sliced_wires == b.sliced_wires
+    assert plan_tree(diagrams[0].wiring, target_bits=None, trials=1)[1] == ()
+    with pytest.raises(ValueError):
+        BatchContraction(CudaRel, diagrams, trees=trees[:-1])
 
 
 @pytest.mark.gpu
