@@ -205,6 +205,27 @@ TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t
                              const uint32_t* primes, int64_t slice_begin,
                              int64_t slice_end, int64_t group_size);
 
+/* ---------------------------------------------------------------------------------
+ * Planner (host only; touches no device and needs no GPU).
+ *
+ * The dynamic program of subtree reconfiguration over the n (1..20) inputs of one cut
+ * subtree: the cheapest binary contraction of the inputs, where the partial result of an
+ * input subset m keeps the wires of m that the subtree's root keeps or an input outside
+ * m carries, and a step costs 2^(live wires of its two operands together). Wire sets are
+ * bitsets of `words` (1..64) 64-bit words: bits[i * words ...] the wires of input i,
+ * keep[] the root's wires, live[] the unsliced wires. With max_bits >= 0 a partial result
+ * (other than the whole subtree) with more than max_bits live wires is infeasible.
+ * Outputs: *best_full the cheapest total cost (INFINITY when infeasible); split[m]
+ * (2^n entries) the operand of m's cheapest split that holds m's lowest input;
+ * kept[m * words ...] (2^n * words words) the wires m's partial result keeps. Splits are
+ * visited in a fixed order and only a strictly cheaper one replaces the best, so results
+ * are deterministic. Stands in for the tree search of cotengra's hyper-optimiser
+ * (ctg.array_contract_tree), which the reference calls at
+ * tensorsat/contractions/cotengra.py:78-85; cotengra itself is not part of this build. */
+TSG_API tsg_status tsg_plan_subset_dp(int32_t n, int32_t words, const uint64_t* bits,
+                              const uint64_t* keep, const uint64_t* live, int32_t max_bits,
+                              double* best_full, uint32_t* split, uint64_t* kept);
+
 /* Synchronizes `stream` and reports whether any kernel of this library recorded a device-
  * side failure since the last call (a bounded wait that gave up: TSG_ERR_TIMEOUT); the
  * record is cleared. Runs launched before the failure are invalid. */

@@ -50,6 +50,7 @@ EXPORTED_SYMBOLS = (
     "tsg_take_device_error",
     "tsg_static_scratch_bytes",
     "tsg_plan_run_static",
+    "tsg_plan_subset_dp",
 )
 
 
@@ -130,6 +131,10 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_validate.restype = c_int32
     lib.tsg_plan_validate.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_int64,
                                       c_int64, c_int64]
+    u64p = POINTER(ctypes.c_uint64)
+    lib.tsg_plan_subset_dp.restype = c_int32
+    lib.tsg_plan_subset_dp.argtypes = [c_int32, c_int32, u64p, u64p, u64p, c_int32,
+                                       POINTER(ctypes.c_double), POINTER(c_uint32), u64p]
 
 
 def library_path() -> str:

@@ -22,12 +22,15 @@ Answers never depend on the tree; trees only change cost.
 
 from __future__ import annotations
 
+import ctypes
 import math
 import random
 from dataclasses import dataclass, field
 from typing import Sequence
 
 import numpy as np
+
+from . import _native
 
 TSG_MAX_BITS = 62
 
@@ -290,6 +293,37 @@ def minfill_order(net: Network, rng: random.Random, prefix: Sequence[int] = ()) 
     return order
 
 
+def subset_dp(n: int, num_wires: int, bits: Sequence[int], keep: int, live: int,
+              max_bits: int | None) -> tuple[float, np.ndarray, np.ndarray]:
+    """Cheapest binary contraction of ``n`` inputs by dynamic programming over their
+    subsets (native ``tsg_plan_subset_dp``). Wire sets are Python ints over
+    ``num_wires`` bit positions: ``bits[i]`` the wires of input i, ``keep`` the wires the
+    result keeps, ``live`` the unsliced ones. Returns (total cost, split, kept): the cost
+    is the sum over steps of 2^(live wires of both operands), ``split[m]`` the part of
+    subset m holding its lowest input in m's cheapest split, ``kept[m]`` (uint64 words)
+    the wires m's partial result keeps (those of m that ``keep`` or an input outside m
+    carries). With ``max_bits`` no partial result but the whole may keep more than
+    ``max_bits`` live wires (cost infinity when that cannot be met)."""
+    words = max(1, (num_wires + 63) // 64)
+    mask = (1 << 64) - 1
+
+    def to_words(v: int) -> list[int]:
+        return [(v >> (64 * w)) & mask for w in range(words)]
+
+    b = np.array([to_words(v) for v in bits], dtype=np.uint64).reshape(-1)
+    k = np.array(to_words(keep), dtype=np.uint64)
+    lv = np.array(to_words(live), dtype=np.uint64)
+    split = np.zeros(1 << n, dtype=np.uint32)
+    kept = np.zeros((1 << n) * words, dtype=np.uint64)
+    best = ctypes.c_double()
+    u64p = ctypes.POINTER(ctypes.c_uint64)
+    _native.check(_native.lib().tsg_plan_subset_dp(
+        n, words, b.ctypes.data_as(u64p), k.ctypes.data_as(u64p), lv.ctypes.data_as(u64p),
+        -1 if max_bits is None else int(max_bits), ctypes.byref(best),
+        split.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), kept.ctypes.data_as(u64p)))
+    return best.value, split, kept.reshape(1 << n, words)
+
+
 def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
                 sliced: frozenset[int] = frozenset(), max_bits: int | None = None
                 ) -> ContractionTree:
@@ -347,36 +381,8 @@ def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
             keep_x = sum(1 << index[w] for w in wires[x] if w in index)
             live = sum(1 << i for w, i in index.items() if w not in sliced)
             full = (1 << n) - 1
-            union = [0] * (full + 1)
-            for m in range(1, full + 1):
-                low = m & -m
-                union[m] = union[m ^ low] | bits[low.bit_length() - 1]
-            kept = [union[m] & (keep_x | union[full ^ m]) for m in range(full + 1)]
-            inf = float("inf")
-            best = [0.0] * (full + 1)
-            split = [0] * (full + 1)
-            for m in range(1, full + 1):
-                if m & (m - 1) == 0:
-                    continue
-                if m != full and max_bits is not None and (kept[m] & live).bit_count() > max_bits:
-                    best[m] = inf  # intermediate above the cap
-                    continue
-                low = m & -m
-                rest = m ^ low
-                top = inf
-                sub = rest
-                while True:  # A = low | sub (contains the lowest input), B = the rest
-                    a = low | sub
-                    b = m ^ a
-                    if b:
-                        c = best[a] + best[b] + 2.0 ** ((kept[a] | kept[b]) & live).bit_count()
-                        if c < top:
-                            top, split[m] = c, a
-                    if sub == 0:
-                        break
-                    sub = (sub - 1) & rest
-                best[m] = top
-            if not best[full] < old * (1 - 1e-9):
+            best_full, split, kept = subset_dp(n, len(index), bits, keep_x, live, max_bits)
+            if not best_full < old * (1 - 1e-9):
                 continue
             # rebuild the subtree below x from the splits; x keeps its id and wires
             for y in internal:
@@ -388,7 +394,7 @@ def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
                 nonlocal next_id
                 if m & (m - 1) == 0:
                     return frontier[m.bit_length() - 1]
-                a = split[m]
+                a = int(split[m])
                 na, nb = build(a), build(m ^ a)
                 if m == full:
                     y = x
@@ -396,7 +402,7 @@ def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
                     y = next_id
                     next_id += 1
                     inv = {v: k for k, v in index.items()}
-                    km = kept[m]
+                    km = sum(int(k) << (64 * w) for w, k in enumerate(kept[m]))
                     wires[y] = frozenset(inv[i] for i in range(km.bit_length()) if km >> i & 1)
                 children[y] = (na, nb)
                 return y

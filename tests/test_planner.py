@@ -169,3 +169,56 @@ def test_emulated_5sat_sliced_plan_counts(n, m, seed, target):
     leaves = _leaves(d, c)
     assert int(emulate_all(arrs, leaves, "count")[0]) * c.discard_factor == exp
     assert int(emulate_all(arrs, leaves, "or_and")[0]) == int(exp > 0)
+
+
+def test_native_subset_dp_equals_python_restatement():
+    """tsg_plan_subset_dp against the pure-Python dynamic program: random subtrees with
+    1-3 words of wires, with and without a cap, must give the same cost, splits and kept
+    wires (bit for bit)."""
+    import random
+
+    from plan_dp_reference import subset_dp_reference
+
+    rng = random.Random(0)
+    for trial in range(60):
+        n = rng.randint(1, 9)
+        nw = rng.choice([5, 20, 63, 64, 65, 130])
+        bits = [sum(1 << w for w in rng.sample(range(nw), rng.randint(0, min(nw, 12))))
+                for _ in range(n)]
+        keep = sum(1 << w for w in range(nw) if rng.random() < 0.2)
+        live = sum(1 << w for w in range(nw) if rng.random() < 0.9)
+        max_bits = rng.choice([None, 4, 8, 12])
+        got_best, got_split, got_kept = planner.subset_dp(n, nw, bits, keep, live, max_bits)
+        best, split, kept = subset_dp_reference(n, bits, keep, live, max_bits)
+        assert got_best == best, trial
+        assert [int(x) for x in got_split] == split, trial
+        words = got_kept.shape[1]
+        assert [sum(int(k) << (64 * w) for w, k in enumerate(row)) for row in got_kept] == kept
+        assert words == max(1, (nw + 63) // 64)
+
+
+@pytest.mark.parametrize("k,n,m,seed,target,trials", [(3, 30, 128, 0, 14, 2), (3, 36, 150, 3, 16, 2),
+                                                     (5, 20, 420, 0, 12, 1),
+                                                     (3, 60, 256, 0, 26, 2)])
+def test_plans_with_native_dp_equal_python_dp_plans(monkeypatch, k, n, m, seed, target, trials):
+    """Whole plans (reconfiguration before and after slicing) are the same trees and
+    sliced wires whichever implementation of the subset DP runs."""
+    from plan_dp_reference import subset_dp_reference
+
+    cnf = CNFInstance.random(k, n, m, rng=seed)
+    d = cnf.clause_diagram()
+    net = planner.Network([tuple(ws) for ws in d.wiring.slot_wires_list],
+                          {w: 2 for w in range(d.wiring.num_wires)}, ())
+    native = planner.optimize(net, target_bits=target, trials=trials, seed=seed)
+
+    def python_dp(n_, num_wires, bits, keep, live, max_bits):
+        best, split, kept = subset_dp_reference(n_, bits, keep, live, max_bits)
+        words = [[(v >> (64 * w)) & (2**64 - 1) for w in range(max(1, -(-v.bit_length() // 64)))]
+                 for v in kept]
+        return best, np.array(split, dtype=np.uint64), words
+
+    monkeypatch.setattr(planner, "subset_dp", python_dp)
+    reference = planner.optimize(net, target_bits=target, trials=trials, seed=seed)
+    assert native[0].steps == reference[0].steps
+    assert native[0].node_wires == reference[0].node_wires
+    assert native[1] == reference[1]
