@@ -433,7 +433,7 @@ def _plan_instance(args):
 def run_ragged(args) -> None:
     lo, hi = args.n_range
     instances = ragged_instances(args.instances, lo, hi)
-    # planning is host work (about 0.4 s per instance here): spread it over the host cores
+    # planning is host work (tens of milliseconds per instance): spread it over the host cores
     # in spawned processes, before this process touches CUDA
     with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
         trees = pool.map(_plan_instance, [(c.num_vars, c.clauses) for c in instances],
