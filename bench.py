@@ -58,6 +58,9 @@ def parse_args():
                         "random instances of uneven sizes (batched runs, CUDA graphs)")
     p.add_argument("--instances", type=int, default=512, help="ragged: batch size")
     p.add_argument("--n-range", type=int, nargs=2, default=[30, 40], help="ragged: n bounds")
+    p.add_argument("--plan-only", action="store_true",
+                   help="ragged: plan the batch on the host cores and print its algorithmic "
+                        "bytes per n (no GPU, no timing of contractions)")
     return p.parse_args()
 
 
@@ -430,14 +433,51 @@ def _plan_instance(args):
                      target_bits=TARGET_BITS, trials=1)
 
 
+def ragged_plan_report(args, instances, trees, plan_s: float) -> None:
+    """Algorithmic bytes of every planned instance (3-prime count + OR-AND bit, both
+    operands read once and the result written once per step), summarised per n."""
+    from tensorsat_gb300.contractions.gpu import GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+
+    by_n: dict[int, list[float]] = {}
+    peak = 0
+    for cnf, (tree, sliced) in zip(instances, trees):
+        c = GpuContraction(CudaRel, cnf.clause_diagram().wiring, tree=tree, sliced=sliced)
+        p = c.sliced_plan
+        total = (p.bytes_per_slice(4, NUM_PRIMES) + p.bytes_per_slice(1, 1)) * c.num_slices
+        by_n.setdefault(cnf.num_vars, []).append(total)
+        peak = max(peak, c.stats()["peak_bits"])
+    everything = sorted(b for bs in by_n.values() for b in bs)
+    lo, hi = args.n_range
+    buckets = {}
+    for a in range(lo, hi + 1, 10):
+        bs = sorted(b for n, v in by_n.items() if a <= n < a + 10 for b in v)
+        if bs:
+            buckets[f"{a}-{min(a + 9, hi)}"] = {
+                "instances": len(bs), "median_bytes": bs[len(bs) // 2], "max_bytes": bs[-1],
+                "sum_bytes": sum(bs)}
+    print(json.dumps({
+        "workload": f"ragged batch of {len(instances)} random 3-SAT instances, n uniform in "
+                    f"[{lo}, {hi}], clause ratio uniform in [3.5, 5.0], seeded per instance",
+        "plan_only": True, "trials": 1, "target_bits": TARGET_BITS, "peak_bits_max": peak,
+        "planning_s": round(plan_s, 1), "planning_cores": min(os.cpu_count() or 1, 32),
+        "total_bytes": sum(everything), "median_bytes": everything[len(everything) // 2],
+        "by_n": buckets}), flush=True)
+
+
 def run_ragged(args) -> None:
     lo, hi = args.n_range
     instances = ragged_instances(args.instances, lo, hi)
     # planning is host work (tens of milliseconds per instance): spread it over the host cores
     # in spawned processes, before this process touches CUDA
+    t_plan = time.perf_counter()
     with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
         trees = pool.map(_plan_instance, [(c.num_vars, c.clauses) for c in instances],
                          chunksize=4)
+    t_plan = time.perf_counter() - t_plan
+    if args.plan_only:
+        ragged_plan_report(args, instances, trees, t_plan)
+        return
 
     import torch
 

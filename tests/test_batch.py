@@ -147,3 +147,21 @@ def test_batch_serving_graphs_follow_loaded_leaves(cuda):
     assert len(batch._graphs) == 2  # one capture per ring, replayed ever since
     with pytest.raises(ValueError):
         batch.load(one[:-1])
+
+
+def test_ragged_plan_only_report_runs_on_the_host():
+    """bench.py --workload ragged --plan-only plans a batch on the host cores and reports
+    its algorithmic bytes per n without touching a GPU."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--workload", "ragged",
+                          "--instances", "6", "--n-range", "12", "16", "--plan-only"],
+                         capture_output=True, text=True, timeout=600, check=True)
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["plan_only"] is True
+    assert sum(b["instances"] for b in line["by_n"].values()) == 6
+    assert line["total_bytes"] > 0 and line["peak_bits_max"] <= 26
