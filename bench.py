@@ -433,6 +433,14 @@ def _plan_instance(args):
                      target_bits=TARGET_BITS, trials=1)
 
 
+def _dpll_instance(args):
+    """Exact model count of one instance by the oracle's DPLL counter (the checker)."""
+    num_vars, clauses = args
+    from oracle import finrel_oracle as orc
+
+    return orc.dpll_count(num_vars, clauses)[0]
+
+
 def ragged_plan_report(args, instances, trees, plan_s: float) -> None:
     """Algorithmic bytes of every planned instance (3-prime count + OR-AND bit, both
     operands read once and the result written once per step), summarised per n."""
@@ -471,13 +479,14 @@ def run_ragged(args) -> None:
     # planning is host work (tens of milliseconds per instance): spread it over the host cores
     # in spawned processes, before this process touches CUDA
     t_plan = time.perf_counter()
+    jobs = [(c.num_vars, c.clauses) for c in instances]
     with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
-        trees = pool.map(_plan_instance, [(c.num_vars, c.clauses) for c in instances],
-                         chunksize=4)
-    t_plan = time.perf_counter() - t_plan
-    if args.plan_only:
-        ragged_plan_report(args, instances, trees, t_plan)
-        return
+        trees = pool.map(_plan_instance, jobs, chunksize=4)
+        t_plan = time.perf_counter() - t_plan
+        if args.plan_only:
+            ragged_plan_report(args, instances, trees, t_plan)
+            return
+        expected = pool.map(_dpll_instance, jobs, chunksize=4)
 
     import torch
 
@@ -549,6 +558,10 @@ def run_ragged(args) -> None:
         answers.append((b.count(num_primes=NUM_PRIMES), [bool(x) for x in b.contract()]))
     torch.cuda.synchronize()
     uncaptured_value = len(diagrams) / (time.perf_counter() - t0)
+    got_counts = [int(x) for counts, _ in answers for x in counts]
+    got_bits = [b for _, bits in answers for b in bits]
+    if got_counts != expected or got_bits != [e > 0 for e in expected]:
+        raise RuntimeError("batched counts or SAT bits differ from the DPLL counts")
 
     # end to end, serving form: every chunk captures one graph per ring on its first call
     # (set-up, like planning); each timed pass copies every instance's host leaves into the
@@ -597,6 +610,8 @@ def run_ragged(args) -> None:
                    "instances": len(instances), "n_range": [lo, hi],
                    "graphs": len(graphs), "instances_per_graph": RAGGED_CHUNK,
                    "l2": "not flushed: small instances are L2-resident by design"},
+        "parity": f"counts and SAT bits of all {len(instances)} instances equal the "
+                  "oracle's DPLL counts",
         "plain": {"value": plain_value, "unit": UNIT, "sample": sample,
                   "form": "GpuContraction.count + contract per instance"},
         "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
