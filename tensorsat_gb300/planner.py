@@ -328,13 +328,15 @@ def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
                 sliced: frozenset[int] = frozenset(), max_bits: int | None = None
                 ) -> ContractionTree:
     """Subtree reconfiguration. For every internal node x, the subtree below x is cut at
-    up to ``subtree_size`` inputs (expanding its most expensive steps first) and replaced
-    by the cheapest binary contraction of those inputs, found by dynamic programming over
-    subsets. A partial contraction of a subset S keeps a wire when x keeps it or an input
+    up to ``subtree_size`` (at most 20) inputs (expanding its most expensive steps first)
+    and replaced by the cheapest binary contraction of those inputs, found by dynamic
+    programming over subsets (:func:`subset_dp`). A partial contraction of a subset S keeps a wire when x keeps it or an input
     outside S carries it. Cost is the tree's index-space cost per slice: the sum over
     steps of 2^|wires of both operands, sliced wires excluded|. With ``max_bits`` no new
     intermediate may exceed 2^max_bits entries per slice. The root and every leaf are
     unchanged, so the answers are too."""
+    if subtree_size > 20:
+        raise ValueError("subtree_size must be at most 20")
     L = tree.num_leaves
     wires: dict[int, frozenset[int]] = dict(enumerate(tree.node_wires))
     children: dict[int, tuple[int, int]] = {L + s: ab for s, ab in enumerate(tree.steps)}
