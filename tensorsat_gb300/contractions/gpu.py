@@ -16,8 +16,11 @@ tree contracted over the integers, either modulo 2^64 (exact when the count boun
 
 from __future__ import annotations
 
+import json
 import math
+import os
 from dataclasses import dataclass
+from pathlib import Path
 from typing import Any, Sequence
 
 import numpy as np
@@ -134,6 +137,15 @@ def plan_tree(wiring: Wiring, target_bits: int | None = 26, trials: int = 8,
     tree, sl = planner.optimize(_network(_prepare(wiring)), target_bits=target_bits,
                                 trials=trials, seed=seed)
     return tree, tuple(sorted(sl))
+
+
+_CHECKPOINT_FORMAT = "tensorsat_gb300.count_checkpoint/1"
+
+
+def _write_json(path: Path, data: dict) -> None:
+    tmp = path.with_name(path.name + ".tmp")
+    tmp.write_text(json.dumps(data))
+    os.replace(tmp, path)
 
 
 def _functional_ports(t: np.ndarray) -> list[int]:
@@ -582,6 +594,73 @@ class GpuContraction(Contraction):
         else:
             raise ValueError(f"unknown count ring {ring!r}")
         return self._counts_from_root(counts)
+
+    # -- plans and checkpoints --------------------------------------------------------
+
+    def plan_dict(self) -> dict:
+        """The tree and sliced wires (``planner.plan_to_dict``) with the prepared leaf
+        wires they index, as JSON data."""
+        d = planner.plan_to_dict(self._tree, self._plan.sliced)
+        d["leaf_wires"] = [list(ws) for ws in self._leaves.leaf_wires]
+        return d
+
+    def save_plan(self, path: str | os.PathLike) -> None:
+        """Writes :meth:`plan_dict` as JSON (atomically: a temporary file, then a rename),
+        so another process can skip planning with :meth:`from_plan`."""
+        _write_json(Path(path), self.plan_dict())
+
+    @classmethod
+    def from_plan(cls, box_class: type, wiring: Wiring,
+                  plan: dict | str | os.PathLike) -> "GpuContraction":
+        """A contraction for ``wiring`` that runs a saved plan (a :meth:`plan_dict` or the
+        path of a :meth:`save_plan` file) instead of planning. Raises ValueError when the
+        plan was made for other leaves."""
+        data = plan if isinstance(plan, dict) else json.loads(Path(plan).read_text())
+        tree, sliced = planner.plan_from_dict(data)
+        if [tuple(ws) for ws in data.get("leaf_wires", [])] != \
+                [tuple(ws) for ws in _prepare(wiring).leaf_wires]:
+            raise ValueError("the plan was made for a different wiring")
+        return cls(box_class, wiring, tree=tree, sliced=sliced)
+
+    def count_checkpointed(self, diagram: Diagram, path: str | os.PathLike, *,
+                           chunk_slices: int, ring: str = "modp",
+                           num_primes: int | None = None, group: int | None = None) -> int:
+        """Exact model count of a closed network, run ``chunk_slices`` slices at a time.
+        After every chunk its count (chunks are disjoint slice ranges, whose counts add
+        up) is recorded in the JSON file at ``path`` together with the plan; a later call
+        with the same file skips the recorded chunks, so an interrupted run resumes where
+        it stopped. Raises ValueError when the file belongs to another plan or other
+        arguments."""
+        if self._leaves.out_unique:
+            raise ValueError("count_checkpointed counts closed networks only")
+        if chunk_slices < 1:
+            raise ValueError("chunk_slices must be positive")
+        path = Path(path)
+        settings = {"ring": ring, "num_primes": num_primes, "chunk_slices": int(chunk_slices)}
+        plan = self.plan_dict()
+        done: dict[str, str] = {}
+        if path.exists():
+            state = json.loads(path.read_text())
+            if state.get("format") != _CHECKPOINT_FORMAT or state.get("plan") != plan or \
+                    state.get("settings") != settings:
+                raise ValueError(f"{path} records another plan or other count arguments")
+            done = dict(state["done"])
+        ns = self.num_slices
+        # every chunk starts at a multiple of the slice group (a power of two)
+        if group is None:
+            code = _native.TSG_RING_U64 if ring == "u64" else _native.TSG_RING_MODP
+            group = self.choose_group(code, 1 if ring == "u64" else _native.TSG_MAX_PRIMES)
+        group = min(group, chunk_slices & -chunk_slices)
+        for begin in range(0, ns, chunk_slices):
+            key = str(begin)
+            if key in done:
+                continue
+            rng = (begin, min(ns, begin + chunk_slices))
+            done[key] = str(int(self.count(diagram, ring=ring, num_primes=num_primes,
+                                           group=group, slice_range=rng)))
+            _write_json(path, {"format": _CHECKPOINT_FORMAT, "plan": plan,
+                               "settings": settings, "done": done})
+        return sum(int(v) for v in done.values())
 
     def _counts_from_root(self, counts: np.ndarray) -> Any:
         """Counts (``int`` for a closed network, an object array over the out wires

@@ -113,6 +113,38 @@ class ContractionTree:
         return tuple(path)
 
 
+PLAN_FORMAT = "tensorsat_gb300.plan/1"
+
+
+def plan_to_dict(tree: ContractionTree, sliced: Sequence[int]) -> dict:
+    """A tree and its sliced wires as plain JSON data (format ``PLAN_FORMAT``)."""
+    return {
+        "format": PLAN_FORMAT,
+        "num_leaves": tree.num_leaves,
+        "steps": [list(ab) for ab in tree.steps],
+        "node_wires": [sorted(ws) for ws in tree.node_wires],
+        "out_wires": list(tree.out_wires),
+        "sliced": sorted(int(w) for w in sliced),
+    }
+
+
+def plan_from_dict(data: dict) -> tuple[ContractionTree, tuple[int, ...]]:
+    """Inverse of :func:`plan_to_dict`; raises ValueError on another format or a
+    malformed tree (steps must consume earlier nodes, node wire sets must match)."""
+    if not isinstance(data, dict) or data.get("format") != PLAN_FORMAT:
+        raise ValueError(f"not a {PLAN_FORMAT} plan")
+    L = int(data["num_leaves"])
+    steps = [(int(a), int(b)) for a, b in data["steps"]]
+    node_wires = [frozenset(int(w) for w in ws) for ws in data["node_wires"]]
+    if len(node_wires) != L + len(steps):
+        raise ValueError("plan: node_wires must list every leaf and step")
+    for s, (a, b) in enumerate(steps):
+        if not (0 <= a < L + s and 0 <= b < L + s and a != b):
+            raise ValueError(f"plan: step {s} must combine two earlier nodes")
+    tree = ContractionTree(L, steps, node_wires, tuple(int(w) for w in data["out_wires"]))
+    return tree, tuple(int(w) for w in data["sliced"])
+
+
 def _primal(tensors: dict[int, frozenset[int]], protect: frozenset[int]) -> dict[int, set[int]]:
     adj: dict[int, set[int]] = {}
     for ws in tensors.values():

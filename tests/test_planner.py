@@ -222,3 +222,62 @@ def test_plans_with_native_dp_equal_python_dp_plans(monkeypatch, k, n, m, seed, 
     assert native[0].steps == reference[0].steps
     assert native[0].node_wires == reference[0].node_wires
     assert native[1] == reference[1]
+
+
+def test_plans_round_trip_through_json(tmp_path):
+    cnf = CNFInstance.random(3, 16, 68, rng=1)
+    d = cnf.clause_diagram()
+    c = GpuContraction(CudaRel, d.wiring, target_bits=6, trials=1)
+    path = tmp_path / "plan.json"
+    c.save_plan(path)
+    again = GpuContraction.from_plan(CudaRel, d.wiring, path)
+    assert again.tree.steps == c.tree.steps and again.tree.node_wires == c.tree.node_wires
+    assert again.sliced_wires == c.sliced_wires
+    for k, v in c.sliced_plan.native_arrays().items():
+        np.testing.assert_array_equal(again.sliced_plan.native_arrays()[k], v)
+    other = CNFInstance.random(3, 16, 68, rng=2).clause_diagram()
+    with pytest.raises(ValueError):
+        GpuContraction.from_plan(CudaRel, other.wiring, path)
+    with pytest.raises(ValueError):
+        planner.plan_from_dict({"format": "something else"})
+    bad = c.plan_dict()
+    bad["steps"][0] = [0, 0]
+    with pytest.raises(ValueError):
+        planner.plan_from_dict(bad)
+
+
+def test_checkpointed_count_resumes_after_an_interruption(tmp_path, monkeypatch):
+    """count_checkpointed records each finished chunk; after a failure mid-run a second
+    call counts only the chunks still missing, and the total is the sum over all slices.
+    The per-chunk GPU count is replaced by a host function of the slice range here (the
+    real one, GpuContraction.count with slice_range, is covered by the GPU tests)."""
+    cnf = CNFInstance.random(3, 20, 85, rng=2)
+    d = cnf.clause_diagram()
+    c = GpuContraction(CudaRel, d.wiring, target_bits=8, trials=1)
+    ns = c.num_slices
+    assert ns >= 8
+    calls = []
+
+    def fake_count(self, diagram, *, ring, num_primes, group, slice_range):
+        assert slice_range[0] % group == 0
+        calls.append(slice_range)
+        if len(calls) == 3 and fail["on"]:
+            raise RuntimeError("interrupted")
+        return sum(range(*slice_range)) + 1
+
+    fail = {"on": True}
+    monkeypatch.setattr(GpuContraction, "count", fake_count)
+    path = tmp_path / "count.json"
+    with pytest.raises(RuntimeError):
+        c.count_checkpointed(d, path, chunk_slices=ns // 8, group=64)
+    assert len(calls) == 3
+    fail["on"] = False
+    calls.clear()
+    total = c.count_checkpointed(d, path, chunk_slices=ns // 8, group=64)
+    assert len(calls) == 8 - 2  # the two finished chunks are not recounted
+    assert total == sum(range(ns)) + 8
+    calls.clear()
+    assert c.count_checkpointed(d, path, chunk_slices=ns // 8, group=64) == total
+    assert calls == []
+    with pytest.raises(ValueError):  # other arguments, same file
+        c.count_checkpointed(d, path, chunk_slices=ns // 4, group=64)
