@@ -477,7 +477,11 @@ def run_ragged(args) -> None:
     lo, hi = args.n_range
     instances = ragged_instances(args.instances, lo, hi)
     # planning is host work (tens of milliseconds per instance): spread it over the host cores
-    # in spawned processes, before this process touches CUDA
+    # in spawned processes, before this process touches CUDA. The planner calls the native
+    # library's host code: load (and if needed build) it here once, not in every worker.
+    from tensorsat_gb300 import _native
+
+    _native.lib()
     t_plan = time.perf_counter()
     jobs = [(c.num_vars, c.clauses) for c in instances]
     with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
