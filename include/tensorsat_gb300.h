@@ -205,6 +205,22 @@ TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t
                              const uint32_t* primes, int64_t slice_begin,
                              int64_t slice_end, int64_t group_size);
 
+/* Kernel families of a tree step (tsg_plan_describe). */
+#define TSG_KERNEL_GENERAL 0 /* one output entry per thread, bit-scatter offsets */
+#define TSG_KERNEL_TILE 1    /* tile kernel: V positions and NE enumerated outputs per thread */
+#define TSG_KERNEL_STREAM 2  /* streaming kernel: TMA-staged operands, persistent blocks */
+
+/* For every tree step s, the kernel tsg_plan_run launches for it with these arguments
+ * (the first slice group of size group_size, 1 <= group_size <= slices), as four int32
+ * at kinds[4 s ...]: the family (TSG_KERNEL_*), then the template parameters V (tile
+ * kernel: positions per thread, else 0), NE (enumerated output combinations per thread)
+ * and NK (summed combinations unrolled at compile time; 0 = a runtime count). Builds and
+ * bounds-checks every launch like tsg_plan_validate; touches no device memory and needs no
+ * GPU. No counterpart in the reference, which contracts every step with one numpy einsum
+ * (tensorsat/lang/fin_rel.py:276,283). */
+TSG_API tsg_status tsg_plan_describe(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                             const uint32_t* primes, int64_t group_size, int32_t* kinds);
+
 /* ---------------------------------------------------------------------------------
  * Planner (host only; touches no device and needs no GPU).
  *

@@ -29,6 +29,10 @@ TSG_RING_U64 = 2
 TSG_MAX_BITS = 62
 TSG_MAX_PRIMES = 4
 
+TSG_KERNEL_GENERAL = 0
+TSG_KERNEL_TILE = 1
+TSG_KERNEL_STREAM = 2
+
 EXPORTED_SYMBOLS = (
     "tsg_last_error",
     "tsg_abi_version",
@@ -51,6 +55,7 @@ EXPORTED_SYMBOLS = (
     "tsg_static_scratch_bytes",
     "tsg_plan_run_static",
     "tsg_plan_subset_dp",
+    "tsg_plan_describe",
 )
 
 
@@ -131,6 +136,9 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_validate.restype = c_int32
     lib.tsg_plan_validate.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_int64,
                                       c_int64, c_int64]
+    lib.tsg_plan_describe.restype = c_int32
+    lib.tsg_plan_describe.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_int64,
+                                      _i32p]
     u64p = POINTER(ctypes.c_uint64)
     lib.tsg_plan_subset_dp.restype = c_int32
     lib.tsg_plan_subset_dp.argtypes = [c_int32, c_int32, u64p, u64p, u64p, c_int32,

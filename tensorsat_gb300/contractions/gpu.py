@@ -233,6 +233,7 @@ class NativePlan:
         self.leaf_sizes = sizes
         self.pool_bytes = max(off, 16)
         self.num_sliced = len(plan.sliced)
+        self.num_steps = len(plan.tree.steps)
         self._arrs = arrs
         handle = _native.c_void_p()
         lsp = np.ascontiguousarray(arrs["leaf_slice_pos"], dtype=np.int32)
@@ -259,6 +260,16 @@ class NativePlan:
         _native.check(self._lib.tsg_plan_launch_count(self.handle, begin, end, group,
                                                       _native.ctypes.byref(out)))
         return int(out.value)
+
+    def describe(self, ring: int, primes: Sequence[int], group: int) -> np.ndarray:
+        """(steps, 4) int32: per tree step the kernel family (``TSG_KERNEL_*``) and its
+        template parameters V, NE, NK, as ``tsg_plan_run`` would launch them for a slice
+        group of ``group`` (host only, no GPU needed)."""
+        parr = (_native.c_uint32 * max(1, len(primes)))(*primes)
+        out = np.zeros((self.num_steps, 4), dtype=np.int32)
+        _native.check(self._lib.tsg_plan_describe(self.handle, ring, len(primes), parr, group,
+                                                  _native.ptr_i32(out)))
+        return out
 
     def validate(self, ring: int, primes: Sequence[int], begin: int, end: int, group: int) -> None:
         """Host-side bounds check of every launch (no GPU needed)."""

@@ -904,14 +904,38 @@ struct RunTimer {
   }
 };
 
-// Shared body of tsg_plan_run, tsg_plan_run_timed and tsg_plan_validate. With dry == true
-// no pointer is dereferenced and nothing is launched: every launch's arguments are built
-// and bounds-checked only. With a timer, every launch is followed by an event record.
+// Kernel and template parameters of one built launch, as tsg_plan_describe reports them
+// (the same selection as launch_step and the launch_tile_* / launch_stream_* switches).
+void describe_launch(const LaunchArgs& la, int ring, int32_t* out) {
+  if (la.streamed) {
+    const int nk = std::min(la.t.n_k, 4);
+    out[0] = TSG_KERNEL_STREAM;
+    out[1] = 0;
+    out[2] = la.shape.ne == 1 || la.shape.ne == 2 ? la.shape.ne : 4;
+    out[3] = nk == 1 || nk == 2 ? nk : 4;
+  } else if (la.tile) {
+    const int nk = la.shape.nk;
+    out[0] = TSG_KERNEL_TILE;
+    out[1] = la.shape.v;
+    out[2] = la.shape.ne == 1 || la.shape.ne == 2 ? la.shape.ne : 4;
+    out[3] = nk == 1 || nk == 2 ? nk : (nk == 4 && ring == TSG_RING_OR_AND ? 4 : 0);
+  } else {
+    out[0] = TSG_KERNEL_GENERAL;
+    out[1] = out[2] = out[3] = 0;
+  }
+}
+
+// Shared body of tsg_plan_run, tsg_plan_run_timed, tsg_plan_validate and
+// tsg_plan_describe. With dry == true no pointer is dereferenced and nothing is launched:
+// every launch's arguments are built and bounds-checked only (and, with `kinds`, each
+// step's kernel of the first slice group is recorded). With a timer, every launch is
+// followed by an event record.
 tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
                     const uint32_t* primes, const uint8_t* pool, int64_t slice_begin,
                     int64_t slice_end, int64_t group_size, void* workspace,
                     int64_t workspace_bytes, void* result_dev, int32_t accumulate,
-                    cudaStream_t stream, bool dry, RunTimer* timer = nullptr) {
+                    cudaStream_t stream, bool dry, RunTimer* timer = nullptr,
+                    int32_t* kinds = nullptr) {
   TSG_TRY(check_range(plan, slice_begin, slice_end, group_size));
   int64_t eb;
   int planes;
@@ -959,7 +983,10 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
   auto step = [&](int s, int64_t base, int64_t cnt) -> tsg_status {
     if (dry) {
       LaunchArgs la;
-      return build_step(c, s, base, cnt, &la);
+      TSG_TRY(build_step(c, s, base, cnt, &la));
+      if (kinds && (!plan->steps[s].dep || base == slice_begin))
+        describe_launch(la, ring, kinds + 4 * s);
+      return TSG_OK;
     }
     TSG_TRY(launch_step(c, s, base, cnt));
     return timed(s);
@@ -1197,6 +1224,16 @@ tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t num_pri
   if (!plan) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_validate: null plan");
   return run_impl(plan, ring, num_primes, primes, nullptr, slice_begin, slice_end, group_size,
                   nullptr, 0, nullptr, 0, nullptr, /*dry=*/true);
+}
+
+tsg_status tsg_plan_describe(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                             const uint32_t* primes, int64_t group_size, int32_t* kinds) {
+  if (!plan || !kinds) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_describe: null pointer");
+  const int64_t slices = int64_t(1) << plan->num_sliced;
+  if (group_size < 1 || group_size > slices)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_describe: group_size outside [1, slices]");
+  return run_impl(plan, ring, num_primes, primes, nullptr, 0, group_size, group_size,
+                  nullptr, 0, nullptr, 0, nullptr, /*dry=*/true, nullptr, kinds);
 }
 
 tsg_status tsg_batch_workspace_bytes(int32_t num_instances, const tsg_plan* const* plans,

@@ -182,3 +182,45 @@ def test_kissat_and_benchmark_plans_validate_in_every_ring():
                          (_native.TSG_RING_U64, ())]:
         for g in (1, 64):
             npl.validate(ring, primes, 0, 2 * g, g)
+
+
+def _profiled_kernels():
+    """(ring, step) -> (family, V, NE, NK) of every launch in the committed ncu summary of
+    the n=60 benchmark tree (one MODP run with 3 primes and one OR-AND run, 64 slices)."""
+    path = HEADER.parent.parent / "profiles" / "tree_steps_n60_dram.txt"
+    rings = {"modp": _native.TSG_RING_MODP, "or_and": _native.TSG_RING_OR_AND}
+    out = {}
+    for line in path.read_text().splitlines():
+        if line.startswith("#") or not line.strip():
+            continue
+        ring, step = line.split()[:2]
+        m = re.search(r"tsg::(tree_step_\w+)<([^>]*)>", line)
+        name, args = m.group(1), [int(x) for x in m.group(2).split(",")]
+        if name == "tree_step_tile_kernel":
+            kind = (_native.TSG_KERNEL_TILE, args[1], args[2], args[3])
+        elif name == "tree_step_stream_kernel":
+            kind = (_native.TSG_KERNEL_STREAM, 0, args[1], args[2])
+        else:
+            kind = (_native.TSG_KERNEL_GENERAL, 0, 0, 0)
+        out[(rings[ring], int(step))] = kind
+    return out
+
+
+def test_kernel_choice_matches_the_profiled_launches():
+    """tsg_plan_describe reports, on the host, the kernel that ran for every step in the
+    committed launch list of the benchmark (n=60, m=256, seed 0, 8 planner trials, 64
+    slices per group): the host-side selection is the one the GPU executed."""
+    cnf = CNFInstance.random(3, 60, 256, rng=0)
+    c = GpuContraction(CudaRel, cnf.clause_diagram().wiring, target_bits=26, trials=8, seed=0)
+    npl = c.native_plan()
+    expected = _profiled_kernels()
+    assert len(expected) >= 20
+    got = {_native.TSG_RING_MODP: npl.describe(_native.TSG_RING_MODP, PRIMES_31[:3], 64),
+           _native.TSG_RING_OR_AND: npl.describe(_native.TSG_RING_OR_AND, (), 64)}
+    for (ring, step), kind in expected.items():
+        assert tuple(int(x) for x in got[ring][step]) == kind, (ring, step)
+    kinds = got[_native.TSG_RING_MODP][:, 0]
+    assert set(kinds) <= {_native.TSG_KERNEL_GENERAL, _native.TSG_KERNEL_TILE,
+                          _native.TSG_KERNEL_STREAM}
+    with pytest.raises(_native.TsgValueError):
+        npl.describe(_native.TSG_RING_OR_AND, (), c.num_slices + 1)
