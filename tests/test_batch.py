@@ -165,3 +165,13 @@ def test_ragged_plan_only_report_runs_on_the_host():
     assert line["plan_only"] is True
     assert sum(b["instances"] for b in line["by_n"].values()) == 6
     assert line["total_bytes"] > 0 and line["peak_bits_max"] <= 26
+
+
+def test_batch_load_checks_its_diagrams_before_any_device_work():
+    instances = ragged_instances(3, 10, 14, seed=6)
+    one = [cnf.clause_diagram("1" + "?" * (cnf.num_vars - 1)) for cnf in instances]
+    batch = BatchContraction(CudaRel, one, target_bits=6, trials=1)
+    with pytest.raises(ValueError):
+        batch.load(one[:-1])  # wrong count
+    with pytest.raises(ValueError):
+        batch.load(list(reversed(one)))  # other wirings

@@ -281,3 +281,18 @@ def test_checkpointed_count_resumes_after_an_interruption(tmp_path, monkeypatch)
     assert calls == []
     with pytest.raises(ValueError):  # other arguments, same file
         c.count_checkpointed(d, path, chunk_slices=ns // 4, group=64)
+
+
+def test_checkpointed_count_argument_errors(tmp_path):
+    cnf = CNFInstance.random(3, 12, 50, rng=0)
+    closed = cnf.clause_diagram()
+    c = GpuContraction(CudaRel, closed.wiring, target_bits=4, trials=1)
+    with pytest.raises(ValueError):
+        c.count_checkpointed(closed, tmp_path / "a.json", chunk_slices=0, group=1)
+    opened = cnf.clause_diagram("_" + "?" * 11)
+    o = GpuContraction(CudaRel, opened.wiring, target_bits=4, trials=1)
+    with pytest.raises(ValueError):
+        o.count_checkpointed(opened, tmp_path / "b.json", chunk_slices=4, group=1)
+    (tmp_path / "c.json").write_text('{"format": "something else"}')
+    with pytest.raises(ValueError):
+        c.count_checkpointed(closed, tmp_path / "c.json", chunk_slices=4, group=1)
