@@ -224,3 +224,27 @@ def test_kernel_choice_matches_the_profiled_launches():
                           _native.TSG_KERNEL_STREAM}
     with pytest.raises(_native.TsgValueError):
         npl.describe(_native.TSG_RING_OR_AND, (), c.num_slices + 1)
+
+
+def test_subset_dp_rejects_bad_sizes_and_nulls():
+    lib = _native.lib()
+    u64 = ctypes.c_uint64 * 4
+    bits, keep, live = u64(1, 2, 4, 8), u64(0), u64(15)
+    best = ctypes.c_double()
+    split = (ctypes.c_uint32 * 16)()
+    kept = (ctypes.c_uint64 * 16)()
+    for n, words in [(0, 1), (21, 1), (4, 0), (4, 65)]:
+        assert lib.tsg_plan_subset_dp(n, words, bits, keep, live, -1, ctypes.byref(best),
+                                      split, kept) == _native.TSG_ERR_INVALID_ARGUMENT
+    assert lib.tsg_plan_subset_dp(4, 1, None, keep, live, -1, ctypes.byref(best), split,
+                                  kept) == _native.TSG_ERR_INVALID_ARGUMENT
+    assert lib.tsg_plan_subset_dp(4, 1, bits, keep, live, -1, ctypes.byref(best), split,
+                                  kept) == _native.TSG_OK
+    # four disjoint one-wire inputs, nothing kept: no partial result keeps a wire, so each
+    # of the 3 steps costs 2^0
+    assert best.value == 3.0
+    # every wire kept: pairs first, then the pair of pairs (4 + 4 + 16) beats a chain (28)
+    assert lib.tsg_plan_subset_dp(4, 1, bits, u64(15), live, -1, ctypes.byref(best), split,
+                                  kept) == _native.TSG_OK
+    assert best.value == 24.0
+    assert kept[15] == 15 and split[15] in (0b0011, 0b0101, 0b1001)
