@@ -247,6 +247,23 @@ TSG_API tsg_status tsg_plan_subset_dp(int32_t n, int32_t words, const uint64_t* 
  * record is cleared. Runs launched before the failure are invalid. */
 TSG_API tsg_status tsg_take_device_error(void* stream);
 
+/* Limit of every bounded wait inside the streaming kernel (a consumer waiting for staged
+ * data, the producer waiting for a free stage), in nanoseconds of the GPU's global timer;
+ * between 1 us and the default 2 s. A wait that runs out makes the kernel record
+ * TSG_ERR_TIMEOUT (read by tsg_take_device_error) and return; the producer still waits for
+ * its own copies in flight (up to 2 s) before its block exits. Applies to launches issued
+ * after the call, process-wide. No counterpart in the reference (no device code). */
+TSG_API tsg_status tsg_set_wait_limit_ns(uint64_t limit_ns);
+TSG_API uint64_t tsg_wait_limit_ns(void);
+
+/* Testing hook: with stages >= 0, the producer warp of every streaming block stops after
+ * issuing that many stages (it issues no further copy and arms no further barrier), so
+ * the consumers' next wait runs out after tsg_wait_limit_ns and the run reports
+ * TSG_ERR_TIMEOUT through tsg_take_device_error; results of such runs are invalid.
+ * stages < 0 (the default) turns it off. Process-wide, for launches issued after the
+ * call. It exercises the bounded-wait exit path without any device fault. */
+TSG_API tsg_status tsg_debug_stall_producer(int64_t stages);
+
 /* ---------------------------------------------------------------------------------
  * Allocation-free variant (no counterpart in the reference).
  *
@@ -263,7 +280,9 @@ TSG_API tsg_status tsg_take_device_error(void* stream);
  *     before any device work; lower group_size or use tsg_plan_run.
  *   - The first call on a device resolves the array's device address with
  *     cudaGetSymbolAddress (with that device current) and caches it; make that first
- *     call before any stream capture.
+ *     call before any stream capture. The cached address belongs to the device's primary
+ *     context, which the CUDA runtime uses: it is not refreshed after cudaDeviceReset or
+ *     for a caller that makes another context current, so such callers use tsg_plan_run.
  *   - Every call shares the one array and reuses whatever the previous call left in it:
  *     the executor writes each intermediate before reading it, so nothing needs clearing;
  *     result_dev follows the `accumulate` rule of tsg_plan_run.

@@ -56,6 +56,9 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_run_static",
     "tsg_plan_subset_dp",
     "tsg_plan_describe",
+    "tsg_set_wait_limit_ns",
+    "tsg_wait_limit_ns",
+    "tsg_debug_stall_producer",
 )
 
 
@@ -139,6 +142,12 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_describe.restype = c_int32
     lib.tsg_plan_describe.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_int64,
                                       _i32p]
+    lib.tsg_set_wait_limit_ns.restype = c_int32
+    lib.tsg_set_wait_limit_ns.argtypes = [ctypes.c_uint64]
+    lib.tsg_wait_limit_ns.restype = ctypes.c_uint64
+    lib.tsg_wait_limit_ns.argtypes = []
+    lib.tsg_debug_stall_producer.restype = c_int32
+    lib.tsg_debug_stall_producer.argtypes = [c_int64]
     u64p = POINTER(ctypes.c_uint64)
     lib.tsg_plan_subset_dp.restype = c_int32
     lib.tsg_plan_subset_dp.argtypes = [c_int32, c_int32, u64p, u64p, u64p, c_int32,

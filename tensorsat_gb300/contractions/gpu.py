@@ -16,6 +16,7 @@ tree contracted over the integers, either modulo 2^64 (exact when the count boun
 
 from __future__ import annotations
 
+import hashlib
 import json
 import math
 import os
@@ -139,7 +140,7 @@ def plan_tree(wiring: Wiring, target_bits: int | None = 26, trials: int = 8,
     return tree, tuple(sorted(sl))
 
 
-_CHECKPOINT_FORMAT = "tensorsat_gb300.count_checkpoint/1"
+_CHECKPOINT_FORMAT = "tensorsat_gb300.count_checkpoint/2"
 
 
 def _write_json(path: Path, data: dict) -> None:
@@ -358,7 +359,9 @@ class GpuContraction(Contraction):
         self._tree = tree
         self._plan = planner.SlicedPlan(tree, tuple(sorted(sl)), list(lw.leaf_wires))
         self._native: NativePlan | None = None
-        self._pool_cache: tuple[int, torch.Tensor] | None = None
+        # (diagram, device pool) of the last cached diagram; the diagram itself is held so
+        # that its id cannot be reused by a new diagram while the entry lives
+        self._pool_cache: tuple[Diagram, torch.Tensor] | None = None
 
     # -- plan inspection ------------------------------------------------------------
 
@@ -412,14 +415,14 @@ class GpuContraction(Contraction):
         """The diagram's leaf tensors packed into one device uint8 buffer (one host-to-
         device copy for host leaves; cached for the last diagram unless ``cache`` is
         False)."""
-        if cache and self._pool_cache is not None and self._pool_cache[0] == id(diagram):
+        if cache and self._pool_cache is not None and self._pool_cache[0] is diagram:
             return self._pool_cache[1]
         dev = _device.require_cuda()
         host, device_leaves = self._host_pool(diagram)
         pool = torch.from_numpy(host).to(dev, non_blocking=False)
         self._finish_pool(pool, device_leaves)
         if cache:
-            self._pool_cache = (id(diagram), pool)
+            self._pool_cache = (diagram, pool)
         return pool
 
     def _host_pool(self, diagram: Diagram) -> tuple[np.ndarray, list[tuple[int, Any]]]:
@@ -445,6 +448,22 @@ class GpuContraction(Contraction):
             arr = arr.reshape(-1)
             host[off: off + arr.size] = arr
         return host, device_leaves
+
+    def leaf_digest(self, diagram: Diagram) -> str:
+        """SHA-256 of the diagram's leaf values as this contraction packs them (host and
+        synthetic leaves at their pool offsets, then every device-resident or diagonal
+        leaf by id). Two diagrams with this wiring have equal digests exactly when they
+        contract the same leaf tensors."""
+        host, device_leaves = self._host_pool(diagram)
+        h = hashlib.sha256(host.tobytes())
+        for l, box in device_leaves:
+            if isinstance(box, CudaRel):
+                arr = box._tensor.detach().cpu().numpy()
+            else:
+                arr = leaf_array(box)
+            h.update(f"leaf {l} {tuple(arr.shape)}".encode())
+            h.update(np.ascontiguousarray(arr, dtype=np.uint8).tobytes())
+        return h.hexdigest()
 
     def _finish_pool(self, pool: torch.Tensor, device_leaves: list[tuple[int, Any]]) -> None:
         """Writes the device leaves of :meth:`_host_pool` into a device pool that already
@@ -640,8 +659,9 @@ class GpuContraction(Contraction):
         After every chunk its count (chunks are disjoint slice ranges, whose counts add
         up) is recorded in the JSON file at ``path`` together with the plan; a later call
         with the same file skips the recorded chunks, so an interrupted run resumes where
-        it stopped. Raises ValueError when the file belongs to another plan or other
-        arguments."""
+        it stopped. The file also records a digest of the leaf tensors
+        (:meth:`leaf_digest`). Raises ValueError when the file belongs to another plan,
+        other arguments or other leaves (another instance with the same wiring)."""
         if self._leaves.out_unique:
             raise ValueError("count_checkpointed counts closed networks only")
         if chunk_slices < 1:
@@ -649,12 +669,16 @@ class GpuContraction(Contraction):
         path = Path(path)
         settings = {"ring": ring, "num_primes": num_primes, "chunk_slices": int(chunk_slices)}
         plan = self.plan_dict()
+        leaves = self.leaf_digest(diagram)
         done: dict[str, str] = {}
         if path.exists():
             state = json.loads(path.read_text())
             if state.get("format") != _CHECKPOINT_FORMAT or state.get("plan") != plan or \
                     state.get("settings") != settings:
                 raise ValueError(f"{path} records another plan or other count arguments")
+            if state.get("leaves") != leaves:
+                raise ValueError(f"{path} records the counts of other leaf tensors (another "
+                                 "instance with the same wiring)")
             done = dict(state["done"])
         ns = self.num_slices
         # every chunk starts at a multiple of the slice group (a power of two)
@@ -670,7 +694,7 @@ class GpuContraction(Contraction):
             done[key] = str(int(self.count(diagram, ring=ring, num_primes=num_primes,
                                            group=group, slice_range=rng)))
             _write_json(path, {"format": _CHECKPOINT_FORMAT, "plan": plan,
-                               "settings": settings, "done": done})
+                               "settings": settings, "leaves": leaves, "done": done})
         return sum(int(v) for v in done.values())
 
     def _counts_from_root(self, counts: np.ndarray) -> Any:

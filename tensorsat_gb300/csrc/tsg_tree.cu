@@ -18,6 +18,7 @@
 // as one shift-and-mask.
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <type_traits>
 #include <map>
@@ -33,6 +34,11 @@ namespace {
 
 // Device-side failure record of the streaming kernels (they receive its address).
 __device__ int g_device_error = 0;  // 0 = ok, else TSG_ERR_TIMEOUT
+
+// Limit of each bounded device-side wait of the streaming kernels (tsg_set_wait_limit_ns)
+// and the producer stall of tsg_debug_stall_producer (< 0: off). Read at every launch.
+std::atomic<uint64_t> g_wait_limit_ns{kWaitLimitNs};
+std::atomic<int64_t> g_stall_after{-1};
 
 // Address of g_device_error on the current device (looked up once per device).
 tsg_status device_error_address(int** out) {
@@ -790,6 +796,8 @@ tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   TSG_TRY(build_step(c, s, base, cnt, &la));
   if (la.streamed) {
     TSG_TRY(device_error_address(&la.stream.error));
+    la.stream.wait_ns = g_wait_limit_ns.load(std::memory_order_relaxed);
+    la.stream.stop_after = g_stall_after.load(std::memory_order_relaxed);
     if (c.ring == TSG_RING_U64) TSG_TRY(launch_stream_u64(la, c.ra, c.stream));
     else TSG_TRY(launch_stream_modp(la, c.ra, c.stream));
     TSG_CUDA_TRY(cudaGetLastError());
@@ -1281,6 +1289,20 @@ tsg_status tsg_batch_run(int32_t num_instances, const tsg_plan* const* plans, in
 }
 
 int64_t tsg_static_scratch_bytes(void) { return kStaticScratchBytes; }
+
+tsg_status tsg_set_wait_limit_ns(uint64_t limit_ns) {
+  if (limit_ns < 1000 || limit_ns > kWaitLimitNs)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "set_wait_limit_ns: limit outside [1 us, 2 s]");
+  g_wait_limit_ns.store(limit_ns, std::memory_order_relaxed);
+  return TSG_OK;
+}
+
+uint64_t tsg_wait_limit_ns(void) { return g_wait_limit_ns.load(std::memory_order_relaxed); }
+
+tsg_status tsg_debug_stall_producer(int64_t stages) {
+  g_stall_after.store(stages < 0 ? -1 : stages, std::memory_order_relaxed);
+  return TSG_OK;
+}
 
 tsg_status tsg_take_device_error(void* stream) {
   int err = 0;

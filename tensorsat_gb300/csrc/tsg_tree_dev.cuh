@@ -593,16 +593,20 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
 //   * 8 consumer warps (4 positions per thread) combine an item from its stage, write the
 //     result from registers as 16-byte vectors, and release the stage (one arrival per
 //     warp on the stage's `empty` barrier); nothing else synchronises the block.
-// Every mbarrier wait is bounded: on expiry the thread records an error in
-// the executor's error record (StreamArgs::error) and sets the block's bail flag; the producer then waits (bounded) for
-// the copies it has in flight and every thread returns.
+// Every mbarrier wait is bounded (StreamArgs::wait_ns): on expiry the thread records an
+// error in the executor's error record (StreamArgs::error) and sets the block's bail flag;
+// the producer then waits (bounded by kDrainLimitNs) for the copies it has in flight and
+// every thread returns.
 
 constexpr int kStreamTileBits = 10;                      // 256 consumer threads x 4
 constexpr int kStreamTile = 1 << kStreamTileBits;
 constexpr int kStreamConsumers = 256;
 constexpr int kStreamThreads = kStreamConsumers + 32;    // + the producer warp
 constexpr int kStreamMaxStages = 8;
-constexpr uint64_t kWaitLimitNs = 2000000000ull;         // one bounded wait: 2 s
+constexpr uint64_t kWaitLimitNs = 2000000000ull;         // default limit of one bounded wait: 2 s
+// Limit of the producer's final wait for its own copies in flight: never shorter than the
+// default, so that a block never exits while a bulk copy still writes its shared memory.
+constexpr uint64_t kDrainLimitNs = kWaitLimitNs;
 constexpr uint32_t kSuspendHintNs = 20000;               // longest suspension per try_wait
 
 
@@ -657,22 +661,24 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Bounded wait for phase `parity` of `bar`: false when kWaitLimitNs of wall-clock time
-// (the global nanosecond timer) passed without the phase completing.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Bounded wait for phase `parity` of `bar`: false when `limit_ns` of wall-clock time (the
+// global nanosecond timer) passed without the phase completing.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t limit_ns) {
   if (mbar_try_wait_suspend(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (;;) {
     if (mbar_try_wait_suspend(bar, parity)) return true;
-    if (global_ns() - t0 > kWaitLimitNs) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 
 // Warp-uniform bounded wait (every lane of the warp calls it): lane 0 polls, the outcome
 // is broadcast, and on success every lane observes the completed phase itself (acquire).
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity,
+                                               uint64_t limit_ns) {
   int ok = 0;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity) ? 1 : 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait_bounded(bar, parity, limit_ns) ? 1 : 0;
   ok = __shfl_sync(0xffffffffu, ok, 0);
   if (ok) (void)mbar_try_wait(bar, parity);
   return ok != 0;
@@ -698,6 +704,9 @@ struct StreamArgs {
   int32_t stages;        // stages in the ring (2 .. kStreamMaxStages)
   int32_t kchunks;       // stages per item: its summed combinations, 4 (NK) per stage
   int* error;            // set to TSG_ERR_TIMEOUT when a bounded wait gives up
+  uint64_t wait_ns;      // limit of every bounded wait of the pipeline (default 2 s)
+  int64_t stop_after;    // testing hook: the producer stops after issuing this many stages
+                         // (< 0: never), so that the consumers' next wait runs out
 };
 
 // Offsets of one staged item, written by the producer next to its stage.
@@ -807,11 +816,12 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
         for (int kc = 0; kc < sa.kchunks; ++kc, ++i) {  // one stage per KU summed combinations
           const int s = (int)(i % nst);
           const uint32_t round = (uint32_t)(i / nst);
-          if (__shfl_sync(0xffffffffu, (int)bail, 0)) {
+          if (__shfl_sync(0xffffffffu, (int)bail, 0) ||
+              (sa.stop_after >= 0 && i >= (uint64_t)sa.stop_after)) {
             stop = true;
             break;
           }
-          if (round > 0 && !mbar_wait_warp(&empty[s], (round - 1) & 1)) {
+          if (round > 0 && !mbar_wait_warp(&empty[s], (round - 1) & 1, sa.wait_ns)) {
             if (lane == 0) {
               atomicExch(sa.error, TSG_ERR_TIMEOUT);
               bail = 1;
@@ -846,7 +856,7 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
     if (lane == 0) {
       const uint64_t first = i > (uint64_t)nst ? i - nst : 0;
       for (uint64_t j = first; j < i; ++j)
-        (void)mbar_wait_bounded(&full[j % nst], (uint32_t)((j / nst) & 1));
+        (void)mbar_wait_bounded(&full[j % nst], (uint32_t)((j / nst) & 1), kDrainLimitNs);
     }
     return;
   }
@@ -872,7 +882,7 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
     for (int kc = 0; kc < sa.kchunks; ++kc, ++i) {
       const int s = (int)(i % nst);
       if (__shfl_sync(0xffffffffu, (int)bail, 0)) return false;
-      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
+      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1), sa.wait_ns)) {
         if (lane == 0) {
           atomicExch(sa.error, TSG_ERR_TIMEOUT);
           bail = 1;
@@ -968,7 +978,7 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
       }
       const int s = (int)(i % nst);
       if (__shfl_sync(0xffffffffu, (int)bail, 0)) return;
-      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1))) {
+      if (!mbar_wait_warp(&full[s], (uint32_t)((i / nst) & 1), sa.wait_ns)) {
         if (lane == 0) {
           atomicExch(sa.error, TSG_ERR_TIMEOUT);
           bail = 1;

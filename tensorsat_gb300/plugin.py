@@ -56,6 +56,11 @@ def make_finrel_cuda(tensorsat_module: Any | None = None) -> type:
         def from_finrel(cls, rel: Any) -> "FinRelCuda":
             return cls._new(_dev(np.asarray(rel.tensor)))
 
+        @classmethod
+        def from_array(cls, array: Any) -> "FinRelCuda":
+            """The relation whose {0,1} tensor is ``array`` (copied to the device)."""
+            return cls._new(_dev(np.asarray(array)))
+
         def to_finrel(self) -> Any:
             return FinRel._new(self._FinRelCuda__tensor.cpu().numpy())
 

@@ -11,8 +11,12 @@ sources importable *without modifying them*:
    ``typing_validation.validate`` are installed in ``sys.modules``;
 3. bytecode writing is disabled so no ``__pycache__`` lands in the upstream tree.
 
-Only ``tests/golden/make_golden.py`` uses this; nothing under the product package or
-the GPU test suite imports it (the upstream checkout is absent on GPU hosts).
+Where the sources come from (:func:`reference_root`): the directory named by the
+``TENSORSAT_REFERENCE`` environment variable (an upstream checkout, as
+``tests/golden/make_golden.py`` needs for the upstream example files), else the
+``baseline/_ref`` install of the unmodified upstream package at the repository root (which
+travels with the repository to GPU hosts). ``tests/golden/make_golden.py`` and the
+reference-side plugin tests use it; nothing under the product package imports it.
 """
 
 from __future__ import annotations
@@ -26,7 +30,29 @@ import re
 import sys
 import types
 
-REFERENCE_ROOT = os.environ.get("TENSORSAT_REFERENCE", "/root/reference")
+REPO_ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+INSTALLED_ROOT = os.path.join(REPO_ROOT, "baseline", "_ref")
+
+
+def candidate_roots() -> list[str]:
+    """Directories searched for the upstream ``tensorsat`` package, in order."""
+    roots = []
+    env = os.environ.get("TENSORSAT_REFERENCE")
+    if env:
+        roots.append(env)
+    roots.append(INSTALLED_ROOT)
+    return roots
+
+
+def reference_root() -> str | None:
+    """The first candidate directory that holds ``tensorsat/``, or None."""
+    for root in candidate_roots():
+        if os.path.isdir(os.path.join(root, "tensorsat")):
+            return root
+    return None
+
+
+REFERENCE_ROOT = reference_root() or INSTALLED_ROOT
 
 _TYPEVAR_DEFAULT = re.compile(r"(TypeVar\([^()]*?),\s*default\s*=\s*[A-Za-z_][\w\.]*\s*\)")
 
@@ -117,4 +143,4 @@ def install() -> None:
 
 
 def available() -> bool:
-    return os.path.isdir(os.path.join(REFERENCE_ROOT, "tensorsat"))
+    return reference_root() is not None

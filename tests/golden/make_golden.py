@@ -1,9 +1,9 @@
 """Generates the golden fixtures of tests/golden from the upstream tensorsat sources.
 
-Run in a container that holds the upstream checkout (``TENSORSAT_REFERENCE``, default
-``/root/reference``):
+Run in a container that holds the upstream checkout, named by ``TENSORSAT_REFERENCE``
+(the example files it reads lie outside the installed package):
 
-    python tests/golden/make_golden.py
+    TENSORSAT_REFERENCE=/root/reference python tests/golden/make_golden.py
 
 Everything here is computed by the upstream code itself, imported through
 ``_ref_import`` (no upstream file is modified or copied):

@@ -248,3 +248,20 @@ def test_subset_dp_rejects_bad_sizes_and_nulls():
                                   kept) == _native.TSG_OK
     assert best.value == 24.0
     assert kept[15] == 15 and split[15] in (0b0011, 0b0101, 0b1001)
+
+
+def test_wait_limit_setting_is_range_checked():
+    """The bounded-wait limit of the streaming kernel is settable between 1 us and the 2 s
+    default; values outside are rejected and leave the setting unchanged."""
+    lib = _native.lib()
+    default = lib.tsg_wait_limit_ns()
+    assert default == 2_000_000_000
+    try:
+        assert lib.tsg_set_wait_limit_ns(999) == _native.TSG_ERR_INVALID_ARGUMENT
+        assert lib.tsg_set_wait_limit_ns(3_000_000_000) == _native.TSG_ERR_INVALID_ARGUMENT
+        assert lib.tsg_wait_limit_ns() == default
+        assert lib.tsg_set_wait_limit_ns(1_000_000) == _native.TSG_OK
+        assert lib.tsg_wait_limit_ns() == 1_000_000
+    finally:
+        assert lib.tsg_set_wait_limit_ns(default) == _native.TSG_OK
+    assert lib.tsg_debug_stall_producer(-5) == _native.TSG_OK  # off

@@ -283,6 +283,39 @@ def test_checkpointed_count_resumes_after_an_interruption(tmp_path, monkeypatch)
         c.count_checkpointed(d, path, chunk_slices=ns // 4, group=64)
 
 
+def test_checkpointed_count_rejects_other_leaves(tmp_path, monkeypatch):
+    """A checkpoint records a digest of the leaf tensors: resuming it with a diagram of the
+    same wiring but another clause tensor (one literal's sign flipped) raises ValueError
+    instead of adding chunk counts of another instance."""
+    cnf = CNFInstance.random(3, 20, 85, rng=2)
+    flipped = [list(c) for c in cnf.clauses]
+    flipped[0][0] = -flipped[0][0]
+    other = CNFInstance(cnf.num_vars, flipped)
+    d, d2 = cnf.clause_diagram(), other.clause_diagram()
+    assert d2.wiring == d.wiring
+    c = GpuContraction(CudaRel, d.wiring, target_bits=8, trials=1)
+    assert c.leaf_digest(d) != c.leaf_digest(d2)
+    assert c.leaf_digest(d) == c.leaf_digest(cnf.clause_diagram())
+
+    def fake_count(self, diagram, *, ring, num_primes, group, slice_range):
+        if calls and fail["on"]:
+            raise RuntimeError("interrupted")
+        calls.append(slice_range)
+        return 1
+
+    calls: list = []
+    fail = {"on": True}
+    monkeypatch.setattr(GpuContraction, "count", fake_count)
+    path = tmp_path / "count.json"
+    with pytest.raises(RuntimeError):
+        c.count_checkpointed(d, path, chunk_slices=c.num_slices // 4, group=64)
+    assert len(calls) == 1
+    fail["on"] = False
+    with pytest.raises(ValueError, match="other leaf tensors"):
+        c.count_checkpointed(d2, path, chunk_slices=c.num_slices // 4, group=64)
+    assert c.count_checkpointed(d, path, chunk_slices=c.num_slices // 4, group=64) == 4
+
+
 def test_checkpointed_count_argument_errors(tmp_path):
     cnf = CNFInstance.random(3, 12, 50, rng=0)
     closed = cnf.clause_diagram()
