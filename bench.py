@@ -12,6 +12,17 @@ bit). Every slice of an instance runs the same kernels on the same shapes, so
 (leaves) are resident in HBM for ``value``; ``e2e`` goes through the public API
 (``GpuContraction.count`` / ``.contract``) from host leaves to host results each step.
 
+The tree is the committed plan ``plans/3sat_n60_m256_rng0_t26.json`` (the project's
+planner with ``target_bits=26, trials=8, seed=0``; ``--replan`` plans again), so both arms
+contract the same tree and the reference arm loads no native code.
+
+``batched`` (default run, one GPU): a bounded ragged batch of random 3-SAT instances (n
+uniform in [30, 40], clause ratio uniform in [3.5, 5.0], seeded per instance), planned on
+the host cores before the first CUDA call, timed as captured-graph replays, in the plain
+per-instance form (``GpuContraction.count`` + ``.contract``) and in the serving form
+(``BatchContraction.load`` + ``graph=True``), with every count and SAT bit checked against
+the oracle's DPLL counts.
+
 ``--impl reference`` times the reference's CPU path for the same workload (the oracle's
 restatement of the upstream numpy contraction: per-slice einsum in the OR-AND semiring and
 over exact integers), one slice per process on all host cores.
@@ -40,6 +51,7 @@ UNIT = "instances/s"
 N_VARS, N_CLAUSES = 60, 256
 TARGET_BITS = 26
 NUM_PRIMES = 3
+PLAN_FILE = ROOT / "plans" / "3sat_n60_m256_rng0_t26.json"
 
 
 def parse_args():
@@ -61,6 +73,12 @@ def parse_args():
     p.add_argument("--plan-only", action="store_true",
                    help="ragged: plan the batch on the host cores and print its algorithmic "
                         "bytes per n (no GPU, no timing of contractions)")
+    p.add_argument("--replan", action="store_true",
+                   help="plan the n=60 tree instead of loading the committed plan")
+    p.add_argument("--no-batched", action="store_true",
+                   help="skip the ragged batched-vs-plain leg of the default run")
+    p.add_argument("--batched-steps", type=int, default=3,
+                   help="timed graph-replay passes of the ragged leg")
     return p.parse_args()
 
 
@@ -131,16 +149,57 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_workload(seed: int, trials: int):
+def committed_plan(args) -> dict | None:
+    """The committed plan of the headline workload (seed 0, 8 trials), unless replanning."""
+    if args.replan or args.seed != 0 or args.trials != 8 or not PLAN_FILE.exists():
+        return None
+    return json.loads(PLAN_FILE.read_text())
+
+
+def build_workload(args):
     from tensorsat_gb300.contractions.gpu import GpuContraction
     from tensorsat_gb300.lang.cuda_rel import CudaRel
     from tensorsat_gb300.lib.sat import CNFInstance
 
-    cnf = CNFInstance.random(3, N_VARS, N_CLAUSES, rng=seed)
+    cnf = CNFInstance.random(3, N_VARS, N_CLAUSES, rng=args.seed)
     diagram = cnf.clause_diagram()
-    contraction = GpuContraction(CudaRel, diagram.wiring, target_bits=TARGET_BITS,
-                                 trials=trials, seed=0)
+    plan = committed_plan(args)
+    if plan is not None:
+        contraction = GpuContraction.from_plan(CudaRel, diagram.wiring, plan)
+    else:
+        contraction = GpuContraction(CudaRel, diagram.wiring, target_bits=TARGET_BITS,
+                                     trials=args.trials, seed=0)
     return cnf, diagram, contraction
+
+
+class PlanView:
+    """The tree facts the CPU arm and the config need (steps, sliced wires, slice count,
+    cost), read from a plan without building a GPU contraction."""
+
+    def __init__(self, tree, sliced) -> None:
+        self.tree = tree
+        self.sliced_wires = tuple(sliced)
+        self.num_slices = 1 << len(self.sliced_wires)
+
+    def stats(self) -> dict:
+        tot, peak, _ = self.tree.cost(frozenset(self.sliced_wires))
+        return {"num_sliced": len(self.sliced_wires), "log2_index_space_per_slice": tot,
+                "peak_bits": peak}
+
+
+def reference_workload(args):
+    """Instance and tree of the CPU arm: the committed plan when it applies (no native
+    code is loaded), else the planner."""
+    from tensorsat_gb300 import planner
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    cnf = CNFInstance.random(3, N_VARS, N_CLAUSES, rng=args.seed)
+    plan = committed_plan(args)
+    if plan is not None:
+        tree, sliced = planner.plan_from_dict(plan)
+        return cnf, PlanView(tree, sliced)
+    _, _, contraction = build_workload(args)
+    return cnf, PlanView(contraction.tree, contraction.sliced_wires)
 
 
 # --------------------------------------------------------------------------------------
@@ -180,7 +239,7 @@ def run_reference(args) -> None:
         return
     cores = os.cpu_count() or 1
     pool = cpu_pool(cores)
-    cnf, _, contraction = build_workload(args.seed, args.trials)
+    cnf, contraction = reference_workload(args)
     ns = contraction.num_slices
     for w in range(args.warmup):
         cpu_sample(pool, cores, cnf, contraction, w * cores)
@@ -257,13 +316,20 @@ def run_gb300(args) -> None:
         dist.init_process_group("nccl")
     cores = os.cpu_count() or 1
     want_cpu = rank == 0 and world == 1 and not args.no_cpu_baseline
-    pool = cpu_pool(cores) if want_cpu else None  # spawn before the first CUDA call
+    want_batched = rank == 0 and world == 1 and not args.no_batched
 
     from tensorsat_gb300 import _native
     from tensorsat_gb300.contractions.gpu import PRIMES_31
 
-    lib = _native.lib()
-    cnf, diagram, contraction = build_workload(args.seed, args.trials)
+    lib = _native.lib()  # builds the library if needed, before the workers load it
+    # host work before the first CUDA call: spawned workers, the ragged batch's plans and
+    # DPLL counts
+    pool = cpu_pool(cores) if (want_cpu or want_batched) else None
+    ragged = None
+    if want_batched:
+        lo, hi = args.n_range
+        ragged = ragged_prepare(pool, args.instances, lo, hi)
+    cnf, diagram, contraction = build_workload(args)
     npl = contraction.native_plan()
     primes = PRIMES_31[:NUM_PRIMES]
     ns = contraction.num_slices
@@ -364,13 +430,45 @@ def run_gb300(args) -> None:
             e2e_times.append(time.perf_counter() - t0)
     e2e_value = world * group / ns / statistics.mean(e2e_times) if e2e_times else None
 
+    batched = None
+    if ragged is not None:
+        instances, trees, expected, plan_s = ragged
+        lo, hi = args.n_range
+        r = ragged_measure(instances, trees, expected, args.batched_steps, args.warmup,
+                           args.e2e_steps, local)
+        ratio = r["e2e_value"] / r["plain_value"] if r["e2e_value"] else None
+        batched = {
+            "metric": RAGGED_METRIC, "value": r["value"], "unit": UNIT,
+            "workload": ragged_workload_text(len(instances), lo, hi),
+            "form": f"captured CUDA graphs ({r['graphs']}: one per {RAGGED_CHUNK}-instance "
+                    f"chunk and ring) replayed, inputs resident",
+            "steps": args.batched_steps, "ms_per_step": statistics.mean(r["step_ms"]),
+            "plain": {"value": r["plain_value"], "unit": UNIT, "instances": len(instances),
+                      "form": "GpuContraction.count + contract per instance, host leaves "
+                              "uploaded and results read back by every call"},
+            "e2e": {"value": r["e2e_value"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": len(instances) * (4 * NUM_PRIMES + 1),
+                    "passes": r["e2e_passes"],
+                    "form": "BatchContraction.load + count/contract(graph=True): host leaves "
+                            "in, captured graphs replayed, counts and bits out"},
+            "e2e_uncaptured": {"value": r["uncaptured_value"], "unit": UNIT},
+            "batched_over_plain_e2e": ratio, "target_ratio": 1.5,
+            "meets_target": bool(ratio is not None and ratio >= 1.5),
+            "parity": f"counts and SAT bits of all {len(instances)} instances equal the "
+                      "oracle's DPLL counts in the plain, batched and served forms",
+            "planning_s": round(plan_s, 2), "planning_cores": cores,
+            "gpu_launches_per_pass": r["launches"], "clocks": r["clocks"],
+            "step_ms": [round(x, 3) for x in r["step_ms"]],
+        }
+
     cpu = None
     if want_cpu:
         dt, _ = cpu_sample(pool, cores, cnf, contraction, 0)
-        pool.close()
         cpu = {"value": cores / ns / dt, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{cores} slices of {ns} (one per process, exact-integer count + "
                          f"OR-AND bit per slice, numpy einsum), {dt:.1f} s"}
+    if pool is not None:
+        pool.close()
 
     if rank == 0:
         line = {
@@ -394,6 +492,7 @@ def run_gb300(args) -> None:
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(),
             "step_ms": [round(x, 3) for x in step_ms],
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -473,25 +572,23 @@ def ragged_plan_report(args, instances, trees, plan_s: float) -> None:
         "by_n": buckets}), flush=True)
 
 
-def run_ragged(args) -> None:
-    lo, hi = args.n_range
-    instances = ragged_instances(args.instances, lo, hi)
-    # planning is host work (tens of milliseconds per instance): spread it over the host cores
-    # in spawned processes, before this process touches CUDA. The planner calls the native
-    # library's host code: load (and if needed build) it here once, not in every worker.
-    from tensorsat_gb300 import _native
-
-    _native.lib()
-    t_plan = time.perf_counter()
+def ragged_prepare(pool, count: int, n_lo: int, n_hi: int):
+    """Instances, planner trees and DPLL counts of the ragged batch. Planning is host work
+    (tens of milliseconds per instance) spread over the host cores in spawned workers,
+    before the calling process touches CUDA."""
+    instances = ragged_instances(count, n_lo, n_hi)
     jobs = [(c.num_vars, c.clauses) for c in instances]
-    with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
-        trees = pool.map(_plan_instance, jobs, chunksize=4)
-        t_plan = time.perf_counter() - t_plan
-        if args.plan_only:
-            ragged_plan_report(args, instances, trees, t_plan)
-            return
-        expected = pool.map(_dpll_instance, jobs, chunksize=4)
+    t0 = time.perf_counter()
+    trees = pool.map(_plan_instance, jobs, chunksize=4)
+    plan_s = time.perf_counter() - t0
+    expected = pool.map(_dpll_instance, jobs, chunksize=4)
+    return instances, trees, expected, plan_s
 
+
+def ragged_measure(instances, trees, expected, steps: int, warmup: int, e2e_steps: int,
+                   device_index: int) -> dict:
+    """Times the ragged batch on the GPU in three forms and checks every answer against the
+    DPLL counts; returns the figures (instances/s) and the run's facts."""
     import torch
 
     from tensorsat_gb300 import _native
@@ -499,8 +596,7 @@ def run_ragged(args) -> None:
     from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
     from tensorsat_gb300.lang.cuda_rel import CudaRel
 
-    torch.cuda.set_device(0)
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", device_index)
     diagrams = [cnf.clause_diagram() for cnf in instances]
     primes = PRIMES_31[:NUM_PRIMES]
     chunks = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK],
@@ -523,34 +619,38 @@ def run_ragged(args) -> None:
         for g in graphs:
             g.replay()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    with ClockSampler(0) as clocks:
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    with ClockSampler(device_index) as clocks:
         ev[0].record(stream)
-        for k in range(args.steps):
+        for k in range(steps):
             step()
             ev[k + 1].record(stream)
         torch.cuda.synchronize()
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
-    value = len(instances) * args.steps / (sum(step_ms) / 1000.0)
+    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    value = len(instances) * steps / (sum(step_ms) / 1000.0)
     GpuContraction.check_device()
 
-    # plain form: one instance per call through the public API (count + SAT bit)
-    sample = min(len(diagrams), 64)
+    # plain form: one instance per call through the public API (count + SAT bit), host
+    # leaves uploaded by every call, the same instances
     plain = [GpuContraction(CudaRel, d.wiring, tree=t[0], sliced=t[1])
-             for d, t in zip(diagrams[:sample], trees)]
+             for d, t in zip(diagrams, trees)]
     for c, d in zip(plain[:4], diagrams[:4]):
         c.count(d, ring="modp", num_primes=NUM_PRIMES)
         bool(c.contract(d))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for c, d in zip(plain, diagrams[:sample]):
-        c.count(d, ring="modp", num_primes=NUM_PRIMES, cache_leaves=False)
-        bool(c.contract(d, cache_leaves=False))
+    plain_counts, plain_bits = [], []
+    for c, d in zip(plain, diagrams):
+        plain_counts.append(int(c.count(d, ring="modp", num_primes=NUM_PRIMES,
+                                        cache_leaves=False)))
+        plain_bits.append(bool(c.contract(d, cache_leaves=False)))
     torch.cuda.synchronize()
-    plain_value = sample / (time.perf_counter() - t0)
+    plain_value = len(plain) / (time.perf_counter() - t0)
+    if plain_counts != expected or plain_bits != [e > 0 for e in expected]:
+        raise RuntimeError("plain-form counts or SAT bits differ from the DPLL counts")
 
     # end to end, batched, uncaptured: host leaves in (uploaded again), one tsg_batch_run
     # per chunk and ring, counts and bits out
@@ -570,9 +670,8 @@ def run_ragged(args) -> None:
     # end to end, serving form: every chunk captures one graph per ring on its first call
     # (set-up, like planning); each timed pass copies every instance's host leaves into the
     # captured pools (pinned staging), replays the graphs and reads counts and bits back
-    serve = chunks
     serve_groups = []
-    for b in serve:
+    for b in chunks:
         gm = b.groups(_native.TSG_RING_MODP, NUM_PRIMES, budget)
         go = b.groups(_native.TSG_RING_OR_AND, 1, budget)
         need = max(b.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, gm),
@@ -585,12 +684,12 @@ def run_ragged(args) -> None:
     torch.cuda.synchronize()
     e2e_times = []
     h2d = 0
-    for k in range(args.e2e_steps + 1):
+    for k in range(e2e_steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         copied = 0
         served = []
-        for b, (gm, go), i in zip(serve, serve_groups, range(0, len(diagrams), RAGGED_CHUNK)):
+        for b, (gm, go), i in zip(chunks, serve_groups, range(0, len(diagrams), RAGGED_CHUNK)):
             copied += b.load(diagrams[i: i + RAGGED_CHUNK])
             served.append((b.count(num_primes=NUM_PRIMES, groups=gm, graph=True),
                            [bool(x) for x in b.contract(groups=go, graph=True)]))
@@ -601,33 +700,65 @@ def run_ragged(args) -> None:
             e2e_times.append(time.perf_counter() - t0)
         h2d = copied
     e2e_value = len(diagrams) / statistics.mean(e2e_times) if e2e_times else None
-    launches = sum(g.launches for g in graphs)
+    return {
+        "value": value, "step_ms": step_ms, "clocks": clocks.summary(),
+        "launches": sum(g.launches for g in graphs), "graphs": len(graphs),
+        "plain_value": plain_value, "uncaptured_value": uncaptured_value,
+        "e2e_value": e2e_value, "e2e_passes": len(e2e_times), "h2d": h2d,
+    }
+
+
+def ragged_workload_text(count: int, lo: int, hi: int) -> str:
+    return (f"ragged batch of {count} random 3-SAT instances, n uniform in [{lo}, {hi}], "
+            f"clause ratio uniform in [3.5, 5.0], seeded per instance")
+
+
+def run_ragged(args) -> None:
+    lo, hi = args.n_range
+    # The planner calls the native library's host code: load (and if needed build) it here
+    # once, not in every worker.
+    from tensorsat_gb300 import _native
+
+    _native.lib()
+    if args.plan_only:
+        instances = ragged_instances(args.instances, lo, hi)
+        jobs = [(c.num_vars, c.clauses) for c in instances]
+        t_plan = time.perf_counter()
+        with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
+            trees = pool.map(_plan_instance, jobs, chunksize=4)
+        ragged_plan_report(args, instances, trees, time.perf_counter() - t_plan)
+        return
+    with cpu_pool(max(1, min(os.cpu_count() or 1, 32))) as pool:
+        instances, trees, expected, _ = ragged_prepare(pool, args.instances, lo, hi)
+
+    import torch
+
+    torch.cuda.set_device(0)
+    r = ragged_measure(instances, trees, expected, args.steps, args.warmup, args.e2e_steps, 0)
     line = {
-        "metric": RAGGED_METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "metric": RAGGED_METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u32 residues mod 3 primes + u8 OR-AND",
+        "ms_per_step": statistics.mean(r["step_ms"]), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32 residues mod 3 primes + u8 OR-AND",
         "data": "synthetic (seeded CNFInstance.random per instance, no dataset)",
-        "config": {"workload": f"ragged batch of {len(instances)} random 3-SAT instances, n "
-                               f"uniform in [{lo}, {hi}], clause ratio uniform in [3.5, 5.0], "
-                               f"seeded per instance",
+        "config": {"workload": ragged_workload_text(len(instances), lo, hi),
                    "instances": len(instances), "n_range": [lo, hi],
-                   "graphs": len(graphs), "instances_per_graph": RAGGED_CHUNK,
+                   "graphs": r["graphs"], "instances_per_graph": RAGGED_CHUNK,
                    "l2": "not flushed: small instances are L2-resident by design"},
         "parity": f"counts and SAT bits of all {len(instances)} instances equal the "
-                  "oracle's DPLL counts",
-        "plain": {"value": plain_value, "unit": UNIT, "sample": sample,
+                  "oracle's DPLL counts (plain, batched and served forms)",
+        "plain": {"value": r["plain_value"], "unit": UNIT, "sample": len(instances),
                   "form": "GpuContraction.count + contract per instance"},
-        "e2e": ({"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": ({"value": r["e2e_value"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                  "d2h_bytes_per_step": len(instances) * (4 * NUM_PRIMES + 1),
                  "form": "BatchContraction.load + count/contract(graph=True) per chunk: "
                          "host leaves in, captured graphs replayed, counts and bits out",
-                 "passes": len(e2e_times)} if e2e_value is not None else None),
-        "e2e_uncaptured": {"value": uncaptured_value, "unit": UNIT,
+                 "passes": r["e2e_passes"]} if r["e2e_value"] is not None else None),
+        "e2e_uncaptured": {"value": r["uncaptured_value"], "unit": UNIT,
                            "form": "BatchContraction.count + contract per chunk, no graph"},
-        "gpu_launches": launches * args.steps,
-        "clocks": clocks.summary(),
-        "step_ms": [round(x, 3) for x in step_ms],
+        "gpu_launches": r["launches"] * args.steps,
+        "clocks": r["clocks"],
+        "step_ms": [round(x, 3) for x in r["step_ms"]],
     }
     print(json.dumps(line), flush=True)
 

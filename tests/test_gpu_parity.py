@@ -214,6 +214,24 @@ def test_assignment_search_reuses_one_plan(cuda):
     assert trace == kats["ksat4_n20_m195_rng1_assignment_search"]["trace"]
 
 
+def test_temporary_variants_do_not_share_a_cached_pool(cuda):
+    """One plan, leaf variants passed as unnamed temporaries in a loop: each freed
+    diagram's id may be reused by the next one, so the leaf-pool cache must not match on
+    ids. The SAT bits and counts of every variant equal brute force."""
+    cnf = CNFInstance.random(3, 12, 40, rng=5)
+    d = cnf.diagram()
+    c = GpuContraction(CudaRel, cnf.contraction_wiring())
+    specs = [f"{a:012b}" for a in range(0, 4096, 97)]
+    want = [orc.brute_force_count(12, list(cnf.clauses) + [(i + 1,) if b == "1" else (-(i + 1),)
+                                                       for i, b in enumerate(s)]) > 0
+            for s in specs]
+    assert any(want) and not all(want)
+    got = [bool(c.contract((cnf.inputs(s) >> d).flatten())) for s in specs]
+    assert got == want
+    counts = [c.count((cnf.inputs(s) >> d).flatten()) for s in specs]
+    assert counts == [int(w) for w in want]
+
+
 def test_sharp_sat_example(cuda):
     kats = _json("notebook_kats.json")["sharp_sat_example"]
     cnf = CNFInstance(3, [tuple(c) for c in kats["clauses"]])
