@@ -330,6 +330,8 @@ def run_gb300(args) -> None:
         lo, hi = args.n_range
         ragged = ragged_prepare(pool, args.instances, lo, hi)
     cnf, diagram, contraction = build_workload(args)
+    # the checker's exact count of the whole instance (DPLL, in a spawned worker)
+    dpll = pool.apply_async(_dpll_instance, ((cnf.num_vars, cnf.clauses),)) if pool else None
     npl = contraction.native_plan()
     primes = PRIMES_31[:NUM_PRIMES]
     ns = contraction.num_slices
@@ -430,6 +432,26 @@ def run_gb300(args) -> None:
             e2e_times.append(time.perf_counter() - t0)
     e2e_value = world * group / ns / statistics.mean(e2e_times) if e2e_times else None
 
+    # the whole instance: exact count and SAT bit over all slices, the slices sharded
+    # across the ranks (one all-reduce per ring combines the shares)
+    pg = dist.group.WORLD if dist else None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    full_count = contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES, group=group,
+                                   process_group=pg)
+    full_sat = bool(contraction.contract(diagram, group=group, process_group=pg))
+    torch.cuda.synchronize()
+    full_s = time.perf_counter() - t0
+    instance = {"count": int(full_count), "sat": full_sat, "seconds": round(full_s, 3),
+                "ranks": world, "form": "GpuContraction.count + contract over all "
+                f"{ns} slices, process_group={'WORLD' if pg else None}"}
+    if dpll is not None:
+        want = dpll.get(timeout=600)
+        instance["dpll_count"] = want
+        if full_count != want or full_sat != (want > 0):
+            raise RuntimeError(f"instance count {full_count} / SAT bit {full_sat} differ from "
+                               f"the DPLL count {want}")
+
     batched = None
     if ragged is not None:
         instances, trees, expected, plan_s = ragged
@@ -492,6 +514,7 @@ def run_gb300(args) -> None:
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(),
             "step_ms": [round(x, 3) for x in step_ms],
+            "instance": instance,
             "batched": batched,
         }
         print(json.dumps(line), flush=True)

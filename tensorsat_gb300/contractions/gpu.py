@@ -27,7 +27,7 @@ from typing import Any, Sequence
 import numpy as np
 import torch
 
-from .. import _device, _native, planner
+from .. import _device, _native, planner, sharding
 from ..diagrams import Diagram, TensorLikeType, Wiring
 from ..lang.cuda_rel import CudaRel, leaf_array
 from .abc import Contraction
@@ -548,18 +548,82 @@ class GpuContraction(Contraction):
     def contract(self, diagram: Diagram, *, progbar: bool = False, order: Any = None,
                  autojit: Any = "auto", group: int | None = None,
                  slice_range: tuple[int, int] | None = None,
-                 cache_leaves: bool = True) -> CudaRel:
+                 cache_leaves: bool = True, process_group: Any = None) -> CudaRel:
         """Validates and contracts the diagram in the OR-AND semiring; returns the result
         box (a scalar box for a SAT network: ``bool(box)`` is the SAT bit).
 
         ``slice_range`` restricts the run to slices ``[begin, end)`` (the OR of those
-        slices only); ``progbar``, ``order`` and ``autojit`` are accepted for signature
-        parity with ``CotengraContraction.contract`` and have no effect."""
+        slices only). With a ``torch.distributed`` ``process_group`` every rank of the
+        group contracts its own contiguous share of the slices and one all-reduce ORs the
+        shares, so every rank returns the whole result (see :meth:`shard_range`).
+        ``progbar``, ``order`` and ``autojit`` are accepted for signature parity with
+        ``CotengraContraction.contract`` and have no effect."""
         self.validate(diagram)
-        res = self.run(diagram, _native.TSG_RING_OR_AND, group=group, slice_range=slice_range,
+        if process_group is None:
+            res = self.run(diagram, _native.TSG_RING_OR_AND, group=group,
+                           slice_range=slice_range, cache_leaves=cache_leaves)
+            self.check_device()
+            return self._box_from_root(res)
+        group = self._shard_group(_native.TSG_RING_OR_AND, 1, group, process_group)
+        local = self.shard_range(slice_range, group, process_group)
+        entries = 1 << len(self._leaves.out_unique)
+        if local[0] < local[1]:
+            root = self._ring_root(diagram, _native.TSG_RING_OR_AND, (), local, group,
+                                   cache_leaves)
+        else:
+            root = np.zeros(entries, dtype=np.uint8)
+        root = sharding.allreduce_or(torch.from_numpy(root.astype(np.int32)).to(
+            sharding.collective_device(process_group)), group=process_group)
+        return self._box_from_root(torch.from_numpy(root.cpu().numpy().astype(np.uint8)))
+
+    # -- slices across ranks ------------------------------------------------------------
+
+    def shard_range(self, slice_range: tuple[int, int] | None, group: int,
+                    process_group: Any = None) -> tuple[int, int]:
+        """This rank's share of ``slice_range`` (default: every slice): with a process
+        group the range is split into contiguous pieces, one per rank in rank order, each
+        starting at a multiple of ``group`` (ranks launch whole slice groups); without one
+        the whole range. A share may be empty."""
+        b, e = slice_range if slice_range is not None else (0, self.num_slices)
+        if not 0 <= b <= e <= self.num_slices:
+            raise ValueError(f"slice range {(b, e)} outside [0, {self.num_slices}]")
+        if process_group is None:
+            return (b, e)
+        import torch.distributed as dist
+
+        if b % group:
+            raise ValueError("a sharded slice range must start at a multiple of the group")
+        world = dist.get_world_size(process_group)
+        rank = dist.get_rank(process_group)
+        lo, hi = sharding.slice_ranges(e - b, world, group)[rank]
+        return (b + lo, b + hi)
+
+    def _shard_group(self, ring: int, planes: int, group: int | None,
+                     process_group: Any) -> int:
+        """The slice group of a run; sharded runs agree on it before splitting (every
+        rank's share starts at a multiple of it), so it must be given or the same on every
+        rank: the default takes the smallest choice over the ranks."""
+        if group is not None or self.num_slices == 1:
+            return 1 if self.num_slices == 1 else group
+        g = self.choose_group(ring, planes)
+        if process_group is not None:
+            g = sharding.allreduce_min_int(g, process_group)
+        return g
+
+    def _ring_root(self, diagram: Diagram, ring: int, primes: Sequence[int],
+                   slice_range: tuple[int, int], group: int, cache_leaves: bool) -> np.ndarray:
+        """Root entries of one device run over ``slice_range``, on the host: uint8 [entries]
+        (OR-AND), uint64 [entries] (U64) or uint32 [planes, entries] (MODP, plain
+        residues). Raises if a kernel recorded a device-side failure."""
+        res = self.run(diagram, ring, primes=primes, group=group, slice_range=slice_range,
                        cache_leaves=cache_leaves)
         self.check_device()
-        return self._box_from_root(res)
+        host = res.cpu().numpy()
+        if ring == _native.TSG_RING_U64:
+            return host.view(np.uint64)
+        if ring == _native.TSG_RING_MODP:
+            return host.view(np.uint32).reshape(len(primes), -1)
+        return host
 
     def _box_from_root(self, res: torch.Tensor) -> CudaRel:
         """Result box from the OR-AND root entries (over the distinct out wires)."""
@@ -572,7 +636,7 @@ class GpuContraction(Contraction):
 
     def count(self, diagram: Diagram, *, ring: str = "auto", num_primes: int | None = None,
               group: int | None = None, slice_range: tuple[int, int] | None = None,
-              cache_leaves: bool = True) -> Any:
+              cache_leaves: bool = True, process_group: Any = None) -> Any:
         """Exact model count (``int``) of a closed network, or a numpy object array of
         counts indexed by the out wires.
 
@@ -580,7 +644,11 @@ class GpuContraction(Contraction):
         with CRT, ``"auto"`` picks u64 when the count bound is below 2^64 and otherwise
         enough primes for the bound. ``slice_range`` restricts the run to slices
         ``[begin, end)``: the result is then that range's share of the count (shares of
-        disjoint ranges add up to the count).
+        disjoint ranges add up to the count). With a ``torch.distributed``
+        ``process_group`` (one rank per GPU) every rank counts its own contiguous share
+        of the slices (:meth:`shard_range`) with no exchange while contracting, and one
+        all-reduce adds the shares (per prime mod p, or mod 2^64), so every rank returns
+        the whole count.
         """
         self.validate(diagram)
         arrays = []
@@ -592,13 +660,19 @@ class GpuContraction(Contraction):
         bound = count_bound_bits(self._wiring, arrays)
         if ring == "auto":
             ring = "u64" if bound < 64 else "modp"
+        entries = 1 << len(self._leaves.out_unique)
         if ring == "u64":
             if bound >= 64:
                 raise OverflowError("count bound exceeds 2^64: use ring='modp'")
-            res = self.run(diagram, _native.TSG_RING_U64, group=group, slice_range=slice_range,
-                           cache_leaves=cache_leaves)
-            self.check_device()
-            vals = res.cpu().numpy().view(np.uint64)
+            g = self._shard_group(_native.TSG_RING_U64, 1, group, process_group)
+            local = self.shard_range(slice_range, g, process_group)
+            if local[0] < local[1]:
+                vals = self._ring_root(diagram, _native.TSG_RING_U64, (), local, g,
+                                       cache_leaves)
+            else:
+                vals = np.zeros(entries, dtype=np.uint64)
+            if process_group is not None:
+                vals = sharding.allreduce_u64(vals, process_group)
             counts = np.array([int(v) for v in vals], dtype=object)
         elif ring == "modp":
             if num_primes is None:
@@ -612,13 +686,23 @@ class GpuContraction(Contraction):
                 raise OverflowError(
                     f"count bound 2^{bound:.0f} needs more than {num_primes} 31-bit primes"
                 )
+            g = self._shard_group(_native.TSG_RING_MODP, min(num_primes, _native.TSG_MAX_PRIMES),
+                                  group, process_group)
+            local = self.shard_range(slice_range, g, process_group)
             residues = []
             for i in range(0, num_primes, _native.TSG_MAX_PRIMES):
                 chunk = primes[i: i + _native.TSG_MAX_PRIMES]
-                res = self.run(diagram, _native.TSG_RING_MODP, primes=chunk, group=group,
-                               slice_range=slice_range, cache_leaves=cache_leaves)
-                self.check_device()
-                planes = res.cpu().numpy().view(np.uint32).reshape(len(chunk), -1)
+                if local[0] < local[1]:
+                    planes = self._ring_root(diagram, _native.TSG_RING_MODP, chunk, local, g,
+                                             cache_leaves)
+                else:
+                    planes = np.zeros((len(chunk), entries), dtype=np.uint32)
+                if process_group is not None:
+                    summed = sharding.allreduce_residues(
+                        torch.from_numpy(planes.astype(np.int64)).to(
+                            sharding.collective_device(process_group)),
+                        chunk, group=process_group)
+                    planes = summed.cpu().numpy()
                 residues.extend(planes[p] for p in range(len(chunk)))
             counts = crt(residues, primes)
         else:

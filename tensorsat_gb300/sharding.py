@@ -10,8 +10,9 @@ prime) or an OR (SAT bits) of a few words, done with one ``torch.distributed`` a
 
 from __future__ import annotations
 
-from typing import Sequence
+from typing import Any, Sequence
 
+import numpy as np
 import torch
 
 
@@ -60,3 +61,38 @@ def allreduce_or(bits: torch.Tensor, group=None) -> torch.Tensor:
     out = bits.to(torch.int32).clone()
     dist.all_reduce(out, op=dist.ReduceOp.MAX, group=group)
     return out
+
+
+def collective_device(group: Any = None) -> torch.device:
+    """Where a collective's tensors live: the current GPU for NCCL groups, the host for
+    Gloo."""
+    import torch.distributed as dist
+
+    if dist.get_backend(group) == "nccl":
+        return torch.device("cuda", torch.cuda.current_device())
+    return torch.device("cpu")
+
+
+def allreduce_u64(values: np.ndarray, group: Any = None) -> np.ndarray:
+    """All-reduces uint64 counts by their sum mod 2^64. Each value travels as two 32-bit
+    halves in int64 lanes (sums of halves over < 2^31 ranks cannot overflow), and the
+    halves are recombined on the host."""
+    import torch.distributed as dist
+
+    v = np.ascontiguousarray(values, dtype=np.uint64).reshape(-1)
+    halves = np.stack([(v & np.uint64(0xFFFFFFFF)).astype(np.int64),
+                       (v >> np.uint64(32)).astype(np.int64)])
+    t = torch.from_numpy(halves).to(collective_device(group))
+    dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    lo, hi = t.cpu().numpy()
+    return np.array([(int(a) + (int(b) << 32)) & 0xFFFFFFFFFFFFFFFF for a, b in zip(lo, hi)],
+                    dtype=np.uint64)
+
+
+def allreduce_min_int(value: int, group: Any = None) -> int:
+    """The smallest of one integer per rank (every rank gets it)."""
+    import torch.distributed as dist
+
+    t = torch.tensor([int(value)], dtype=torch.int64, device=collective_device(group))
+    dist.all_reduce(t, op=dist.ReduceOp.MIN, group=group)
+    return int(t.item())

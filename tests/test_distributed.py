@@ -42,33 +42,53 @@ def _worker(rank: int, world: int, port: int, q) -> None:
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
+        import numpy as np
+
         from oracle import finrel_oracle as orc
-        from tensorsat_gb300 import planner
-        from tensorsat_gb300.contractions.gpu import PRIMES_31
+        from tensorsat_gb300 import _native
+        from tensorsat_gb300.contractions.gpu import GpuContraction
+        from tensorsat_gb300.lang.cuda_rel import CudaRel
         from tensorsat_gb300.lib.sat import CNFInstance
 
         cnf = CNFInstance.random(3, 16, 66, rng=9)
-        wires = [tuple(dict.fromkeys(abs(l) - 1 for l in c)) for c in cnf.clauses]
-        net = planner.Network(wires, {w: 2 for w in range(16)}, ())
-        tree, sliced = planner.optimize(net, target_bits=5, trials=1, seed=0)
-        sliced = tuple(sorted(sliced))
-        ns = 1 << len(sliced)
-        b, e = slice_ranges(ns, world, 2)[rank]
-        part = 0
-        for sid in range(b, e):
-            fixed = {w: (sid >> j) & 1 for j, w in enumerate(sliced)}
-            part += orc.cnf_count_by_tree(16, cnf.clauses, tree.steps, fixed=fixed)
-        primes = PRIMES_31[:3]
-        res = torch.tensor([[part % p] for p in primes], dtype=torch.int64)
-        total = allreduce_residues(res, primes)
-        bit = allreduce_or(torch.tensor([1 if part else 0]))
-        if rank == 0:
-            q.put((int(total[0, 0]), int(bit[0]), orc.brute_force_count(16, cnf.clauses)))
+        d = cnf.clause_diagram()
+        c = GpuContraction(CudaRel, d.wiring, target_bits=5, trials=1)
+        steps, sliced = list(c.tree.steps), list(c.sliced_wires)
+        shares = []
+
+        def host_root(self, diagram, ring, primes, slice_range, group, cache_leaves):
+            # the device run of one rank's share, replaced by the oracle's contraction of
+            # the same slices along the same tree
+            shares.append(tuple(slice_range))
+            total = 0
+            for sid in range(*slice_range):
+                fixed = {w: (sid >> j) & 1 for j, w in enumerate(sliced)}
+                total += orc.cnf_count_by_tree(16, cnf.clauses, steps, "count", fixed=fixed)
+            if ring == _native.TSG_RING_MODP:
+                return np.array([[total % p] for p in primes], dtype=np.uint32)
+            if ring == _native.TSG_RING_U64:
+                return np.array([total % (1 << 64)], dtype=np.uint64)
+            return np.array([1 if total else 0], dtype=np.uint8)
+
+        GpuContraction._ring_root = host_root
+        pg = dist.group.WORLD
+        n_modp = c.count(d, ring="modp", num_primes=3, group=2, process_group=pg)
+        n_u64 = c.count(d, ring="u64", group=2, process_group=pg)
+        bit = bool(c.contract(d, group=2, process_group=pg))
+        half = c.count(d, ring="modp", num_primes=2, group=2,
+                       slice_range=(0, c.num_slices // 2), process_group=pg)
+        q.put((rank, n_modp, n_u64, bit, half, shares, c.num_slices,
+               orc.brute_force_count(16, cnf.clauses)))
     finally:
         dist.destroy_process_group()
 
 
 def test_two_rank_sharded_count_gloo():
+    """GpuContraction.count / .contract with a process group on two gloo CPU ranks: each
+    rank runs only its own contiguous, group-aligned share of the slices, and one
+    all-reduce per ring combines the shares into the exact count (mod primes with CRT,
+    mod 2^64) and the SAT bit on every rank. The device run of a share is replaced by the
+    oracle's contraction of the same slices (the GPU tests cover the device run)."""
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
@@ -79,6 +99,16 @@ def test_two_rank_sharded_count_gloo():
         p.join(timeout=240)
     for p in procs:
         assert p.exitcode == 0
-    total, bit, exp = q.get(timeout=10)
-    assert total == exp % 2147483647
-    assert bit == int(exp > 0)
+    got = sorted(q.get(timeout=10) for _ in range(2))
+    ns, exp = got[0][6], got[0][7]
+    assert exp > 0
+    for rank, n_modp, n_u64, bit, half, shares, _, _ in got:
+        assert n_modp == n_u64 == exp
+        assert bit is True
+        assert 0 <= half <= exp
+    assert got[0][4] == got[1][4]
+    # the two ranks' shares of each call tile the slices with no overlap
+    for call in range(4):
+        a, b = got[0][5][call], got[1][5][call]
+        assert a[0] == 0 and a[1] == b[0] and a[0] % 2 == 0 and b[0] % 2 == 0
+    assert got[1][5][0][1] == ns and got[1][5][3][1] == ns // 2
