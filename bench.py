@@ -388,7 +388,9 @@ def run_gb300(args) -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
     value = world * args.steps * group / ns / elapsed
-    launches_per_step = (npl.launch_count(*slice_range(0), group) * 2)
+    launches_per_step = (npl.launch_count(*slice_range(0), group, _native.TSG_RING_MODP,
+                                          NUM_PRIMES)
+                         + npl.launch_count(*slice_range(0), group, _native.TSG_RING_OR_AND))
 
     # Roofline of the dominant launch: one more pass over the next slice group with a CUDA
     # event after every launch (tsg_plan_run_timed); the tree step with the largest device
@@ -405,7 +407,12 @@ def run_gb300(args) -> None:
                                         ("or_and", _native.TSG_RING_OR_AND, (), ws_sat, res_sat)):
             ms = npl.run_timed(ring, pr, pool_dev, b, e, group, ws, res, False, sh)
             acc_ms[name] = ms if acc_ms[name] is None else [x + y for x, y in zip(acc_ms[name], ms)]
-    step_bytes = {"modp": sp.step_bytes_per_slice(4, NUM_PRIMES), "or_and": sp.step_bytes_per_slice(1, 1)}
+    # algorithmic bytes per step; a fused producer moves nothing, its consumer reads the
+    # producer's operands instead of the producer's result
+    fused = {"modp": npl.fused_steps(_native.TSG_RING_MODP, primes, group, contraction.tree),
+             "or_and": npl.fused_steps(_native.TSG_RING_OR_AND, (), group, contraction.tree)}
+    step_bytes = {"modp": sp.step_bytes_per_slice(4, NUM_PRIMES, fused["modp"]),
+                  "or_and": sp.step_bytes_per_slice(1, 1, fused["or_and"])}
     nsteps = len(step_bytes["modp"])
     ring_name, dom = max(((r, s) for r in acc_ms for s in range(nsteps)),
                          key=lambda rs: acc_ms[rs[0]][rs[1]])
@@ -414,7 +421,7 @@ def run_gb300(args) -> None:
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     step_total_ms = sum(sum(v) for v in acc_ms.values()) / timing_passes
     traffic = dominant_traffic(ring_name, dom, group)
-    step_roofline = (sp.bytes_per_slice(4, NUM_PRIMES) + sp.bytes_per_slice(1, 1)) * group / step_s / 1e9
+    step_roofline = (sum(step_bytes["modp"]) + sum(step_bytes["or_and"])) * group / step_s / 1e9
 
     # end to end through the public API: host leaves in, host results out, every step
     e2e_times = []

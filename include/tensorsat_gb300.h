@@ -147,9 +147,28 @@ TSG_API tsg_status tsg_plan_workspace_bytes(const tsg_plan* plan, int32_t ring, 
 /* Root output bits of the plan (the result tensor has 2^bits entries per plane). */
 TSG_API tsg_status tsg_plan_root_bits(const tsg_plan* plan, int32_t* bits_out);
 
-/* Number of kernel launches tsg_plan_run issues for the given slice range and group. */
+/* Number of kernel launches tsg_plan_run issues for the given slice range and group when
+ * no step is fused (the OR-AND ring, or fusion off); tsg_plan_launches counts them for a
+ * given ring. */
 TSG_API tsg_status tsg_plan_launch_count(const tsg_plan* plan, int64_t slice_begin,
                                  int64_t slice_end, int64_t group_size, int64_t* count_out);
+
+/* Number of kernel launches tsg_plan_run issues for these arguments (fused steps issue
+ * none of their own). Host only. */
+TSG_API tsg_status tsg_plan_launches(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                             int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                             int64_t* count_out);
+
+/* Fused steps, on (1, the default) or off (0), for plans whose layouts are made after the
+ * call (layouts are made per plan, ring and group on first use and kept). In the count
+ * rings a step whose large result is read once, as the reused operand of its consumer's
+ * tile form, is not launched: the consumer computes each entry it needs from the step's
+ * two operands, so the result never exists in HBM (it is written and read back otherwise;
+ * the conditions are in the library's choose_fusion). Results are identical either way;
+ * fused plans need less workspace and move fewer bytes. Process-wide. No counterpart in
+ * the reference, which runs one einsum per tree node (tensorsat/_autoray.py:31-62). */
+TSG_API tsg_status tsg_set_fusion(int32_t enabled);
+TSG_API int32_t tsg_fusion_enabled(void);
 
 /* Contracts slices [slice_begin, slice_end) of the plan, `group_size` slices per launch
  * group (a power of two; slice_begin must be a multiple of it, the last group may be
@@ -209,12 +228,16 @@ TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t
 #define TSG_KERNEL_GENERAL 0 /* one output entry per thread, bit-scatter offsets */
 #define TSG_KERNEL_TILE 1    /* tile kernel: V positions and NE enumerated outputs per thread */
 #define TSG_KERNEL_STREAM 2  /* streaming kernel: TMA-staged operands, persistent blocks */
+#define TSG_KERNEL_FUSED 3   /* fused kernel: a tile-form step that computes its reused operand
+                                from that operand's own two operands (see tsg_set_fusion) */
+#define TSG_KERNEL_NONE 4    /* no launch: the step's result is computed inside its consumer */
 
 /* For every tree step s, the kernel tsg_plan_run launches for it with these arguments
  * (the first slice group of size group_size, 1 <= group_size <= slices), as four int32
  * at kinds[4 s ...]: the family (TSG_KERNEL_*), then the template parameters V (tile
  * kernel: positions per thread, else 0), NE (enumerated output combinations per thread)
- * and NK (summed combinations unrolled at compile time; 0 = a runtime count). Builds and
+ * and NK (summed combinations unrolled at compile time; 0 = a runtime count); a step
+ * computed inside its consumer reports TSG_KERNEL_NONE and zeros. Builds and
  * bounds-checks every launch like tsg_plan_validate; touches no device memory and needs no
  * GPU. No counterpart in the reference, which contracts every step with one numpy einsum
  * (tensorsat/lang/fin_rel.py:276,283). */

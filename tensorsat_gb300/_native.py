@@ -32,6 +32,8 @@ TSG_MAX_PRIMES = 4
 TSG_KERNEL_GENERAL = 0
 TSG_KERNEL_TILE = 1
 TSG_KERNEL_STREAM = 2
+TSG_KERNEL_FUSED = 3
+TSG_KERNEL_NONE = 4
 
 EXPORTED_SYMBOLS = (
     "tsg_last_error",
@@ -59,6 +61,9 @@ EXPORTED_SYMBOLS = (
     "tsg_set_wait_limit_ns",
     "tsg_wait_limit_ns",
     "tsg_debug_stall_producer",
+    "tsg_plan_launches",
+    "tsg_set_fusion",
+    "tsg_fusion_enabled",
 )
 
 
@@ -142,6 +147,13 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_describe.restype = c_int32
     lib.tsg_plan_describe.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_int64,
                                       _i32p]
+    lib.tsg_plan_launches.restype = c_int32
+    lib.tsg_plan_launches.argtypes = [c_void_p, c_int32, c_int32, c_int64, c_int64, c_int64,
+                                      _i64p]
+    lib.tsg_set_fusion.restype = c_int32
+    lib.tsg_set_fusion.argtypes = [c_int32]
+    lib.tsg_fusion_enabled.restype = c_int32
+    lib.tsg_fusion_enabled.argtypes = []
     lib.tsg_set_wait_limit_ns.restype = c_int32
     lib.tsg_set_wait_limit_ns.argtypes = [ctypes.c_uint64]
     lib.tsg_wait_limit_ns.restype = ctypes.c_uint64

@@ -227,7 +227,7 @@ class BatchContraction:
         with torch.cuda.graph(graph):
             args = self._call(ring, primes, groups, ws, results,
                               torch.cuda.current_stream(dev).cuda_stream)
-        launches = sum(c.native_plan().launch_count(0, c.num_slices, g)
+        launches = sum(c.native_plan().launch_count(0, c.num_slices, g, ring, max(1, planes))
                        for c, g in zip(self._contractions, groups))
         return BatchGraph(graph, results, list(groups), launches,
                           [ws, self.pools(), args, list(primes)])

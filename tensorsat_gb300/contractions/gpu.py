@@ -256,11 +256,33 @@ class NativePlan:
                                                          _native.ctypes.byref(out)))
         return int(out.value)
 
-    def launch_count(self, begin: int, end: int, group: int) -> int:
+    def launch_count(self, begin: int, end: int, group: int, ring: int | None = None,
+                     num_primes: int = 1) -> int:
+        """Kernel launches of one run over slices [begin, end); with ``ring`` the exact
+        count for that ring (fused steps launch nothing), else every step's launch."""
         out = _native.c_int64()
-        _native.check(self._lib.tsg_plan_launch_count(self.handle, begin, end, group,
-                                                      _native.ctypes.byref(out)))
+        if ring is None:
+            _native.check(self._lib.tsg_plan_launch_count(self.handle, begin, end, group,
+                                                          _native.ctypes.byref(out)))
+        else:
+            _native.check(self._lib.tsg_plan_launches(self.handle, ring, num_primes, begin,
+                                                      end, group, _native.ctypes.byref(out)))
         return int(out.value)
+
+    def fused_steps(self, ring: int, primes: Sequence[int], group: int,
+                    tree: planner.ContractionTree) -> dict[int, int]:
+        """{consumer step: producer step} of the steps a run in ``ring`` fuses (the
+        producer is computed inside its consumer and never stored)."""
+        kinds = self.describe(ring, primes, group)
+        L = tree.num_leaves
+        out = {}
+        for s, k in enumerate(kinds):
+            if int(k[0]) != _native.TSG_KERNEL_FUSED:
+                continue
+            for x in tree.steps[s]:
+                if x >= L and int(kinds[x - L][0]) == _native.TSG_KERNEL_NONE:
+                    out[s] = x - L
+        return out
 
     def describe(self, ring: int, primes: Sequence[int], group: int) -> np.ndarray:
         """(steps, 4) int32: per tree step the kernel family (``TSG_KERNEL_*``) and its

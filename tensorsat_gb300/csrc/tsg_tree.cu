@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <type_traits>
 #include <map>
@@ -39,6 +40,9 @@ __device__ int g_device_error = 0;  // 0 = ok, else TSG_ERR_TIMEOUT
 // and the producer stall of tsg_debug_stall_producer (< 0: off). Read at every launch.
 std::atomic<uint64_t> g_wait_limit_ns{kWaitLimitNs};
 std::atomic<int64_t> g_stall_after{-1};
+
+// Fused steps (tsg_set_fusion): on by default; read when a layout is made.
+std::atomic<int> g_fusion{1};
 
 // Address of g_device_error on the current device (looked up once per device).
 tsg_status device_error_address(int** out) {
@@ -78,8 +82,12 @@ struct Layout {
   int64_t group;
   int64_t elem_bytes;
   int planes;
+  bool fusion;                  // fused steps enabled when the layout was made
   std::vector<int64_t> offset;  // byte offset of each step's output in the workspace
+                                // (-1: computed inside its consumer, never stored)
   std::vector<int64_t> plane;   // plane stride (elements) of each step's output
+  std::vector<int> fused_from;  // step whose result this step computes itself, or -1
+  std::vector<char> fused_away; // the step is computed inside its consumer (no launch)
   int64_t bytes;
 };
 
@@ -178,10 +186,73 @@ tsg_status elem_info(int32_t ring, int32_t num_primes, int64_t* elem_bytes, int*
   }
 }
 
+// Live (unsliced) bits of operand v: a leaf's rank less its sliced bits, or a step's
+// output bits.
+int live_bits(const tsg_plan* plan, int v) {
+  if (v < 0) return plan->steps[-v - 1].out_bits;
+  const LeafInfo& lf = plan->leaves[v];
+  int r = lf.rank;
+  for (int p : lf.spos)
+    if (p >= 0) r--;
+  return r;
+}
+
+// Fused steps of a layout (count rings only): a step p whose result P is read by exactly
+// one consumer s is computed inside s, never stored, when
+//   - P carries every output bit of s but at most two (the enumerated E bits of s's tile
+//     form, so each entry of P is computed once per launch) and at least as many output
+//     bits as s's other operand (P is the operand the tile form reuses across E);
+//   - s sums at most 2 bits and p at most 1 (the fused kernel's instantiations), s has at
+//     least two F bits (4 positions per thread) and at most 30 output bits, every tensor
+//     involved has at most 31 bits, and both steps depend on the slice alike;
+//   - P expands its operands: 2^bits(P) >= 2^16 and >= 4 x (entries of A + entries of B);
+//   - neither p's operands nor s take part in another fusion (decided in step order).
+// Returns fused_from[s] = p or -1.
+std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem_bytes) {
+  const auto& steps = plan->steps;
+  const int ns = (int)steps.size();
+  std::vector<int> fused_from(ns, -1);
+  std::vector<char> away(ns, 0);
+  if (elem_bytes == 1 || group > 65535) return fused_from;  // OR-AND: no fused kernel
+  auto rank_ok = [&](int v) {
+    return v >= 0 ? plan->leaves[v].rank <= 31 : steps[-v - 1].out_bits <= 31;
+  };
+  for (int s = 0; s < ns; ++s) {
+    const StepInfo& cs = steps[s];
+    if (away[s] || fused_from[s] >= 0) continue;
+    if (cs.k_bits > 2 || cs.out_bits > 30 || cs.out_bits < 2) continue;
+    for (int xo = 0; xo < 2; ++xo) {
+      const int v = cs.op[xo];
+      if (v >= 0) continue;
+      const int p = -v - 1;
+      const StepInfo& ps = steps[p];
+      if (ps.dep != cs.dep || ps.k_bits > 1 || fused_from[p] >= 0) continue;
+      if (ps.out_bits < 16) continue;
+      if (!rank_ok(ps.op[0]) || !rank_ok(ps.op[1]) || !rank_ok(cs.op[1 - xo])) continue;
+      int carried[2] = {0, 0};
+      for (int o = 0; o < 2; ++o)
+        for (int i = 0; i < cs.out_bits; ++i) carried[o] += cs.pos[o][i] >= 0;
+      const int ne_bits = cs.out_bits - carried[xo];
+      if (ne_bits > 2 || cs.out_bits - ne_bits < 2) continue;
+      if (carried[xo] < carried[1 - xo] || (carried[xo] == carried[1 - xo] && xo != 0)) continue;
+      const double pe = std::ldexp(1.0, ps.out_bits);
+      const double ab = std::ldexp(1.0, live_bits(plan, ps.op[0])) +
+                        std::ldexp(1.0, live_bits(plan, ps.op[1]));
+      if (pe < 4.0 * ab) continue;
+      fused_from[s] = p;
+      away[p] = 1;
+      break;
+    }
+  }
+  return fused_from;
+}
+
 tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int planes,
                       const Layout** out) {
+  const bool fusion = g_fusion.load(std::memory_order_relaxed) != 0;
   for (const Layout& l : plan->layouts) {
-    if (l.group == group && l.elem_bytes == elem_bytes && l.planes == planes) {
+    if (l.group == group && l.elem_bytes == elem_bytes && l.planes == planes &&
+        l.fusion == fusion) {
       *out = &l;
       return TSG_OK;
     }
@@ -192,8 +263,13 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
   lay.group = group;
   lay.elem_bytes = elem_bytes;
   lay.planes = planes;
+  lay.fusion = fusion;
   lay.offset.assign(ns, -1);
   lay.plane.assign(ns, 0);
+  lay.fused_from = fusion ? choose_fusion(plan, group, elem_bytes) : std::vector<int>(ns, -1);
+  lay.fused_away.assign(ns, 0);
+  for (int s = 0; s < ns; ++s)
+    if (lay.fused_from[s] >= 0) lay.fused_away[lay.fused_from[s]] = 1;
   std::vector<int64_t> bytes(ns, 0);
   for (int s = 0; s < ns; ++s) {
     const int64_t slices = steps[s].dep ? group : 1;
@@ -206,20 +282,26 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
     bytes[s] = align256(elems * elem_bytes * planes);
   }
   Arena arena;
-  // prologue: slice-independent steps; then one group of slice-dependent steps.
+  // prologue: slice-independent steps; then one group of slice-dependent steps. A fused
+  // step gets no buffer; its operands stay live until its consumer has run.
+  auto release_operands = [&](int s, int r) {
+    for (int o = 0; o < 2; ++o) {
+      const int v = steps[r].op[o];
+      if (v >= 0) continue;
+      const int x = -v - 1;
+      if (lay.fused_away[x]) continue;
+      // an independent result read by a dependent step is re-read by every group
+      if (!steps[x].dep && steps[s].dep) continue;
+      arena.release(lay.offset[x], bytes[x]);
+    }
+  };
   for (int phase = 0; phase < 2; ++phase) {
     for (int s = 0; s < ns; ++s) {
-      if (steps[s].dep != (phase == 1)) continue;
+      if (steps[s].dep != (phase == 1) || lay.fused_away[s]) continue;
       lay.offset[s] = arena.alloc(bytes[s]);
       arena.note();
-      for (int o = 0; o < 2; ++o) {
-        const int v = steps[s].op[o];
-        if (v >= 0) continue;
-        const int x = -v - 1;
-        // an independent result read by a dependent step is re-read by every group
-        if (!steps[x].dep && steps[s].dep) continue;
-        arena.release(lay.offset[x], bytes[x]);
-      }
+      release_operands(s, s);
+      if (lay.fused_from[s] >= 0) release_operands(s, lay.fused_from[s]);
     }
   }
   lay.bytes = std::max<int64_t>(arena.peak(), 256);
@@ -357,7 +439,7 @@ OperandDesc describe_operand(const RunCtx& c, const StepInfo& st, int o, int64_t
   } else {
     const int x = -v - 1;
     const StepInfo& xs = plan->steps[x];
-    d.ptr = c.ws ? c.ws + c.lay->offset[x] : nullptr;
+    d.ptr = (c.ws && c.lay->offset[x] >= 0) ? c.ws + c.lay->offset[x] : nullptr;
     d.plane = (uint64_t)c.lay->plane[x];
     if (xs.dep)
       for (int j = 0; j < gb; ++j) d.gp.push_back({j, xs.out_bits + j});
@@ -401,10 +483,110 @@ uint64_t scatter_pairs(const std::vector<std::pair<int, int>>& pairs, uint64_t x
 }
 
 
+// Index bits of a tile form: the F bits (threads and tiles, fastest first) and the E bits
+// (enumerated inside a thread) of the step's output.
+struct TileBits {
+  std::vector<int> fbits, ebits;
+};
+
+// Fills the tile operand `op` of an operand whose output-bit positions are pos[0 ..
+// out_bits) (-1: not carried) and whose summed, slot and constant terms are in `d`;
+// sets *ok = false when the operand is outside what the tile kernel handles.
+tsg_status fill_tile_operand(TileOperand& op, const int* pos, const OperandDesc& d,
+                             const uint8_t* ptr, const TileBits& tb, int tile_bits, int v,
+                             int n_k, int ring, bool* ok) {
+  const std::vector<int>& fbits = tb.fbits;
+  const std::vector<int>& ebits = tb.ebits;
+  const int nf = (int)fbits.size();
+  const int ne = 1 << ebits.size();
+  op.ptr = ptr;
+  op.base = d.base;
+  op.plane = d.plane;
+  op.leaf = d.leaf ? 1 : 0;
+  std::vector<std::pair<int, int>> lo, hi, ep;
+  for (int fi = 0; fi < nf; ++fi) {
+    const int p = pos[fbits[fi]];
+    if (p >= 0) (fi < tile_bits ? lo : hi).push_back({fi, p});
+  }
+  for (size_t b = 0; b < ebits.size(); ++b) {
+    const int p = pos[ebits[b]];
+    if (p >= 0) ep.push_back({(int)b, p});
+  }
+  TSG_TRY(make_narrow(lo, &op.f_lo, ok));
+  if (*ok) TSG_TRY(make_narrow(hi, &op.f_hi, ok));
+  for (const auto& pr : d.kp)
+    if (pr.second >= 32) *ok = false;
+  if (!*ok) return TSG_OK;
+  TSG_TRY(make_bitmap(d.gp, &op.g));
+  bool contig = v >= 4, bcast = true;
+  for (int j = 0; j < v; ++j) {
+    op.tab[j] = (uint32_t)scatter_pairs(lo, j);
+    contig = contig && op.tab[j] == (uint32_t)j;
+    bcast = bcast && op.tab[j] == 0;
+  }
+  // vector loads need every start offset to be a multiple of V elements: the fastest
+  // output bits occupy the operand's fastest bits, so only the constant part can break
+  // that (leaf offsets are the caller's; workspace buffers are 256-byte aligned)
+  if (contig && (op.base & (uint64_t)(v - 1)) != 0) contig = false;
+  op.mode = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
+  if (op.mode == kModeGather && v == 4) {
+    // exactly two distinct offsets, 0 and tab[3] (one of the two fastest output bits)
+    bool pair = op.tab[0] == 0 && op.tab[3] != 0;
+    int sel = 0;
+    for (int j = 0; j < v && pair; ++j) {
+      if (op.tab[j] == op.tab[3]) sel |= 1 << j;
+      else if (op.tab[j] != 0) pair = false;
+    }
+    if (pair) {
+      op.mode = kModePair;
+      op.pair_sel = sel;
+    }
+  }
+  if (op.mode == kModeGather && v == 4 && !op.leaf && ring != TSG_RING_OR_AND &&
+      op.tab[0] == 0 && op.tab[1] == 1 && op.tab[2] != 0 && op.tab[3] == op.tab[2] + 1 &&
+      (op.tab[2] & 1) == 0 && (op.base & 1) == 0)
+    op.mode = kModeDual;  // alignment of the pairs is proven in check_tile_bounds
+  if (op.mode == kModeGather && v == 16) {
+    // carried fast F bits (F index, operand bit), ascending F index: distinct value d
+    // has bit k of d = carried bit k of the position
+    std::vector<std::pair<int, int>> cb;
+    for (const auto& pr : lo)
+      if (pr.first < 4) cb.push_back(pr);
+    if (cb.empty() || cb.size() > 3) {
+      *ok = false;  // excluded by the choice of V
+      return TSG_OK;
+    }
+    op.mode = kModePerm;
+    op.pn = 1 << cb.size();
+    for (int dd = 0; dd < op.pn; ++dd) {
+      uint32_t off = 0;
+      for (size_t k = 0; k < cb.size(); ++k)
+        if ((dd >> k) & 1) off |= 1u << cb[k].second;
+      op.dtab[dd] = off;
+    }
+    for (int i = 0; i < 4; ++i) {
+      uint32_t sel = 0;
+      for (int t = 0; t < 4; ++t) {
+        const int j = 4 * i + t;
+        uint32_t dd = 0;
+        for (size_t k = 0; k < cb.size(); ++k) dd |= (uint32_t)((j >> cb[k].first) & 1) << k;
+        sel |= dd << (4 * t);
+      }
+      op.psel[i] = sel;
+    }
+  }
+  op.has_e = ep.empty() ? 0 : 1;
+  for (int e = 0; e < ne; ++e) op.e_off[e] = (uint32_t)scatter_pairs(ep, e);
+  for (int kk = 0; kk < n_k; ++kk) op.k_off[kk] = (uint32_t)scatter_pairs(d.kp, kk);
+  return TSG_OK;
+}
+
 // Builds the tile form of step s from the operand descriptions; sets *ok = false when the
-// step is outside what the tile kernel handles (it then runs the general kernel).
+// step is outside what the tile kernel handles (it then runs the general kernel). The
+// chosen F and E bits go to *bits_out when given.
 tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs& a,
-                      uint64_t cnt, int ring, TileArgs* t, TileShape* shape, bool* ok) {
+                      uint64_t cnt, int ring, TileArgs* t, TileShape* shape, bool* ok,
+                      TileBits* bits_out = nullptr) {
   std::memset(t, 0, sizeof(*t));
   *ok = st.out_bits <= 30 && st.k_bits <= 4 && cnt <= 65535;
   if (!*ok) return TSG_OK;
@@ -413,7 +595,9 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   for (int o = 0; o < 2; ++o)
     for (const auto& pr : d[o].tp) carried[o]++;
   const int big = carried[0] >= carried[1] ? 0 : 1;
-  std::vector<int> ebits, fbits;
+  TileBits tb;
+  std::vector<int>& ebits = tb.ebits;
+  std::vector<int>& fbits = tb.fbits;
   {
     std::vector<int> cand;
     for (int i = 0; i < st.out_bits; ++i)
@@ -480,87 +664,11 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   t->o_contig = ocontig ? 1 : 0;
   for (int e = 0; e < ne; ++e) t->o_e[e] = (uint32_t)scatter_pairs(oe, e);
   for (int o = 0; o < 2; ++o) {
-    TileOperand& op = t->op[o];
-    op.ptr = o == 0 ? a.lhs : a.rhs;
-    op.base = d[o].base;
-    op.plane = d[o].plane;
-    op.leaf = d[o].leaf ? 1 : 0;
-    std::vector<std::pair<int, int>> lo, hi, ep;
-    for (int fi = 0; fi < nf; ++fi) {
-      const int p = st.pos[o][fbits[fi]];
-      if (p >= 0) (fi < tile_bits ? lo : hi).push_back({fi, p});
-    }
-    for (size_t b = 0; b < ebits.size(); ++b) {
-      const int p = st.pos[o][ebits[b]];
-      if (p >= 0) ep.push_back({(int)b, p});
-    }
-    TSG_TRY(make_narrow(lo, &op.f_lo, ok));
-    if (*ok) TSG_TRY(make_narrow(hi, &op.f_hi, ok));
-    for (const auto& pr : d[o].kp)
-      if (pr.second >= 32) *ok = false;
+    TSG_TRY(fill_tile_operand(t->op[o], st.pos[o], d[o], o == 0 ? a.lhs : a.rhs, tb,
+                              tile_bits, v, t->n_k, ring, ok));
     if (!*ok) return TSG_OK;
-    TSG_TRY(make_bitmap(d[o].gp, &op.g));
-    bool contig = v >= 4, bcast = true;
-    for (int j = 0; j < v; ++j) {
-      op.tab[j] = (uint32_t)scatter_pairs(lo, j);
-      contig = contig && op.tab[j] == (uint32_t)j;
-      bcast = bcast && op.tab[j] == 0;
-    }
-    // vector loads need every start offset to be a multiple of V elements: the fastest
-    // output bits occupy the operand's fastest bits, so only the constant part can break
-    // that (leaf offsets are the caller's; workspace buffers are 256-byte aligned)
-    if (contig && (op.base & (uint64_t)(v - 1)) != 0) contig = false;
-    op.mode = contig ? kModeContig : (bcast ? kModeBcast : kModeGather);
-    if (op.mode == kModeGather && v == 4) {
-      // exactly two distinct offsets, 0 and tab[3] (one of the two fastest output bits)
-      bool pair = op.tab[0] == 0 && op.tab[3] != 0;
-      int sel = 0;
-      for (int j = 0; j < v && pair; ++j) {
-        if (op.tab[j] == op.tab[3]) sel |= 1 << j;
-        else if (op.tab[j] != 0) pair = false;
-      }
-      if (pair) {
-        op.mode = kModePair;
-        op.pair_sel = sel;
-      }
-    }
-    if (op.mode == kModeGather && v == 4 && !op.leaf && ring != TSG_RING_OR_AND &&
-        op.tab[0] == 0 && op.tab[1] == 1 && op.tab[2] != 0 && op.tab[3] == op.tab[2] + 1 &&
-        (op.tab[2] & 1) == 0 && (op.base & 1) == 0)
-      op.mode = kModeDual;  // alignment of the pairs is proven in check_tile_bounds
-    if (op.mode == kModeGather && v == 16) {
-      // carried fast F bits (F index, operand bit), ascending F index: distinct value d
-      // has bit k of d = carried bit k of the position
-      std::vector<std::pair<int, int>> cb;
-      for (const auto& pr : lo)
-        if (pr.first < 4) cb.push_back(pr);
-      if (cb.empty() || cb.size() > 3) {
-        *ok = false;  // excluded by the choice of V above
-        return TSG_OK;
-      }
-      op.mode = kModePerm;
-      op.pn = 1 << cb.size();
-      for (int dd = 0; dd < op.pn; ++dd) {
-        uint32_t off = 0;
-        for (size_t k = 0; k < cb.size(); ++k)
-          if ((dd >> k) & 1) off |= 1u << cb[k].second;
-        op.dtab[dd] = off;
-      }
-      for (int i = 0; i < 4; ++i) {
-        uint32_t sel = 0;
-        for (int t = 0; t < 4; ++t) {
-          const int j = 4 * i + t;
-          uint32_t dd = 0;
-          for (size_t k = 0; k < cb.size(); ++k) dd |= (uint32_t)((j >> cb[k].first) & 1) << k;
-          sel |= dd << (4 * t);
-        }
-        op.psel[i] = sel;
-      }
-    }
-    op.has_e = ep.empty() ? 0 : 1;
-    for (int e = 0; e < ne; ++e) op.e_off[e] = (uint32_t)scatter_pairs(ep, e);
-    for (int kk = 0; kk < t->n_k; ++kk) op.k_off[kk] = (uint32_t)scatter_pairs(d[o].kp, kk);
   }
+  if (bits_out) *bits_out = tb;
   return TSG_OK;
 }
 
@@ -753,6 +861,118 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   la.streamed = true;
 }
 
+// Bounds of one operand read through a tile operand: the largest offset its terms can
+// form (slot, tile, thread, V position, E, summed and extra terms) must stay inside
+// [lo_ext, hi_ext), and a vector-read operand's terms must keep V-element alignment.
+tsg_status check_operand_tile(const TileOperand& op, const TileArgs& t, const TileShape& sh,
+                              uint64_t cnt, uint32_t extra_max,
+                              const std::vector<uint32_t>& extra_terms, uint64_t lo_ext,
+                              uint64_t hi_ext) {
+  const int gbits = bit_width(cnt - 1);
+  const int nbits = bit_width(sh.tiles - 1) + t.tile_bits;
+  const int vbits = sh.v == 16 ? 4 : (sh.v == 4 ? 2 : 0);
+  uint32_t tab = 0, eo = 0, ko = 0;
+  for (int j = 0; j < sh.v; ++j) tab = std::max(tab, op.tab[j]);
+  for (int e = 0; e < sh.ne; ++e) eo = std::max(eo, op.e_off[e]);
+  for (int kk = 0; kk < t.n_k; ++kk) ko = std::max(ko, op.k_off[kk]);
+  const uint64_t hi = op.base + scatter_max(op.g, gbits) + narrow_max(op.f_hi, nbits) +
+                      narrow_max(op.f_lo, t.tile_bits, vbits) + tab + eo + ko + extra_max;
+  if (op.base < lo_ext || hi >= hi_ext)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "fused bounds: operand offset outside its tensor");
+  if (op.mode == kModeContig && sh.v > 1) {
+    const uint32_t vmask = (uint32_t)sh.v - 1;
+    bool good = (op.base & vmask) == 0 && (op.plane & vmask) == 0;
+    for (int i = 0; i < op.g.n; ++i) good = good && op.g.dst[i] >= vbits;
+    for (const NarrowMap* m : {&op.f_hi, &op.f_lo})
+      for (int i = 0; i < m->n; ++i) good = good && !(m->dst[i] < vbits && m->src[i] >= vbits);
+    for (int j = 0; j < sh.v; ++j) good = good && op.tab[j] == (uint32_t)j;
+    for (int e = 0; e < sh.ne; ++e) good = good && (op.e_off[e] & vmask) == 0;
+    for (int kk = 0; kk < t.n_k; ++kk) good = good && (op.k_off[kk] & vmask) == 0;
+    for (uint32_t x : extra_terms) good = good && (x & vmask) == 0;
+    if (!good) return fail(TSG_ERR_INVALID_ARGUMENT, "fused bounds: vector load not aligned");
+  }
+  if (op.mode == kModeDual && sh.v == 4) {
+    bool good = (op.base & 1) == 0 && (op.plane & 1) == 0 && (op.tab[2] & 1) == 0 &&
+                op.tab[1] == 1;
+    for (int i = 0; i < op.g.n; ++i) good = good && op.g.dst[i] >= 1;
+    for (const NarrowMap* m : {&op.f_hi, &op.f_lo})
+      for (int i = 0; i < m->n; ++i) good = good && !(m->dst[i] < 1 && m->src[i] >= 1);
+    for (int e = 0; e < sh.ne; ++e) good = good && (op.e_off[e] & 1) == 0;
+    for (int kk = 0; kk < t.n_k; ++kk) good = good && (op.k_off[kk] & 1) == 0;
+    for (uint32_t x : extra_terms) good = good && (x & 1) == 0;
+    if (!good)
+      return fail(TSG_ERR_INVALID_ARGUMENT, "fused bounds: paired vector load not aligned");
+  }
+  return TSG_OK;
+}
+
+// Fused form of consumer step s, whose operand P (the result of step p, never stored) is
+// computed from p's operands A and B: their tile operands are built in s's index space by
+// composing s's map onto P with p's maps onto A and B; p's summed bits become the extra
+// offsets kp_off. Checks every offset on the host like the other launch forms.
+tsg_status build_fused(const RunCtx& c, int s, int64_t base, const TileBits& tb,
+                       LaunchArgs* la) {
+  const tsg_plan* plan = c.plan;
+  const StepInfo& st = plan->steps[s];
+  const int p = c.lay->fused_from[s];
+  const StepInfo& ps = plan->steps[p];
+  int xo = -1;
+  for (int o = 0; o < 2; ++o)
+    if (st.op[o] == -p - 1) xo = o;
+  const TileShape& sh = la->shape;
+  if (xo < 0 || sh.v != 4 || (sh.nk != 1 && sh.nk != 2 && sh.nk != 4) || ps.k_bits > 1 ||
+      la->t.op[xo].has_e)
+    return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused step outside the fused kernel");
+  FusedArgs& f = la->f;
+  std::memset(&f, 0, sizeof(f));
+  f.fx = xo;
+  la->nkp = 1 << ps.k_bits;
+  for (int o = 0; o < 2; ++o) {
+    const OperandDesc dp = describe_operand(c, ps, o, base);
+    // A's bit of the consumer's output bit i: P bit j = st.pos[xo][i] is p's output bit j
+    int pos[TSG_MAX_BITS];
+    for (int i = 0; i < st.out_bits; ++i) {
+      const int j = st.pos[xo][i];
+      pos[i] = j >= 0 ? ps.pos[o][j] : -1;
+    }
+    OperandDesc dc;
+    dc.base = dp.base;
+    dc.ptr = dp.ptr;
+    dc.plane = dp.plane;
+    dc.leaf = dp.leaf;
+    dc.gp = dp.gp;
+    for (int m = 0; m < st.k_bits; ++m) {
+      const int j = st.pos[xo][st.out_bits + m];
+      if (j >= 0 && ps.pos[o][j] >= 0) dc.kp.push_back({m, ps.pos[o][j]});
+    }
+    bool ok = true;
+    TSG_TRY(fill_tile_operand(f.op[o], pos, dc, dp.ptr, tb, la->t.tile_bits, sh.v,
+                              la->t.n_k, c.ring, &ok));
+    if (!ok || f.op[o].has_e)
+      return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused operand outside the tile kernel");
+    std::vector<uint32_t> extra;
+    uint32_t extra_max = 0;
+    for (int kp = 0; kp < la->nkp; ++kp) {
+      uint32_t off = 0;
+      for (int m = 0; m < ps.k_bits; ++m) {
+        const int q = ps.pos[o][ps.out_bits + m];
+        if (q >= 0 && ((kp >> m) & 1)) off |= 1u << q;
+      }
+      f.kp_off[o][kp] = off;
+      extra.push_back(off);
+      extra_max = std::max(extra_max, off);
+    }
+    const int v = ps.op[o];
+    const uint64_t lo_ext = dp.leaf ? (uint64_t)plan->leaves[v].offset : 0;
+    const uint64_t hi_ext = dp.leaf ? lo_ext + (1ull << plan->leaves[v].rank)
+                                    : (uint64_t)c.lay->plane[-v - 1];
+    TSG_TRY(check_operand_tile(f.op[o], la->t, sh, la->cnt, extra_max, extra, lo_ext, hi_ext));
+  }
+  la->t.op[xo].ptr = nullptr;  // P is never read
+  la->fused = true;
+  return TSG_OK;
+}
+
 // Fills the kernel arguments of step s for slices [base, base + cnt) (cnt == 1 and base
 // ignored for slice-independent steps) and bounds-checks them.
 tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchArgs* la) {
@@ -778,10 +998,17 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   }
   TSG_TRY(check_step_bounds(c, s, a, la->is_leaf));
   bool ok = false;
-  TSG_TRY(build_tile(st, d, a, la->cnt, c.ring, &la->t, &la->shape, &ok));
+  TileBits tb;
+  TSG_TRY(build_tile(st, d, a, la->cnt, c.ring, &la->t, &la->shape, &ok, &tb));
   la->tile = ok;
   la->streamed = false;
+  la->fused = false;
   if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
+  if (c.lay->fused_from[s] >= 0) {
+    if (!ok)
+      return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused step outside the tile kernel");
+    return build_fused(c, s, base, tb, la);
+  }
   if (ok) {
     uint64_t extent[2];
     for (int o = 0; o < 2; ++o)
@@ -794,6 +1021,12 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   LaunchArgs la;
   TSG_TRY(build_step(c, s, base, cnt, &la));
+  if (la.fused) {
+    if (c.ring == TSG_RING_U64) TSG_TRY(launch_fused_u64(la, c.ra, c.stream));
+    else TSG_TRY(launch_fused_modp(la, c.ra, c.stream));
+    TSG_CUDA_TRY(cudaGetLastError());
+    return TSG_OK;
+  }
   if (la.streamed) {
     TSG_TRY(device_error_address(&la.stream.error));
     la.stream.wait_ns = g_wait_limit_ns.load(std::memory_order_relaxed);
@@ -915,7 +1148,12 @@ struct RunTimer {
 // Kernel and template parameters of one built launch, as tsg_plan_describe reports them
 // (the same selection as launch_step and the launch_tile_* / launch_stream_* switches).
 void describe_launch(const LaunchArgs& la, int ring, int32_t* out) {
-  if (la.streamed) {
+  if (la.fused) {
+    out[0] = TSG_KERNEL_FUSED;
+    out[1] = la.shape.v;
+    out[2] = la.shape.ne == 1 || la.shape.ne == 2 ? la.shape.ne : 4;
+    out[3] = la.shape.nk;
+  } else if (la.streamed) {
     const int nk = std::min(la.t.n_k, 4);
     out[0] = TSG_KERNEL_STREAM;
     out[1] = 0;
@@ -989,6 +1227,13 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
     return (timer && !dry) ? timer->record(stream, id) : TSG_OK;
   };
   auto step = [&](int s, int64_t base, int64_t cnt) -> tsg_status {
+    if (lay->fused_away[s]) {  // computed inside its consumer: no launch
+      if (dry && kinds) {
+        kinds[4 * s] = TSG_KERNEL_NONE;
+        kinds[4 * s + 1] = kinds[4 * s + 2] = kinds[4 * s + 3] = 0;
+      }
+      return TSG_OK;
+    }
     if (dry) {
       LaunchArgs la;
       TSG_TRY(build_step(c, s, base, cnt, &la));
@@ -1199,6 +1444,31 @@ tsg_status tsg_plan_launch_count(const tsg_plan* plan, int64_t slice_begin, int6
   *count_out = plan->steps.back().dep ? indep + groups * (dep + 1) : indep + 1;
   return TSG_OK;
 }
+
+tsg_status tsg_plan_launches(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                             int64_t slice_begin, int64_t slice_end, int64_t group_size,
+                             int64_t* count_out) {
+  if (!plan || !count_out) return fail(TSG_ERR_INVALID_ARGUMENT, "launches: null pointer");
+  TSG_TRY(check_range(plan, slice_begin, slice_end, group_size));
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  const Layout* lay;
+  TSG_TRY(get_layout(const_cast<tsg_plan*>(plan), group_size, eb, planes, &lay));
+  int64_t indep = 0, dep = 0;
+  for (size_t s = 0; s < plan->steps.size(); ++s)
+    if (!lay->fused_away[s]) (plan->steps[s].dep ? dep : indep)++;
+  const int64_t groups = (slice_end - slice_begin + group_size - 1) / group_size;
+  *count_out = plan->steps.back().dep ? indep + groups * (dep + 1) : indep + 1;
+  return TSG_OK;
+}
+
+tsg_status tsg_set_fusion(int32_t enabled) {
+  g_fusion.store(enabled ? 1 : 0, std::memory_order_relaxed);
+  return TSG_OK;
+}
+
+int32_t tsg_fusion_enabled(void) { return g_fusion.load(std::memory_order_relaxed); }
 
 tsg_status tsg_plan_run(const tsg_plan* plan, int32_t ring, int32_t num_primes,
                         const uint32_t* primes, const uint8_t* leaf_pool_dev,

@@ -583,6 +583,182 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
 }
 
 // ------------------------------------------------------------------------------------
+// Fused steps. A step P = A x B whose large result is read by exactly one consumer step
+// C x P as that step's E-free operand is not launched: the consumer computes each entry
+// of P it needs from A and B, and P never exists in HBM. For the consumer's index x and
+// summed combination k,
+//   P[y(x, k)] = sum over the producer's summed combinations kp of A[a(x, k, kp)] B[b(x, k, kp)]
+// where the offset maps a, b compose the consumer's map onto P with the producer's maps
+// onto A and B (the host builds them as tile operands in the consumer's index space).
+// Every P entry the consumer reads is computed once per (position, summed combination):
+// P carries every output bit but the enumerated ones, so no two threads share an entry.
+
+struct FusedArgs {
+  TileOperand op[2];      // A and B: producer operands, mapped in the consumer's index
+  uint32_t kp_off[2][2];  // per operand, offset of each producer summed combination
+  int32_t fx;             // consumer operand that is computed (never read from memory)
+};
+
+// The V values of P for summed combination `ku` of plane p (offsets a_p, b_p already
+// include the plane): MODP residues in Montgomery form, U64 plain counts.
+template <int kRing, int V, int NKP, typename VT>
+__device__ __forceinline__ void fused_x(const FusedArgs& f, uint64_t a_p, uint64_t b_p, int ku,
+                                        const PlaneConst& pc, VT (&x)[V]) {
+  using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
+  const TileOperand& A = f.op[0];
+  const TileOperand& B = f.op[1];
+  uint64_t acc[V];
+#pragma unroll
+  for (int j = 0; j < V; ++j) acc[j] = 0;
+#pragma unroll
+  for (int kp = 0; kp < NKP; ++kp) {
+    VT av[V], bv[V];
+    tile_load<T, VT, V>(A, a_p + A.k_off[ku] + f.kp_off[0][kp], av);
+    tile_load<T, VT, V>(B, b_p + B.k_off[ku] + f.kp_off[1][kp], bv);
+#pragma unroll
+    for (int j = 0; j < V; ++j) acc[j] += (uint64_t)av[j] * (uint64_t)bv[j];
+  }
+  if constexpr (kRing == TSG_RING_MODP) {
+    // at most two products: below 2 p^2 < p 2^32 (one reduction), or small with leaves
+    const int leaves = A.leaf + B.leaf;
+#pragma unroll
+    for (int j = 0; j < V; ++j) x[j] = mont_finish_c(acc[j], leaves, pc);
+  } else {
+#pragma unroll
+    for (int j = 0; j < V; ++j) x[j] = acc[j];
+  }
+}
+
+// One thread of a fused step (count rings, V = 4 positions, NK summed combinations of the
+// consumer unrolled): per residue plane, the NK x V values of P are computed from A and
+// B, then combined with the other operand Y for every E combination, as in tile_thread.
+template <int kRing, int NE, int NK, int NKP>
+__device__ __forceinline__ void fused_thread(const TileArgs& a, const FusedArgs& f,
+                                             const RingArgs& ring, const TileOperand& Y,
+                                             uint64_t a0, uint64_t b0, uint64_t y0,
+                                             uint64_t oo) {
+  constexpr int V = 4;
+  using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
+  using VT = T;
+  constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
+  constexpr int KU = NK;
+  constexpr bool kHoist = NE * KU * V * sizeof(VT) <= 64;
+  const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
+  const TileOperand& A = f.op[0];
+  const TileOperand& B = f.op[1];
+  const int y_leaf = Y.leaf;
+#pragma unroll 1
+  for (int p = 0; p < PP; ++p) {
+    if (p >= np) break;
+    const PlaneConst pc = plane_const(ring, p);
+    const uint64_t a_p = a0 + (A.leaf ? 0 : p * A.plane);
+    const uint64_t b_p = b0 + (B.leaf ? 0 : p * B.plane);
+    const uint64_t yp = y0 + (Y.leaf ? 0 : p * Y.plane);
+    VT yh[kHoist ? NE : 1][KU][V];
+    if constexpr (kHoist) {
+#pragma unroll
+      for (int e = 0; e < NE; ++e)
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku) tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[ku], yh[e][ku]);
+    }
+    VT x[KU][V];
+#pragma unroll
+    for (int ku = 0; ku < KU; ++ku) fused_x<kRing, V, NKP>(f, a_p, b_p, ku, pc, x[ku]);
+    constexpr bool kDouble = !kHoist && NE > 1;
+    VT ycur[kDouble ? KU : 1][V], ynxt[kDouble ? KU : 1][V];
+    if constexpr (kDouble) {
+#pragma unroll
+      for (int ku = 0; ku < KU; ++ku) tile_load<T, VT, V>(Y, yp + Y.e_off[0] + Y.k_off[ku], ycur[ku]);
+    }
+#pragma unroll
+    for (int e = 0; e < NE; ++e) {
+      if constexpr (kDouble) {
+        if (e + 1 < NE) {
+#pragma unroll
+          for (int ku = 0; ku < KU; ++ku)
+            tile_load<T, VT, V>(Y, yp + Y.e_off[e + 1] + Y.k_off[ku], ynxt[ku]);
+        }
+      }
+      uint64_t acc[V];
+      uint32_t done[V];
+#pragma unroll
+      for (int j = 0; j < V; ++j) {
+        acc[j] = 0;
+        done[j] = 0;
+      }
+#pragma unroll
+      for (int ku = 0; ku < KU; ++ku) {
+        VT yv[V];
+        if constexpr (kHoist) {
+#pragma unroll
+          for (int j = 0; j < V; ++j) yv[j] = yh[e][ku][j];
+        } else if constexpr (kDouble) {
+#pragma unroll
+          for (int j = 0; j < V; ++j) yv[j] = ycur[ku][j];
+        } else {
+          tile_load<T, VT, V>(Y, yp + Y.e_off[e] + Y.k_off[ku], yv);
+        }
+#pragma unroll
+        for (int j = 0; j < V; ++j) acc[j] += (uint64_t)x[ku][j] * (uint64_t)yv[j];
+        if constexpr (kRing == TSG_RING_MODP) {
+          // two Montgomery products stay below p 2^32: reduce every pair of sums
+          if (y_leaf == 0 && (ku & 1) && ku + 1 < KU) {
+#pragma unroll
+            for (int j = 0; j < V; ++j) {
+              done[j] = add_mod(done[j], mont_redc(acc[j], pc.p, pc.pinv), pc.p);
+              acc[j] = 0;
+            }
+          }
+        }
+      }
+      const uint64_t oe = oo + a.o_e[e];
+      if constexpr (kRing == TSG_RING_U64) {
+        uint64_t* out = reinterpret_cast<uint64_t*>(a.out);
+        if (a.o_contig) {
+          reinterpret_cast<ulonglong2*>(out + oe)[0] = make_ulonglong2(acc[0], acc[1]);
+          reinterpret_cast<ulonglong2*>(out + oe)[1] = make_ulonglong2(acc[2], acc[3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = acc[j];
+        }
+      } else {
+        // X is a residue, so the products have at most one leaf factor (Y)
+        uint32_t* out = reinterpret_cast<uint32_t*>(a.out) + p * a.o_plane;
+        uint32_t r[V];
+#pragma unroll
+        for (int j = 0; j < V; ++j) r[j] = add_mod(done[j], mont_finish_c(acc[j], y_leaf, pc), pc.p);
+        if (a.o_contig) {
+          *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1], r[2], r[3]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < V; ++j) out[oe + a.o_tab[j]] = r[j];
+        }
+      }
+      if constexpr (kDouble) {
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku)
+#pragma unroll
+          for (int j = 0; j < V; ++j) ycur[ku][j] = ynxt[ku][j];
+      }
+    }
+  }
+}
+
+template <int kRing, int NE, int NK, int NKP>
+__global__ void __launch_bounds__(kThreads, 2)
+    tree_step_fused_kernel(TileArgs a, FusedArgs f, RingArgs ring) {
+  const uint32_t g = blockIdx.y;
+  const uint32_t f_hi = blockIdx.x << a.tile_bits;
+  const uint32_t f_lo = threadIdx.x * 4u;
+  auto offset = [&](const TileOperand& op) -> uint64_t {
+    return op.base + scatter_bits(op.g, g) + scatter32(op.f_hi, f_hi) + scatter32(op.f_lo, f_lo);
+  };
+  const TileOperand& Y = a.op[1 - f.fx];
+  const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
+  fused_thread<kRing, NE, NK, NKP>(a, f, ring, Y, offset(f.op[0]), offset(f.op[1]), offset(Y), oo);
+}
+
+// ------------------------------------------------------------------------------------
 // Streaming kernel for the large steps (the bulk of the HBM traffic). Persistent blocks
 // walk the (tile, slice) work items with a warp-specialised pipeline:
 //   * an item is one residue plane of one 1024-element tile of one slice;
@@ -1136,8 +1312,11 @@ struct LaunchArgs {
   TileArgs t;       // tile form, valid when `tile`
   TileShape shape;
   StreamArgs stream;
+  FusedArgs f;      // fused form, valid when `fused`
+  int nkp;          // fused: producer summed combinations (1 or 2)
   bool tile;
   bool streamed;    // run by the streaming (TMA-staged) kernel
+  bool fused;       // run by the fused kernel (operand f.fx computed from f.op)
   bool is_leaf[2];
   uint64_t cnt;     // slices of this launch
 };
@@ -1151,6 +1330,8 @@ tsg_status launch_tile_modp_ne4(const LaunchArgs& la, const RingArgs& ra, cudaSt
 tsg_status launch_tile_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_stream_modp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_stream_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
+tsg_status launch_fused_modp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
+tsg_status launch_fused_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 
 }  // namespace dev
 }  // namespace tsg

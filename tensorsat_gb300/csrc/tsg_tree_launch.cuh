@@ -102,6 +102,42 @@ tsg_status launch_stream_ring(const LaunchArgs& la, const RingArgs& ra, cudaStre
   }
 }
 
+template <int kRing, int NE, int NK, int NKP>
+void launch_fused_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  dim3 grid((unsigned)la.shape.tiles, (unsigned)la.cnt);
+  tree_step_fused_kernel<kRing, NE, NK, NKP><<<grid, la.shape.threads, 0, st>>>(la.t, la.f, ra);
+}
+
+template <int kRing, int NE, int NK>
+void launch_fused_nkp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  if (la.nkp == 2) launch_fused_t<kRing, NE, NK, 2>(la, ra, st);
+  else launch_fused_t<kRing, NE, NK, 1>(la, ra, st);
+}
+
+template <int kRing, int NE>
+void launch_fused_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  switch (la.shape.nk) {
+    case 1: launch_fused_nkp<kRing, NE, 1>(la, ra, st); break;
+    case 2: launch_fused_nkp<kRing, NE, 2>(la, ra, st); break;
+    default: launch_fused_nkp<kRing, NE, 4>(la, ra, st); break;
+  }
+}
+
+// The fused kernel: V = 4, the consumer's summed count (1, 2 or 4) and the producer's (1
+// or 2) are template parameters; the host only fuses steps within these limits.
+template <int kRing>
+tsg_status launch_fused_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  if (la.shape.v != 4 || (la.shape.nk != 1 && la.shape.nk != 2 && la.shape.nk != 4) ||
+      la.nkp < 1 || la.nkp > 2)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "fused kernel: shape outside its instantiations");
+  switch (la.shape.ne) {
+    case 1: launch_fused_nk<kRing, 1>(la, ra, st); break;
+    case 2: launch_fused_nk<kRing, 2>(la, ra, st); break;
+    default: launch_fused_nk<kRing, 4>(la, ra, st); break;
+  }
+  return TSG_OK;
+}
+
 }  // namespace
 }  // namespace dev
 }  // namespace tsg

@@ -668,25 +668,39 @@ class SlicedPlan:
             "step_rhs_pos": np.ascontiguousarray(pos[1]),
         }
 
-    def step_bytes_per_slice(self, elem_bytes: int, planes: int = 1) -> list[float]:
+    def step_bytes_per_slice(self, elem_bytes: int, planes: int = 1,
+                             fused: dict[int, int] | None = None) -> list[float]:
         """Algorithmic HBM bytes of each step for one slice: the step reads both operands
         once and writes its result once (leaves are uint8, other tensors elem_bytes *
-        planes)."""
+        planes). ``fused`` maps a consumer step to the producer step it computes itself:
+        the producer then moves nothing, and the consumer reads the producer's two
+        operands instead of the producer's result."""
         t = self.tree
         L = t.num_leaves
         sl = frozenset(self.sliced)
+        fused = fused or {}
+        away = set(fused.values())
+
+        def size(x: int) -> float:
+            n = 2.0 ** len(t.node_wires[x] - sl)
+            return n if x < L else n * elem_bytes * planes
+
         out = []
         for s, (a, b) in enumerate(t.steps):
+            if s in away:
+                out.append(0.0)
+                continue
             tot = 0.0
             for x in (a, b):
-                if x < L:
-                    tot += 2.0 ** len(t.node_wires[x] - sl)
+                if x >= L and x - L == fused.get(s):
+                    tot += sum(size(y) for y in t.steps[x - L])
                 else:
-                    tot += 2.0 ** len(t.node_wires[x] - sl) * elem_bytes * planes
-            tot += 2.0 ** len(t.node_wires[L + s] - sl) * elem_bytes * planes
+                    tot += size(x)
+            tot += size(L + s)
             out.append(tot)
         return out
 
-    def bytes_per_slice(self, elem_bytes: int, planes: int = 1) -> float:
+    def bytes_per_slice(self, elem_bytes: int, planes: int = 1,
+                        fused: dict[int, int] | None = None) -> float:
         """Algorithmic HBM bytes of one slice, all steps (see step_bytes_per_slice)."""
-        return float(sum(self.step_bytes_per_slice(elem_bytes, planes)))
+        return float(sum(self.step_bytes_per_slice(elem_bytes, planes, fused)))

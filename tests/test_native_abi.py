@@ -198,6 +198,8 @@ def _profiled_kernels():
         name, args = m.group(1), [int(x) for x in m.group(2).split(",")]
         if name == "tree_step_tile_kernel":
             kind = (_native.TSG_KERNEL_TILE, args[1], args[2], args[3])
+        elif name == "tree_step_fused_kernel":
+            kind = (_native.TSG_KERNEL_FUSED, 4, args[1], args[2])
         elif name == "tree_step_stream_kernel":
             kind = (_native.TSG_KERNEL_STREAM, 0, args[1], args[2])
         else:
@@ -215,15 +217,58 @@ def test_kernel_choice_matches_the_profiled_launches():
     npl = c.native_plan()
     expected = _profiled_kernels()
     assert len(expected) >= 20
-    got = {_native.TSG_RING_MODP: npl.describe(_native.TSG_RING_MODP, PRIMES_31[:3], 64),
-           _native.TSG_RING_OR_AND: npl.describe(_native.TSG_RING_OR_AND, (), 64)}
+    lib = _native.lib()
+    # the launch list records whether its run fused steps
+    fused_run = any(kind[0] == _native.TSG_KERNEL_FUSED for kind in expected.values())
+    lib.tsg_set_fusion(1 if fused_run else 0)
+    try:
+        got = {_native.TSG_RING_MODP: npl.describe(_native.TSG_RING_MODP, PRIMES_31[:3], 64),
+               _native.TSG_RING_OR_AND: npl.describe(_native.TSG_RING_OR_AND, (), 64)}
+    finally:
+        lib.tsg_set_fusion(1)
     for (ring, step), kind in expected.items():
         assert tuple(int(x) for x in got[ring][step]) == kind, (ring, step)
     kinds = got[_native.TSG_RING_MODP][:, 0]
     assert set(kinds) <= {_native.TSG_KERNEL_GENERAL, _native.TSG_KERNEL_TILE,
-                          _native.TSG_KERNEL_STREAM}
+                          _native.TSG_KERNEL_STREAM, _native.TSG_KERNEL_FUSED,
+                          _native.TSG_KERNEL_NONE}
     with pytest.raises(_native.TsgValueError):
         npl.describe(_native.TSG_RING_OR_AND, (), c.num_slices + 1)
+
+
+def test_fusion_decisions_on_the_benchmark_tree():
+    """The n=60 benchmark tree fuses its expansion steps in the count rings only: each
+    fused producer is an operand of its consumer, launches nothing and needs no
+    workspace; switching fusion off restores the plain launches."""
+    import json
+
+    plan = json.loads((HEADER.parent.parent / "plans" / "3sat_n60_m256_rng0_t26.json").read_text())
+    cnf = CNFInstance.random(3, 60, 256, rng=0)
+    c = GpuContraction.from_plan(CudaRel, cnf.clause_diagram().wiring, plan)
+    npl = c.native_plan()
+    lib = _native.lib()
+    primes = PRIMES_31[:3]
+    assert lib.tsg_fusion_enabled() == 1
+    fused = npl.fused_steps(_native.TSG_RING_MODP, primes, 64, c.tree)
+    assert fused and fused == npl.fused_steps(_native.TSG_RING_U64, (), 64, c.tree)
+    assert npl.fused_steps(_native.TSG_RING_OR_AND, (), 64, c.tree) == {}
+    L = c.tree.num_leaves
+    for s, p in fused.items():
+        assert L + p in c.tree.steps[s]
+    ws_on = npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64)
+    n_on = npl.launch_count(0, 64, 64, _native.TSG_RING_MODP, 3)
+    lib.tsg_set_fusion(0)
+    try:
+        assert npl.fused_steps(_native.TSG_RING_MODP, primes, 64, c.tree) == {}
+        ws_off = npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64)
+        n_off = npl.launch_count(0, 64, 64, _native.TSG_RING_MODP, 3)
+    finally:
+        lib.tsg_set_fusion(1)
+    assert ws_on < ws_off and n_on == n_off - len(fused)
+    assert n_off == npl.launch_count(0, 64, 64)
+    sp = c.sliced_plan
+    saved = sp.bytes_per_slice(4, 3) - sp.bytes_per_slice(4, 3, fused)
+    assert saved > 0.3 * sp.bytes_per_slice(4, 3)
 
 
 def test_subset_dp_rejects_bad_sizes_and_nulls():
