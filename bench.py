@@ -77,6 +77,8 @@ def parse_args():
                    help="plan the n=60 tree instead of loading the committed plan")
     p.add_argument("--no-batched", action="store_true",
                    help="skip the ragged batched-vs-plain leg of the default run")
+    p.add_argument("--no-instance", action="store_true",
+                   help="skip the whole-instance count and its DPLL check")
     p.add_argument("--batched-steps", type=int, default=3,
                    help="timed graph-replay passes of the ragged leg")
     return p.parse_args()
@@ -442,17 +444,19 @@ def run_gb300(args) -> None:
     # the whole instance: exact count and SAT bit over all slices, the slices sharded
     # across the ranks (one all-reduce per ring combines the shares)
     pg = dist.group.WORLD if dist else None
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    full_count = contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES, group=group,
-                                   process_group=pg)
-    full_sat = bool(contraction.contract(diagram, group=group, process_group=pg))
-    torch.cuda.synchronize()
-    full_s = time.perf_counter() - t0
-    instance = {"count": int(full_count), "sat": full_sat, "seconds": round(full_s, 3),
-                "ranks": world, "form": "GpuContraction.count + contract over all "
-                f"{ns} slices, process_group={'WORLD' if pg else None}"}
-    if dpll is not None:
+    instance = None
+    if not args.no_instance:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        full_count = contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES,
+                                       group=group, process_group=pg)
+        full_sat = bool(contraction.contract(diagram, group=group, process_group=pg))
+        torch.cuda.synchronize()
+        full_s = time.perf_counter() - t0
+        instance = {"count": int(full_count), "sat": full_sat, "seconds": round(full_s, 3),
+                    "ranks": world, "form": "GpuContraction.count + contract over all "
+                    f"{ns} slices, process_group={'WORLD' if pg else None}"}
+    if dpll is not None and instance is not None:
         want = dpll.get(timeout=600)
         instance["dpll_count"] = want
         if full_count != want or full_sat != (want > 0):

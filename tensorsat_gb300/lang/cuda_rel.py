@@ -136,7 +136,7 @@ class CudaRel(TensorLikeBox):
     def __new__(cls, tensor: Any = None, *args: Any, **kwargs: Any) -> "CudaRel":
         """Constructs a relation from a Boolean tensor (numpy or torch, values 0/1)."""
         if isinstance(tensor, np.ndarray):
-            t = torch.from_numpy(np.ascontiguousarray(tensor))
+            t = torch.from_numpy(np.require(tensor, requirements="C"))  # keeps 0-d arrays 0-d
         elif isinstance(tensor, torch.Tensor):
             t = tensor
         else:

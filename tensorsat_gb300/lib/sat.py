@@ -223,7 +223,7 @@ class CNFInstance:
 def _host_u8(a: np.ndarray):
     import torch
 
-    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint8))
+    return torch.from_numpy(np.require(a, dtype=np.uint8, requirements="C"))  # keeps 0-d arrays 0-d
 
 
 __all__ = ["CNFInstance", "Clause", "CNFDiagramMode", "bit_unk"]

@@ -36,7 +36,8 @@ def make_finrel_cuda(tensorsat_module: Any | None = None) -> type:
 
     def _dev(t: Any) -> torch.Tensor:
         if isinstance(t, np.ndarray):
-            t = torch.from_numpy(np.ascontiguousarray(t, dtype=np.uint8))
+            # np.array keeps 0-d scalars 0-d (np.ascontiguousarray would make them 1-d)
+            t = torch.from_numpy(np.array(t, dtype=np.uint8, order="C", copy=True))
         return _device.to_device_u8(t)
 
     @final

@@ -157,3 +157,17 @@ def test_contraction_validation():
     nested = cnf.inputs(None) >> cnf.diagram()
     assert not c.can_contract(nested)
     assert len(c.path) == len(c.tree.steps)
+
+
+def test_zero_dim_tensors_keep_their_shape():
+    """0-d arrays stay 0-d in boxes (a scalar relation, or the clause tensor of an empty
+    clause), so their port count matches the wiring."""
+    import numpy as np
+
+    from tensorsat_gb300.lang.cuda_rel import CudaRel, leaf_array
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    assert tuple(CudaRel(np.array(1, dtype=np.uint8)).tensor.shape) == ()
+    d = CNFInstance(2, [(1, 2), ()]).clause_diagram()
+    assert [leaf_array(b).shape for b in d.blocks] == [(2, 2), ()]
+    assert d.wiring.slot_wires_list[1] == ()

@@ -232,6 +232,22 @@ def test_temporary_variants_do_not_share_a_cached_pool(cuda):
     assert counts == [int(w) for w in want]
 
 
+def test_empty_clause_network_counts_zero(cuda):
+    """A clause with no literal is a 0-port tensor holding 0: the network has no model.
+    Its SAT bit and counts match the oracle's DPLL counter, in every ring."""
+    for clauses in ([(1, 2), (), (-3,)], [()], [(1,), (-1, 2), ()]):
+        n = max([abs(l) for c in clauses for l in c] or [1])
+        cnf = CNFInstance(n, clauses)
+        d = cnf.clause_diagram()
+        assert any(orc_shape == () for orc_shape in
+                   (tuple(b.tensor.shape) for b in d.blocks))
+        c = GpuContraction(CudaRel, d.wiring)
+        assert orc.dpll_count(n, clauses)[0] == 0
+        assert c.count(d, ring="u64") == 0
+        assert c.count(d, ring="modp", num_primes=2) == 0
+        assert bool(c.contract(d)) is False
+
+
 def test_sharp_sat_example(cuda):
     kats = _json("notebook_kats.json")["sharp_sat_example"]
     cnf = CNFInstance(3, [tuple(c) for c in kats["clauses"]])
