@@ -160,8 +160,8 @@ TSG_API tsg_status tsg_plan_launches(const tsg_plan* plan, int32_t ring, int32_t
                              int64_t* count_out);
 
 /* Fused steps, on (1, the default) or off (0), for plans whose layouts are made after the
- * call (layouts are made per plan, ring and group on first use and kept). In the count
- * rings a step whose large result is read once, as the reused operand of its consumer's
+ * call (layouts are made per plan, ring and group on first use and kept). In every ring
+ * a step whose large result is read once, as the reused operand of its consumer's
  * tile form, is not launched: the consumer computes each entry it needs from the step's
  * two operands, so the result never exists in HBM (it is written and read back otherwise;
  * the conditions are in the library's choose_fusion). Results are identical either way;

@@ -197,7 +197,7 @@ int live_bits(const tsg_plan* plan, int v) {
   return r;
 }
 
-// Fused steps of a layout (count rings only): a step p whose result P is read by exactly
+// Fused steps of a layout (every ring): a step p whose result P is read by exactly
 // one consumer s is computed inside s, never stored, when
 //   - P carries every output bit of s but at most two (the enumerated E bits of s's tile
 //     form, so each entry of P is computed once per launch) and at least as many output
@@ -213,7 +213,7 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
   const int ns = (int)steps.size();
   std::vector<int> fused_from(ns, -1);
   std::vector<char> away(ns, 0);
-  if (elem_bytes == 1 || group > 65535) return fused_from;  // OR-AND: no fused kernel
+  if (group > 65535) return fused_from;
   auto rank_ok = [&](int v) {
     return v >= 0 ? plan->leaves[v].rank <= 31 : steps[-v - 1].out_bits <= 31;
   };
@@ -586,7 +586,7 @@ tsg_status fill_tile_operand(TileOperand& op, const int* pos, const OperandDesc&
 // chosen F and E bits go to *bits_out when given.
 tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs& a,
                       uint64_t cnt, int ring, TileArgs* t, TileShape* shape, bool* ok,
-                      TileBits* bits_out = nullptr) {
+                      TileBits* bits_out = nullptr, bool allow_v16 = true) {
   std::memset(t, 0, sizeof(*t));
   *ok = st.out_bits <= 30 && st.k_bits <= 4 && cnt <= 65535;
   if (!*ok) return TSG_OK;
@@ -609,7 +609,7 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
   }
   const int nf = (int)fbits.size();
   int v = nf >= 2 ? 4 : 1;
-  if (ring == TSG_RING_OR_AND && nf >= 4) {
+  if (ring == TSG_RING_OR_AND && nf >= 4 && allow_v16) {
     // 16 byte-wide positions when the output takes the 4 fastest F bits as its 4 fastest
     // bits and every operand carries them as its own 4 fastest bits (vector load), at most
     // 3 of them (byte permutes of <= 8 distinct values) or none (broadcast)
@@ -999,7 +999,9 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   TSG_TRY(check_step_bounds(c, s, a, la->is_leaf));
   bool ok = false;
   TileBits tb;
-  TSG_TRY(build_tile(st, d, a, la->cnt, c.ring, &la->t, &la->shape, &ok, &tb));
+  // a fused consumer takes 4 positions per thread in every ring (the fused kernel's form)
+  TSG_TRY(build_tile(st, d, a, la->cnt, c.ring, &la->t, &la->shape, &ok, &tb,
+                     /*allow_v16=*/c.lay->fused_from[s] < 0));
   la->tile = ok;
   la->streamed = false;
   la->fused = false;
@@ -1023,6 +1025,7 @@ tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   TSG_TRY(build_step(c, s, base, cnt, &la));
   if (la.fused) {
     if (c.ring == TSG_RING_U64) TSG_TRY(launch_fused_u64(la, c.ra, c.stream));
+    else if (c.ring == TSG_RING_OR_AND) TSG_TRY(launch_fused_or_and(la, c.ra, c.stream));
     else TSG_TRY(launch_fused_modp(la, c.ra, c.stream));
     TSG_CUDA_TRY(cudaGetLastError());
     return TSG_OK;

@@ -592,6 +592,7 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
 // onto A and B (the host builds them as tile operands in the consumer's index space).
 // Every P entry the consumer reads is computed once per (position, summed combination):
 // P carries every output bit but the enumerated ones, so no two threads share an entry.
+// All rings: residues and counts per position, OR-AND as packed words of 0/1 bytes.
 
 struct FusedArgs {
   TileOperand op[2];      // A and B: producer operands, mapped in the consumer's index
@@ -744,6 +745,53 @@ __device__ __forceinline__ void fused_thread(const TileArgs& a, const FusedArgs&
   }
 }
 
+// One thread of a fused OR-AND step: the four positions of each operand travel as one
+// packed word of 0/1 bytes, so P's word for summed combination ku is the OR over the
+// producer's summed combinations of (A word AND B word).
+template <int NE, int NK, int NKP>
+__device__ __forceinline__ void fused_thread_or_and(const TileArgs& a, const FusedArgs& f,
+                                                    const TileOperand& Y, uint64_t a0,
+                                                    uint64_t b0, uint64_t y0, uint64_t oo) {
+  constexpr int KU = NK;
+  const TileOperand& A = f.op[0];
+  const TileOperand& B = f.op[1];
+  uint32_t x[KU];
+#pragma unroll
+  for (int ku = 0; ku < KU; ++ku) {
+    uint32_t w = 0;
+#pragma unroll
+    for (int kp = 0; kp < NKP; ++kp) {
+      uint32_t aw[1], bw[1];
+      tile_load_packed<4>(A, a0 + A.k_off[ku] + f.kp_off[0][kp], aw);
+      tile_load_packed<4>(B, b0 + B.k_off[ku] + f.kp_off[1][kp], bw);
+      w |= aw[0] & bw[0];
+    }
+    x[ku] = w;
+  }
+  uint32_t yh[NE][KU];
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int ku = 0; ku < KU; ++ku) {
+      uint32_t yw[1];
+      tile_load_packed<4>(Y, y0 + Y.e_off[e] + Y.k_off[ku], yw);
+      yh[e][ku] = yw[0];
+    }
+#pragma unroll
+  for (int e = 0; e < NE; ++e) {
+    uint32_t acc = 0;
+#pragma unroll
+    for (int ku = 0; ku < KU; ++ku) acc |= x[ku] & yh[e][ku];
+    const uint64_t oe = oo + a.o_e[e];
+    if (a.o_contig) {
+      *reinterpret_cast<uint32_t*>(a.out + oe) = acc;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) a.out[oe + a.o_tab[j]] = (acc >> (8 * j)) & 0xff;
+    }
+  }
+}
+
 template <int kRing, int NE, int NK, int NKP>
 __global__ void __launch_bounds__(kThreads, 2)
     tree_step_fused_kernel(TileArgs a, FusedArgs f, RingArgs ring) {
@@ -755,7 +803,12 @@ __global__ void __launch_bounds__(kThreads, 2)
   };
   const TileOperand& Y = a.op[1 - f.fx];
   const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
-  fused_thread<kRing, NE, NK, NKP>(a, f, ring, Y, offset(f.op[0]), offset(f.op[1]), offset(Y), oo);
+  if constexpr (kRing == TSG_RING_OR_AND) {
+    fused_thread_or_and<NE, NK, NKP>(a, f, Y, offset(f.op[0]), offset(f.op[1]), offset(Y), oo);
+  } else {
+    fused_thread<kRing, NE, NK, NKP>(a, f, ring, Y, offset(f.op[0]), offset(f.op[1]),
+                                     offset(Y), oo);
+  }
 }
 
 // ------------------------------------------------------------------------------------
@@ -1332,6 +1385,7 @@ tsg_status launch_stream_modp(const LaunchArgs& la, const RingArgs& ra, cudaStre
 tsg_status launch_stream_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_fused_modp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_fused_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
+tsg_status launch_fused_or_and(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 
 }  // namespace dev
 }  // namespace tsg

@@ -91,3 +91,22 @@ def test_fused_cnf_counts_equal_dpll(cuda, lib):
         assert c.count(d, ring="modp", num_primes=3, group=16) == want
         assert c.count(d, ring="u64", group=16) == want
         assert bool(c.contract(d, group=16)) is True
+
+
+def test_fused_or_and_bits_per_slice(cuda, lib):
+    """The OR-AND ring fuses the same steps (packed words of 0/1 bytes): for every slice of
+    a satisfiable instance, the fused SAT bit equals the unfused one and equals whether the
+    slice's exact count is non-zero."""
+    cnf = CNFInstance.random(3, 44, 187, rng=1)
+    d = cnf.clause_diagram()
+    c = GpuContraction(CudaRel, d.wiring, target_bits=22, trials=2, seed=0)
+    lib.tsg_set_fusion(1)
+    assert c.native_plan().fused_steps(_native.TSG_RING_OR_AND, (), 1, c.tree)
+    ns = c.num_slices
+    counts = [c.count(d, ring="u64", group=1, slice_range=(s, s + 1)) for s in range(ns)]
+    assert 0 < sum(1 for x in counts if x) < ns
+    bits = {}
+    for on in (1, 0):
+        lib.tsg_set_fusion(on)
+        bits[on] = [bool(c.contract(d, group=1, slice_range=(s, s + 1))) for s in range(ns)]
+    assert bits[1] == bits[0] == [x > 0 for x in counts]
