@@ -5,7 +5,6 @@ ranks combine residues and SAT bits with one all-reduce each."""
 from __future__ import annotations
 
 import os
-import socket
 
 import pytest
 import torch
@@ -31,16 +30,10 @@ def test_slice_ranges_partition_and_align():
     assert combine_counts([5, 7], [7]) == 5
 
 
-def _free_port() -> int:
-    with socket.socket() as s:
-        s.bind(("127.0.0.1", 0))
-        return s.getsockname()[1]
-
-
-def _worker(rank: int, world: int, port: int, q) -> None:
-    os.environ["MASTER_ADDR"] = "127.0.0.1"
-    os.environ["MASTER_PORT"] = str(port)
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+def _worker(rank: int, world: int, store_file: str, q) -> None:
+    # a file rendezvous: no TCP port to race for with other processes on the host
+    dist.init_process_group("gloo", init_method=f"file://{store_file}", rank=rank,
+                            world_size=world)
     try:
         import numpy as np
 
@@ -83,7 +76,7 @@ def _worker(rank: int, world: int, port: int, q) -> None:
         dist.destroy_process_group()
 
 
-def test_two_rank_sharded_count_gloo():
+def test_two_rank_sharded_count_gloo(tmp_path):
     """GpuContraction.count / .contract with a process group on two gloo CPU ranks: each
     rank runs only its own contiguous, group-aligned share of the slices, and one
     all-reduce per ring combines the shares into the exact count (mod primes with CRT,
@@ -91,8 +84,8 @@ def test_two_rank_sharded_count_gloo():
     oracle's contraction of the same slices (the GPU tests cover the device run)."""
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = _free_port()
-    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    store = str(tmp_path / "rendezvous")
+    procs = [ctx.Process(target=_worker, args=(r, 2, store, q)) for r in range(2)]
     for p in procs:
         p.start()
     for p in procs:
