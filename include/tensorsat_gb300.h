@@ -205,6 +205,27 @@ TSG_API tsg_status tsg_batch_run(int32_t num_instances, const tsg_plan* const* p
                          void* workspace_dev, int64_t workspace_bytes,
                          void* const* results_dev, void* stream);
 
+/* tsg_batch_run over `lanes` (1..32) concurrent lanes: the instances are spread over the
+ * lanes (longest estimated work first, each to the least loaded lane), every lane is a
+ * stream that forks from `stream` at the call and joins it at the end, and each lane has
+ * its own region of the workspace, whose total size tsg_batch_lanes_workspace_bytes
+ * reports (the largest workspace of each lane's instances, summed over lanes). Instances
+ * on different lanes run concurrently, so the many small launches of small instances
+ * overlap on the GPU. Checks every instance and launch before the first launch, like
+ * tsg_batch_run; neither allocates device memory nor synchronises, and it can be captured
+ * into a CUDA graph (the lanes become parallel branches of the graph). The lane streams
+ * are created once per host thread and device. lanes == 1 is tsg_batch_run with the
+ * lane workspace rule. No counterpart in the reference (one instance per call). */
+TSG_API tsg_status tsg_batch_lanes_workspace_bytes(int32_t num_instances,
+                                           const tsg_plan* const* plans, int32_t ring,
+                                           int32_t num_primes, const int64_t* group_sizes,
+                                           int32_t lanes, int64_t* bytes_out);
+TSG_API tsg_status tsg_batch_run_lanes(int32_t num_instances, const tsg_plan* const* plans,
+                               int32_t ring, int32_t num_primes, const uint32_t* primes,
+                               const uint8_t* const* leaf_pools, const int64_t* group_sizes,
+                               int32_t lanes, void* workspace_dev, int64_t workspace_bytes,
+                               void* const* results_dev, void* stream);
+
 /* tsg_plan_run that also measures: a CUDA event is recorded on `stream` before the first
  * launch and after every launch, and on return (the call waits for the run to finish)
  * step_ms[s] holds the device time of tree step s summed over the slice groups of the

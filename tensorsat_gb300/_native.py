@@ -64,6 +64,8 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_launches",
     "tsg_set_fusion",
     "tsg_fusion_enabled",
+    "tsg_batch_lanes_workspace_bytes",
+    "tsg_batch_run_lanes",
 )
 
 
@@ -147,6 +149,13 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_describe.restype = c_int32
     lib.tsg_plan_describe.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32), c_int64,
                                       _i32p]
+    lib.tsg_batch_lanes_workspace_bytes.restype = c_int32
+    lib.tsg_batch_lanes_workspace_bytes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
+                                                    _i64p, c_int32, _i64p]
+    lib.tsg_batch_run_lanes.restype = c_int32
+    lib.tsg_batch_run_lanes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
+                                        POINTER(c_uint32), POINTER(c_void_p), _i64p, c_int32,
+                                        c_void_p, c_int64, POINTER(c_void_p), c_void_p]
     lib.tsg_plan_launches.restype = c_int32
     lib.tsg_plan_launches.argtypes = [c_void_p, c_int32, c_int32, c_int64, c_int64, c_int64,
                                       _i64p]

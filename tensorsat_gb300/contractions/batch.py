@@ -66,13 +66,19 @@ class BatchContraction:
 
     def __init__(self, box_class: type[CudaRel], diagrams: Sequence[Diagram], *,
                  target_bits: int | None = 26, trials: int = 2, seed: int = 0,
-                 trees: Sequence[tuple[Any, Sequence[int]]] | None = None) -> None:
+                 trees: Sequence[tuple[Any, Sequence[int]]] | None = None,
+                 lanes: int = 16) -> None:
         """``trees`` optionally gives each diagram's (tree, sliced wires), for example from
         :func:`~tensorsat_gb300.contractions.gpu.plan_tree` run in worker processes;
         otherwise every diagram is planned here with ``target_bits``, ``trials`` and
-        ``seed``."""
+        ``seed``. ``lanes`` (1..32) is the number of concurrent lanes the batch's
+        instances are spread over (``tsg_batch_run_lanes``): each lane is a stream with its
+        own workspace region, so the small launches of different instances overlap."""
         if not diagrams:
             raise ValueError("A batch needs at least one diagram.")
+        if not 1 <= lanes <= 32:
+            raise ValueError("lanes must lie in 1..32")
+        self.lanes = min(lanes, len(diagrams))
         self._diagrams = list(diagrams)
         if trees is not None and len(trees) != len(self._diagrams):
             raise ValueError(f"expected {len(self._diagrams)} trees, got {len(trees)}")
@@ -142,19 +148,21 @@ class BatchContraction:
 
     def groups(self, ring: int, planes: int, budget_bytes: int | None = None) -> list[int]:
         """Slice group per instance: the largest power of two whose workspace fits the
-        budget (default: 40% of free device memory); the batch shares one workspace, so
-        the budget bounds every instance."""
+        budget (default: 40% of free device memory) divided by the lanes (every lane holds
+        the workspace of its largest instance)."""
         if budget_bytes is None:
             free, _ = torch.cuda.mem_get_info()
             budget_bytes = int(free * 0.4)
-        return [c.choose_group(ring, planes, budget_bytes) for c in self._contractions]
+        per_lane = max(1, budget_bytes // self.lanes)
+        return [c.choose_group(ring, planes, per_lane) for c in self._contractions]
 
     def workspace_bytes(self, ring: int, planes: int, groups: Sequence[int]) -> int:
         lib = _native.lib()
         handles = _ptr_array([c.native_plan().handle.value for c in self._contractions])
         out = ctypes.c_int64()
-        _native.check(lib.tsg_batch_workspace_bytes(
-            len(self), handles, ring, planes, _native.i64_array(list(groups)), ctypes.byref(out)))
+        _native.check(lib.tsg_batch_lanes_workspace_bytes(
+            len(self), handles, ring, planes, _native.i64_array(list(groups)), self.lanes,
+            ctypes.byref(out)))
         return int(out.value)
 
     def _results(self, ring: int, planes: int) -> list[torch.Tensor]:
@@ -181,9 +189,9 @@ class BatchContraction:
             _native.i64_array(list(groups)),
             _ptr_array([r.data_ptr() for r in results]),
         ]
-        st = lib.tsg_batch_run(len(self), args[0], ring, len(primes), args[1], args[2],
-                               args[3], workspace.data_ptr(), workspace.numel(), args[4],
-                               stream)
+        st = lib.tsg_batch_run_lanes(len(self), args[0], ring, len(primes), args[1], args[2],
+                                     args[3], self.lanes, workspace.data_ptr(),
+                                     workspace.numel(), args[4], stream)
         _native.check(st)
         return args
 

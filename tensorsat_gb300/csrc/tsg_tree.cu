@@ -1273,6 +1273,90 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
 namespace tsg {
 namespace {
 
+constexpr int kMaxLanes = 32;
+
+// Lanes of a batched run (tsg_batch_run_lanes): instances are spread over `lanes`
+// streams that fork from the caller's stream and join it again, so the small launches of
+// different instances overlap on the GPU. Each lane has its own workspace region.
+
+// Estimated work of one instance: index-space entries of every launch (slice-dependent
+// steps once per slice).
+double instance_cost(const tsg_plan* plan) {
+  const double slices = std::ldexp(1.0, plan->num_sliced);
+  double c = 0;
+  for (const StepInfo& st : plan->steps)
+    c += std::ldexp(1.0, st.out_bits + st.k_bits) * (st.dep ? slices : 1.0);
+  return c;
+}
+
+// Lane of every instance: longest-processing-time-first over the estimated costs (ties by
+// instance order), so the lanes finish at about the same time. Deterministic.
+std::vector<int> assign_lanes(int32_t n, const tsg_plan* const* plans, int lanes) {
+  std::vector<int> order(n);
+  std::vector<double> cost(n);
+  for (int i = 0; i < n; ++i) {
+    order[i] = i;
+    cost[i] = instance_cost(plans[i]);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<double> load(lanes, 0.0);
+  std::vector<int> lane(n, 0);
+  for (int i : order) {
+    int best = 0;
+    for (int l = 1; l < lanes; ++l)
+      if (load[l] < load[best]) best = l;
+    lane[i] = best;
+    load[best] += cost[i];
+  }
+  return lane;
+}
+
+// Workspace region of each lane (256-byte aligned offsets) and the total.
+tsg_status lane_regions(int32_t n, const tsg_plan* const* plans, int32_t ring,
+                        int32_t num_primes, const int64_t* group_sizes, int lanes,
+                        const std::vector<int>& lane, std::vector<int64_t>* offset,
+                        std::vector<int64_t>* bytes, int64_t* total) {
+  bytes->assign(lanes, 0);
+  for (int i = 0; i < n; ++i) {
+    int64_t b = 0;
+    TSG_TRY(tsg_plan_workspace_bytes(plans[i], ring, num_primes, group_sizes[i], &b));
+    (*bytes)[lane[i]] = std::max((*bytes)[lane[i]], b);
+  }
+  offset->assign(lanes, 0);
+  int64_t off = 0;
+  for (int l = 0; l < lanes; ++l) {
+    (*offset)[l] = off;
+    off += align256((*bytes)[l]);
+  }
+  *total = std::max<int64_t>(off, 256);
+  return TSG_OK;
+}
+
+// Streams and events of the lanes, made once per host thread and device.
+struct LaneSet {
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+};
+
+tsg_status lane_set(int lanes, LaneSet** out) {
+  thread_local std::map<int, LaneSet> sets;
+  int dev = 0;
+  TSG_CUDA_TRY(cudaGetDevice(&dev));
+  LaneSet& ls = sets[dev];
+  if (!ls.fork) TSG_CUDA_TRY(cudaEventCreateWithFlags(&ls.fork, cudaEventDisableTiming));
+  while ((int)ls.streams.size() < lanes) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    TSG_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    TSG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    ls.streams.push_back(st);
+    ls.joins.push_back(ev);
+  }
+  *out = &ls;
+  return TSG_OK;
+}
+
 // Scratch memory of tsg_plan_run_static: a fixed 64 MiB array in device global memory,
 // owned by this library, held by every GPU that loads it until the process exits. Host
 // code cannot use the array's name as a device address; the address comes from
@@ -1557,6 +1641,84 @@ tsg_status tsg_batch_run(int32_t num_instances, const tsg_plan* const* plans, in
     TSG_TRY(run_impl(plans[i], ring, num_primes, primes, leaf_pools[i], 0, ns, group_sizes[i],
                      workspace_dev, workspace_bytes, results_dev[i], 0, (cudaStream_t)stream,
                      /*dry=*/false));
+  }
+  return TSG_OK;
+}
+
+tsg_status tsg_batch_lanes_workspace_bytes(int32_t num_instances, const tsg_plan* const* plans,
+                                           int32_t ring, int32_t num_primes,
+                                           const int64_t* group_sizes, int32_t lanes,
+                                           int64_t* bytes_out) {
+  if (num_instances < 0 || (num_instances > 0 && (!plans || !group_sizes)) || !bytes_out)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_lanes_workspace_bytes: null pointer or negative count");
+  if (lanes < 1 || lanes > kMaxLanes)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_lanes_workspace_bytes: lanes outside 1..32");
+  for (int32_t i = 0; i < num_instances; ++i)
+    if (!plans[i]) return fail(TSG_ERR_INVALID_ARGUMENT, "batch_lanes_workspace_bytes: null plan");
+  const int used = std::max(1, std::min<int>(lanes, num_instances));
+  const std::vector<int> lane = assign_lanes(num_instances, plans, used);
+  std::vector<int64_t> off, bytes;
+  return lane_regions(num_instances, plans, ring, num_primes, group_sizes, used, lane, &off,
+                      &bytes, bytes_out);
+}
+
+tsg_status tsg_batch_run_lanes(int32_t num_instances, const tsg_plan* const* plans,
+                               int32_t ring, int32_t num_primes, const uint32_t* primes,
+                               const uint8_t* const* leaf_pools, const int64_t* group_sizes,
+                               int32_t lanes, void* workspace_dev, int64_t workspace_bytes,
+                               void* const* results_dev, void* stream) {
+  if (num_instances < 0 ||
+      (num_instances > 0 && (!plans || !leaf_pools || !group_sizes || !results_dev)))
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_run_lanes: null pointer or negative count");
+  if (lanes < 1 || lanes > kMaxLanes)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_run_lanes: lanes outside 1..32");
+  if (num_instances == 0) return TSG_OK;
+  for (int32_t i = 0; i < num_instances; ++i) {
+    if (!plans[i] || !leaf_pools[i] || !results_dev[i])
+      return fail(TSG_ERR_INVALID_ARGUMENT,
+                  "batch_run_lanes: null plan, pool or result of instance " + std::to_string(i));
+    const int64_t ns = int64_t(1) << plans[i]->num_sliced;
+    tsg_status st = run_impl(plans[i], ring, num_primes, primes, nullptr, 0, ns,
+                             group_sizes[i], nullptr, 0, nullptr, 0, nullptr, /*dry=*/true);
+    if (st != TSG_OK)
+      return fail(st, "batch_run_lanes: instance " + std::to_string(i) + ": " + tsg_last_error());
+  }
+  const int used = std::max(1, std::min<int>(lanes, num_instances));
+  const std::vector<int> lane = assign_lanes(num_instances, plans, used);
+  std::vector<int64_t> off, bytes;
+  int64_t total = 0;
+  TSG_TRY(lane_regions(num_instances, plans, ring, num_primes, group_sizes, used, lane, &off,
+                       &bytes, &total));
+  if (!workspace_dev || workspace_bytes < total)
+    return fail(TSG_ERR_WORKSPACE,
+                "batch_run_lanes: workspace smaller than tsg_batch_lanes_workspace_bytes");
+  if (((uintptr_t)workspace_dev & 255) != 0)
+    return fail(TSG_ERR_WORKSPACE, "batch_run_lanes: workspace must be 256-byte aligned");
+  cudaStream_t origin = (cudaStream_t)stream;
+  uint8_t* ws = (uint8_t*)workspace_dev;
+  if (used == 1) {
+    for (int32_t i = 0; i < num_instances; ++i) {
+      const int64_t ns = int64_t(1) << plans[i]->num_sliced;
+      TSG_TRY(run_impl(plans[i], ring, num_primes, primes, leaf_pools[i], 0, ns,
+                       group_sizes[i], ws, bytes[0], results_dev[i], 0, origin, /*dry=*/false));
+    }
+    return TSG_OK;
+  }
+  LaneSet* ls = nullptr;
+  TSG_TRY(lane_set(used, &ls));
+  // fork: every lane waits for the work issued before this call on the caller's stream
+  TSG_CUDA_TRY(cudaEventRecord(ls->fork, origin));
+  for (int l = 0; l < used; ++l) TSG_CUDA_TRY(cudaStreamWaitEvent(ls->streams[l], ls->fork, 0));
+  for (int32_t i = 0; i < num_instances; ++i) {
+    const int l = lane[i];
+    const int64_t ns = int64_t(1) << plans[i]->num_sliced;
+    TSG_TRY(run_impl(plans[i], ring, num_primes, primes, leaf_pools[i], 0, ns, group_sizes[i],
+                     ws + off[l], bytes[l], results_dev[i], 0, ls->streams[l], /*dry=*/false));
+  }
+  // join: the caller's stream waits for every lane
+  for (int l = 0; l < used; ++l) {
+    TSG_CUDA_TRY(cudaEventRecord(ls->joins[l], ls->streams[l]));
+    TSG_CUDA_TRY(cudaStreamWaitEvent(origin, ls->joins[l], 0));
   }
   return TSG_OK;
 }

@@ -54,6 +54,35 @@ def test_batch_workspace_is_the_largest_instance_workspace():
         assert out.value == max(p.workspace_bytes(ring, planes, g) for p, g in zip(plans, groups))
 
 
+def test_lane_workspace_holds_every_lane_region():
+    """Lanes: each lane's region holds the largest workspace of the instances assigned to
+    it, so the total lies between the largest single workspace (one lane) and the sum of
+    all (one instance per lane); lane counts beyond the instances change nothing and
+    lanes outside 1..32 are rejected."""
+    plans = _plans(ragged_instances(6, 10, 20), target_bits=8)
+    lib = _native.lib()
+    groups = [1, 2, 4, 1, 2, 1]
+    handles = (ctypes.c_void_p * len(plans))(*[p.handle.value for p in plans])
+    ring, planes = _native.TSG_RING_MODP, 3
+    each = [p.workspace_bytes(ring, planes, g) for p, g in zip(plans, groups)]
+    align = lambda x: (x + 255) // 256 * 256
+    sizes = {}
+    for lanes in (1, 2, 3, 6, 32):
+        out = ctypes.c_int64()
+        _native.check(lib.tsg_batch_lanes_workspace_bytes(
+            len(plans), handles, ring, planes, _native.i64_array(groups), lanes,
+            ctypes.byref(out)))
+        sizes[lanes] = out.value
+    assert sizes[1] == align(max(each))
+    assert sizes[6] == sizes[32] == sum(align(x) for x in each)
+    assert sizes[1] <= sizes[2] <= sizes[6] and sizes[1] <= sizes[3] <= sizes[6]
+    out = ctypes.c_int64()
+    for bad in (0, 33):
+        assert lib.tsg_batch_lanes_workspace_bytes(
+            len(plans), handles, ring, planes, _native.i64_array(groups), bad,
+            ctypes.byref(out)) == _native.TSG_ERR_INVALID_ARGUMENT
+
+
 def test_batch_rejects_a_bad_instance_before_launching():
     """Instance 2 has a group size that is not a power of two: the call fails in the host
     checks (the pointers are never dereferenced, so placeholders suffice)."""
