@@ -52,6 +52,7 @@ N_VARS, N_CLAUSES = 60, 256
 TARGET_BITS = 26
 NUM_PRIMES = 3
 PLAN_FILE = ROOT / "plans" / "3sat_n60_m256_rng0_t26.json"
+TUNE_FILE = ROOT / "plans" / "3sat_n60_m256_rng0_t26.tune.json"
 
 
 def parse_args():
@@ -77,6 +78,11 @@ def parse_args():
                    help="plan the n=60 tree instead of loading the committed plan")
     p.add_argument("--no-batched", action="store_true",
                    help="skip the ragged batched-vs-plain leg of the default run")
+    p.add_argument("--tune", action="store_true",
+                   help="run the autotuner for the n=60 plan when its tuning file has no "
+                        "entry for this GPU, and store the entry")
+    p.add_argument("--no-tuning", action="store_true",
+                   help="ignore the committed tuning (the executor's own kernel choices)")
     p.add_argument("--no-instance", action="store_true",
                    help="skip the whole-instance count and its DPLL check")
     p.add_argument("--batched-steps", type=int, default=3,
@@ -338,12 +344,34 @@ def run_gb300(args) -> None:
     primes = PRIMES_31[:NUM_PRIMES]
     ns = contraction.num_slices
     dev = torch.device("cuda", local)
+    # the autotuner's per-step kernel choices (committed beside the plan, measured on this
+    # GPU model); --tune measures and stores them when missing
+    tuning = None
+    if committed_plan(args) is not None and not args.no_tuning:
+        from tensorsat_gb300 import autotune
+
+        entries = {r: autotune.load(TUNE_FILE, contraction, r, p)
+                   for r, p in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ()))}
+        if args.tune and any(e is None for e in entries.values()):
+            free, _ = torch.cuda.mem_get_info()
+            for r, p in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ())):
+                entries[r] = autotune.load_or_tune(TUNE_FILE, contraction, diagram, r, p,
+                                                   budget_bytes=int(free * 0.4))
+        if all(e is not None for e in entries.values()):
+            for e in entries.values():
+                autotune.apply(contraction, e)
+            tuning = {("modp" if r == _native.TSG_RING_MODP else "or_and"):
+                      {"group": e["group"], "config": e["config"], "gain": round(e["gain"], 4),
+                       "steps_changed": sum(1 for o in e["options"] if o)}
+                      for r, e in entries.items()}
     if args.group:
         group = args.group
     else:
         free, _ = torch.cuda.mem_get_info()
         budget = int(free * 0.75)
         group = min(ns, 256)
+        if tuning is not None:
+            group = min(group, tuning["modp"]["group"])
         while group > 1 and (npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, group)
                              + npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, group)) > budget:
             group //= 2
@@ -525,6 +553,7 @@ def run_gb300(args) -> None:
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clocks.summary(),
             "step_ms": [round(x, 3) for x in step_ms],
+            "tuning": tuning,
             "instance": instance,
             "batched": batched,
         }

@@ -170,6 +170,18 @@ TSG_API tsg_status tsg_plan_launches(const tsg_plan* plan, int32_t ring, int32_t
 TSG_API tsg_status tsg_set_fusion(int32_t enabled);
 TSG_API int32_t tsg_fusion_enabled(void);
 
+/* Per-step kernel options of a plan in one ring (the autotuner's choices): options[s] is
+ * a bit set of TSG_STEP_NO_STREAM (run step s on the tile kernel even where the streaming
+ * kernel applies) and TSG_STEP_NO_FUSE (never compute step s inside its consumer), for
+ * every step (num_steps entries); options == NULL clears them. Later runs, workspace sizes
+ * and descriptions of that ring follow them; results do not depend on them. Host only.
+ * No counterpart in the reference, whose path choice (cotengra's optimize/order kwargs,
+ * tensorsat/contractions/cotengra.py:62-64,104-106) has no kernel to choose. */
+#define TSG_STEP_NO_STREAM 1
+#define TSG_STEP_NO_FUSE 2
+TSG_API tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring,
+                                     const int32_t* options);
+
 /* Contracts slices [slice_begin, slice_end) of the plan, `group_size` slices per launch
  * group (a power of two; slice_begin must be a multiple of it, the last group may be
  * partial), and combines the per-slice root tensors into result_dev:

@@ -34,6 +34,8 @@ TSG_KERNEL_TILE = 1
 TSG_KERNEL_STREAM = 2
 TSG_KERNEL_FUSED = 3
 TSG_KERNEL_NONE = 4
+TSG_STEP_NO_STREAM = 1
+TSG_STEP_NO_FUSE = 2
 
 EXPORTED_SYMBOLS = (
     "tsg_last_error",
@@ -66,6 +68,7 @@ EXPORTED_SYMBOLS = (
     "tsg_fusion_enabled",
     "tsg_batch_lanes_workspace_bytes",
     "tsg_batch_run_lanes",
+    "tsg_plan_set_step_options",
 )
 
 
@@ -156,6 +159,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_batch_run_lanes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
                                         POINTER(c_uint32), POINTER(c_void_p), _i64p, c_int32,
                                         c_void_p, c_int64, POINTER(c_void_p), c_void_p]
+    lib.tsg_plan_set_step_options.restype = c_int32
+    lib.tsg_plan_set_step_options.argtypes = [c_void_p, c_int32, _i32p]
     lib.tsg_plan_launches.restype = c_int32
     lib.tsg_plan_launches.argtypes = [c_void_p, c_int32, c_int32, c_int64, c_int64, c_int64,
                                       _i64p]

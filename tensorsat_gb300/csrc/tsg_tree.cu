@@ -159,7 +159,10 @@ struct tsg_plan {
   int num_sliced = 0;
   int root_bits = 0;
   int64_t max_entry_bits = 0;
-  std::vector<tsg::Layout> layouts;  // cache keyed by (group, elem_bytes, planes)
+  std::vector<tsg::Layout> layouts;  // cache keyed by (group, elem_bytes, planes, fusion)
+  // per-step kernel options of each ring (TSG_STEP_*; tsg_plan_set_step_options), indexed
+  // by ring; empty = none set
+  std::vector<int32_t> options[3];
 };
 
 namespace tsg {
@@ -184,6 +187,13 @@ tsg_status elem_info(int32_t ring, int32_t num_primes, int64_t* elem_bytes, int*
     default:
       return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: unknown ring");
   }
+}
+
+// Kernel options of step s in the ring of a layout's element size (0 when none are set).
+int32_t step_option(const tsg_plan* plan, int64_t elem_bytes, int s) {
+  const int ring = elem_bytes == 1 ? TSG_RING_OR_AND : (elem_bytes == 8 ? TSG_RING_U64 : TSG_RING_MODP);
+  const std::vector<int32_t>& o = plan->options[ring];
+  return o.empty() ? 0 : o[s];
 }
 
 // Live (unsliced) bits of operand v: a leaf's rank less its sliced bits, or a step's
@@ -227,6 +237,7 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
       const int p = -v - 1;
       const StepInfo& ps = steps[p];
       if (ps.dep != cs.dep || ps.k_bits > 1 || fused_from[p] >= 0) continue;
+      if (step_option(plan, elem_bytes, p) & TSG_STEP_NO_FUSE) continue;
       if (ps.out_bits < 16) continue;
       if (!rank_ok(ps.op[0]) || !rank_ok(ps.op[1]) || !rank_ok(cs.op[1 - xo])) continue;
       int carried[2] = {0, 0};
@@ -1011,7 +1022,7 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
       return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused step outside the tile kernel");
     return build_fused(c, s, base, tb, la);
   }
-  if (ok) {
+  if (ok && !(step_option(plan, c.lay->elem_bytes, s) & TSG_STEP_NO_STREAM)) {
     uint64_t extent[2];
     for (int o = 0; o < 2; ++o)
       extent[o] = la->is_leaf[o] ? 0 : (uint64_t)c.lay->plane[-st.op[o] - 1];
@@ -1547,6 +1558,27 @@ tsg_status tsg_plan_launches(const tsg_plan* plan, int32_t ring, int32_t num_pri
     if (!lay->fused_away[s]) (plan->steps[s].dep ? dep : indep)++;
   const int64_t groups = (slice_end - slice_begin + group_size - 1) / group_size;
   *count_out = plan->steps.back().dep ? indep + groups * (dep + 1) : indep + 1;
+  return TSG_OK;
+}
+
+tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring, const int32_t* options) {
+  if (!plan) return fail(TSG_ERR_INVALID_ARGUMENT, "set_step_options: null plan");
+  if (ring != TSG_RING_OR_AND && ring != TSG_RING_MODP && ring != TSG_RING_U64)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "set_step_options: unknown ring");
+  const size_t ns = plan->steps.size();
+  if (options) {
+    for (size_t i = 0; i < ns; ++i)
+      if (options[i] & ~(TSG_STEP_NO_STREAM | TSG_STEP_NO_FUSE))
+        return fail(TSG_ERR_INVALID_ARGUMENT, "set_step_options: unknown option bit");
+    plan->options[ring].assign(options, options + ns);
+  } else {
+    plan->options[ring].clear();
+  }
+  // layouts depend on the fusion choices: drop the cached ones of this ring
+  const int64_t eb = ring == TSG_RING_OR_AND ? 1 : (ring == TSG_RING_U64 ? 8 : 4);
+  plan->layouts.erase(std::remove_if(plan->layouts.begin(), plan->layouts.end(),
+                                     [&](const Layout& l) { return l.elem_bytes == eb; }),
+                      plan->layouts.end());
   return TSG_OK;
 }
 

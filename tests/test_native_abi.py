@@ -310,3 +310,76 @@ def test_wait_limit_setting_is_range_checked():
     finally:
         assert lib.tsg_set_wait_limit_ns(default) == _native.TSG_OK
     assert lib.tsg_debug_stall_producer(-5) == _native.TSG_OK  # off
+
+
+def test_step_options_change_kernel_choices_not_plans():
+    """Per-step options (the autotuner's choices): TSG_STEP_NO_STREAM puts a streamed step
+    on the tile kernel, TSG_STEP_NO_FUSE keeps a fused producer out of its consumer (its
+    result is stored again, so the workspace grows); clearing restores the executor's
+    choices. Unknown bits are rejected."""
+    import json
+
+    from tensorsat_gb300 import autotune
+
+    plan = json.loads((HEADER.parent.parent / "plans" / "3sat_n60_m256_rng0_t26.json").read_text())
+    cnf = CNFInstance.random(3, 60, 256, rng=0)
+    c = GpuContraction.from_plan(CudaRel, cnf.clause_diagram().wiring, plan)
+    npl = c.native_plan()
+    ring, primes = _native.TSG_RING_MODP, PRIMES_31[:3]
+    base = npl.describe(ring, primes, 64)
+    ws = npl.workspace_bytes(ring, 3, 64)
+    streamed = [s for s in range(npl.num_steps) if base[s][0] == _native.TSG_KERNEL_STREAM]
+    fused = npl.fused_steps(ring, primes, 64, c.tree)
+    assert streamed and fused
+    opts = [0] * npl.num_steps
+    opts[streamed[0]] = _native.TSG_STEP_NO_STREAM
+    p = next(iter(fused.values()))
+    opts[p] = _native.TSG_STEP_NO_FUSE
+    try:
+        autotune.set_options(c, ring, opts)
+        got = npl.describe(ring, primes, 64)
+        assert got[streamed[0]][0] == _native.TSG_KERNEL_TILE
+        assert got[p][0] != _native.TSG_KERNEL_NONE
+        assert npl.workspace_bytes(ring, 3, 64) > ws
+        # other rings keep their own (empty) options
+        assert (npl.describe(_native.TSG_RING_U64, (), 64)[p][0]) == _native.TSG_KERNEL_NONE
+        npl.validate(ring, primes, 0, 128, 64)
+        bad = list(opts)
+        bad[0] = 8
+        with pytest.raises(_native.TsgValueError):
+            autotune.set_options(c, ring, bad)
+    finally:
+        autotune.set_options(c, ring, None)
+    assert (npl.describe(ring, primes, 64) == base).all()
+    assert npl.workspace_bytes(ring, 3, 64) == ws
+
+
+def test_tuning_cache_round_trip(tmp_path):
+    """A cached tuning entry is found under its plan, ring, moduli and GPU name, and
+    applying it sets its options and returns its group."""
+    import json
+
+    from tensorsat_gb300 import autotune
+
+    cnf = CNFInstance.random(3, 30, 128, rng=0)
+    c = _plan_for(cnf, 14)
+    npl = c.native_plan()
+    ring, primes = _native.TSG_RING_MODP, PRIMES_31[:3]
+    opts = [_native.TSG_STEP_NO_STREAM] * npl.num_steps
+    entry = {"ring": ring, "primes": list(primes), "group": 4, "options": opts}
+    path = tmp_path / "plan.tune.json"
+    path.write_text(json.dumps({"format": autotune.TUNE_FORMAT, "entries": {
+        autotune.entry_key(c, ring, primes, "GB300 test"): entry}}))
+    assert autotune.load(path, c, ring, primes, gpu="other GPU") is None
+    assert autotune.load(path, c, _native.TSG_RING_U64, (), gpu="GB300 test") is None
+    got = autotune.load(path, c, ring, primes, gpu="GB300 test")
+    assert got == entry
+    try:
+        assert autotune.apply(c, got) == 4
+        kinds = npl.describe(ring, primes, 4)
+        assert all(k[0] != _native.TSG_KERNEL_STREAM for k in kinds)
+    finally:
+        autotune.set_options(c, ring, None)
+    (tmp_path / "bad.json").write_text('{"format": "x"}')
+    with pytest.raises(ValueError):
+        autotune.load(tmp_path / "bad.json", c, ring, primes, gpu="GB300 test")
