@@ -42,6 +42,22 @@ def _ptr_array(values: Sequence[int]) -> Any:
     return (ctypes.c_void_p * max(1, len(values)))(*values)
 
 
+def _host_results(results: Sequence[torch.Tensor]) -> list[np.ndarray]:
+    """Host copies of the results of a batch: their bytes gathered on the device, then one
+    device-to-host copy, then a numpy view of each result."""
+    if not results:
+        return []
+    raw = [r.reshape(-1).view(torch.uint8) for r in results]
+    flat = torch.cat(raw).cpu().numpy()
+    out, off = [], 0
+    for r, b in zip(results, raw):
+        n = b.numel()
+        dt = {torch.uint8: np.uint8, torch.int32: np.int32, torch.int64: np.int64}[r.dtype]
+        out.append(flat[off: off + n].view(dt).reshape(tuple(r.shape)).copy())
+        off += n
+    return out
+
+
 class BatchGraph:
     """A captured batch run: :meth:`replay` reruns every instance of the batch into the
     same result buffers with one graph launch."""
@@ -166,17 +182,23 @@ class BatchContraction:
         return int(out.value)
 
     def _results(self, ring: int, planes: int) -> list[torch.Tensor]:
+        """One result buffer per instance, as views into one flat device buffer (16-byte
+        aligned slots), so that all results come back to the host in one copy
+        (:func:`_host_results`)."""
         dev = _device.require_cuda()
-        res = []
+        dtype = {_native.TSG_RING_OR_AND: torch.uint8, _native.TSG_RING_U64: torch.int64}.get(
+            ring, torch.int32)
+        esize = torch.tensor([], dtype=dtype).element_size()
+        sizes = []
         for c in self._contractions:
             entries = 1 << len(c._leaves.out_unique)
-            if ring == _native.TSG_RING_OR_AND:
-                res.append(torch.zeros(entries, dtype=torch.uint8, device=dev))
-            elif ring == _native.TSG_RING_U64:
-                res.append(torch.zeros(entries, dtype=torch.int64, device=dev))
-            else:
-                res.append(torch.zeros(planes * entries, dtype=torch.int32, device=dev))
-        return res
+            sizes.append(entries * (planes if ring == _native.TSG_RING_MODP else 1))
+        offsets, off = [], 0
+        for n in sizes:
+            offsets.append(off)
+            off += (n * esize + 15) // 16 * 16
+        flat = torch.zeros(max(off, 16), dtype=torch.uint8, device=dev)
+        return [flat[o: o + n * esize].view(dtype) for o, n in zip(offsets, sizes)]
 
     def _call(self, ring: int, primes: Sequence[int], groups: Sequence[int],
               workspace: torch.Tensor, results: Sequence[torch.Tensor], stream: int) -> list:
@@ -259,14 +281,15 @@ class BatchContraction:
     def contract(self, groups: Sequence[int] | None = None, *, graph: bool = False,
                  workspace: torch.Tensor | None = None) -> list[CudaRel]:
         """OR-AND contraction of every diagram: one result box per diagram (a scalar box
-        for a SAT network: ``bool(box)`` is its SAT bit). ``graph=True`` replays a graph
-        captured on the first such call (see :meth:`load` for new inputs)."""
+        for a SAT network: ``bool(box)`` is its SAT bit), read back to the host in one
+        copy. ``graph=True`` replays a graph captured on the first such call (see
+        :meth:`load` for new inputs)."""
         if graph:
-            res = [r.clone() for r in self._replay(_native.TSG_RING_OR_AND, (), groups,
-                                                   workspace)]
+            res = self._replay(_native.TSG_RING_OR_AND, (), groups, workspace)
         else:
             res = self.run(_native.TSG_RING_OR_AND, groups=groups, workspace=workspace)
-        return [c._box_from_root(r) for c, r in zip(self._contractions, res)]
+        host = _host_results(res)
+        return [c._box_from_root(torch.from_numpy(h)) for c, h in zip(self._contractions, host)]
 
     def count_bounds(self) -> list[float]:
         """log2 upper bound on each diagram's model count (free variables of its oriented
@@ -312,8 +335,8 @@ class BatchContraction:
         else:
             res = self.run(_native.TSG_RING_MODP, primes, groups=groups, workspace=workspace)
         out = []
-        for c, r in zip(self._contractions, res):
-            planes = r.cpu().numpy().view(np.uint32).reshape(num_primes, -1)
+        for c, h in zip(self._contractions, _host_results(res)):
+            planes = h.view(np.uint32).reshape(num_primes, -1)
             counts = crt([planes[p] for p in range(num_primes)], primes)
             out.append(c._counts_from_root(counts))
         return out
