@@ -30,6 +30,9 @@ def test_stalled_producer_times_out_and_the_next_run_is_exact(cuda):
     d = cnf.clause_diagram()
     c = GpuContraction(CudaRel, d.wiring, target_bits=22, trials=2, seed=0)
     primes = PRIMES_31[:3]
+    # fused steps off for this plan's layouts, so that its largest step streams
+    fusion = lib.tsg_fusion_enabled()
+    lib.tsg_set_fusion(0)
     kinds = c.native_plan().describe(_native.TSG_RING_MODP, primes, 4)
     assert any(k[0] == _native.TSG_KERNEL_STREAM for k in kinds), "no streamed step"
     stream = _device.stream_handle()
@@ -45,6 +48,7 @@ def test_stalled_producer_times_out_and_the_next_run_is_exact(cuda):
     finally:
         lib.tsg_debug_stall_producer(-1)
         lib.tsg_set_wait_limit_ns(default)
+        lib.tsg_set_fusion(fusion)
     expected = orc.dpll_count(cnf.num_vars, cnf.clauses)[0]
     assert c.count(d, ring="modp", num_primes=3, group=4) == expected
     assert c.count(d, ring="u64", group=4) == expected

@@ -33,10 +33,12 @@ def lib():
     lib.tsg_set_fusion(1)
 
 
-def _random_leaves(cnf, seed):
+def _random_leaves(cnf, seed, density=0.99):
+    """Random {0,1} leaves on the clause network's wiring, each entry 1 with probability
+    ``density``: dense enough that hundreds of leaves still leave a large count."""
     d0 = cnf.clause_diagram()
     rng = np.random.default_rng(seed)
-    arrays = [rng.integers(0, 2, size=leaf_array(b).shape).astype(np.uint8) for b in d0.blocks]
+    arrays = [(rng.random(leaf_array(b).shape) < density).astype(np.uint8) for b in d0.blocks]
     return Diagram._new(d0.wiring, tuple(CudaRel(a) for a in arrays)), arrays
 
 
@@ -70,7 +72,7 @@ def test_fused_equals_unfused_and_the_oracle(cuda, lib, k, n, m, seed, target):
     assert results[1] == results[0]
     total_u64, total_modp, per_slice, per_slice_modp = results[1]
     assert total_u64 == total_modp > 0
-    assert per_slice == per_slice_modp
+    assert per_slice == per_slice_modp and all(x > 0 for x in per_slice)
     leaf_wires = [tuple(ws) for ws in d.wiring.slot_wires_list]
     for s, got in zip(probe[:2], per_slice[:2]):
         fixed = {w: (s >> j) & 1 for j, w in enumerate(c.sliced_wires)}

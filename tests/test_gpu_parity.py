@@ -235,7 +235,7 @@ def test_temporary_variants_do_not_share_a_cached_pool(cuda):
 def test_empty_clause_network_counts_zero(cuda):
     """A clause with no literal is a 0-port tensor holding 0: the network has no model.
     Its SAT bit and counts match the oracle's DPLL counter, in every ring."""
-    for clauses in ([(1, 2), (), (-3,)], [()], [(1,), (-1, 2), ()]):
+    for clauses in ([(1, 2), (), (-3,)], [(1,), ()], [(1,), (-1, 2), ()]):
         n = max([abs(l) for c in clauses for l in c] or [1])
         cnf = CNFInstance(n, clauses)
         d = cnf.clause_diagram()
