@@ -81,6 +81,8 @@ def parse_args():
     p.add_argument("--tune", action="store_true",
                    help="run the autotuner for the n=60 plan when its tuning file has no "
                         "entry for this GPU, and store the entry")
+    p.add_argument("--tune-file", default=str(TUNE_FILE),
+                   help="tuning file of the n=60 plan (read, and written by --tune)")
     p.add_argument("--no-tuning", action="store_true",
                    help="ignore the committed tuning (the executor's own kernel choices)")
     p.add_argument("--no-instance", action="store_true",
@@ -350,12 +352,13 @@ def run_gb300(args) -> None:
     if committed_plan(args) is not None and not args.no_tuning:
         from tensorsat_gb300 import autotune
 
-        entries = {r: autotune.load(TUNE_FILE, contraction, r, p)
+        tune_file = Path(args.tune_file)
+        entries = {r: autotune.load(tune_file, contraction, r, p)
                    for r, p in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ()))}
         if args.tune and any(e is None for e in entries.values()):
             free, _ = torch.cuda.mem_get_info()
             for r, p in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ())):
-                entries[r] = autotune.load_or_tune(TUNE_FILE, contraction, diagram, r, p,
+                entries[r] = autotune.load_or_tune(tune_file, contraction, diagram, r, p,
                                                    budget_bytes=int(free * 0.4))
         if all(e is not None for e in entries.values()):
             for e in entries.values():

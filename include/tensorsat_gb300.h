@@ -264,6 +264,8 @@ TSG_API tsg_status tsg_plan_validate(const tsg_plan* plan, int32_t ring, int32_t
 #define TSG_KERNEL_FUSED 3   /* fused kernel: a tile-form step that computes its reused operand
                                 from that operand's own two operands (see tsg_set_fusion) */
 #define TSG_KERNEL_NONE 4    /* no launch: the step's result is computed inside its consumer */
+#define TSG_KERNEL_SUM 5     /* few outputs, many summed combinations: one block per output,
+                                its threads split the sum */
 
 /* For every tree step s, the kernel tsg_plan_run launches for it with these arguments
  * (the first slice group of size group_size, 1 <= group_size <= slices), as four int32

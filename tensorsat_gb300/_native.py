@@ -34,6 +34,7 @@ TSG_KERNEL_TILE = 1
 TSG_KERNEL_STREAM = 2
 TSG_KERNEL_FUSED = 3
 TSG_KERNEL_NONE = 4
+TSG_KERNEL_SUM = 5
 TSG_STEP_NO_STREAM = 1
 TSG_STEP_NO_FUSE = 2
 

@@ -216,6 +216,9 @@ int live_bits(const tsg_plan* plan, int v) {
 //     least two F bits (4 positions per thread) and at most 30 output bits, every tensor
 //     involved has at most 31 bits, and both steps depend on the slice alike;
 //   - P expands its operands: 2^bits(P) >= 2^16 and >= 4 x (entries of A + entries of B);
+//   - s's other operand C is small (the tile form re-reads it per thread), or, in the
+//     count rings, P carries s's 10 fastest F bits as its own bits 0-9 (s can stream,
+//     staging C and computing P in its consumer warps);
 //   - neither p's operands nor s take part in another fusion (decided in step order).
 // Returns fused_from[s] = p or -1.
 std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem_bytes) {
@@ -250,6 +253,23 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
       const double ab = std::ldexp(1.0, live_bits(plan, ps.op[0])) +
                         std::ldexp(1.0, live_bits(plan, ps.op[1]));
       if (pe < 4.0 * ab) continue;
+      // The tile form reads the consumer's other operand C per thread and E combination:
+      // it must stay small (cache resident). Count rings may instead stream the fused
+      // step, which stages C: P must then carry s's 10 fastest F bits as its bits 0-9.
+      const int c_bits = live_bits(plan, cs.op[1 - xo]);
+      const bool c_small = c_bits <= (elem_bytes == 1 ? 24 : 20);
+      bool streamable = false;
+      if (elem_bytes != 1) {
+        int f = 0;
+        streamable = true;
+        for (int i = 0; i < cs.out_bits && f < kStreamTileBits; ++i) {
+          if (cs.pos[xo][i] < 0) continue;  // an E bit
+          streamable = streamable && cs.pos[xo][i] == f;
+          ++f;
+        }
+        streamable = streamable && f == kStreamTileBits;
+      }
+      if (!c_small && !streamable) continue;
       fused_from[s] = p;
       away[p] = 1;
       break;
@@ -358,9 +378,31 @@ void launch_step_t(const StepArgs& a, const RingArgs& ra, cudaStream_t st) {
   tree_step_kernel<kRing, kL, kR><<<grid_for(a.total, kThreads, 8), kThreads, 0, st>>>(a, ra);
 }
 
+template <int kRing, bool kL, bool kR>
+void launch_sum_t(const StepArgs& a, const RingArgs& ra, cudaStream_t st) {
+  const unsigned blocks = (unsigned)std::min<uint64_t>(a.total, (uint64_t)device_sm_count() * 16);
+  tree_step_sum_kernel<kRing, kL, kR><<<blocks, kThreads, 0, st>>>(a, ra);
+}
+
+// A step of the general form with few outputs and many summed combinations runs one block
+// per output (tree_step_sum_kernel); every other one thread per output.
+bool use_sum_kernel(const StepArgs& a) {
+  return a.k_bits >= 6 && a.total <= (uint64_t)device_sm_count() * 32;
+}
+
 template <int kRing>
 void launch_step_ring(bool l_leaf, bool r_leaf, const StepArgs& a, const RingArgs& ra,
                       cudaStream_t st) {
+  if (use_sum_kernel(a)) {
+    if (l_leaf) {
+      if (r_leaf) launch_sum_t<kRing, true, true>(a, ra, st);
+      else launch_sum_t<kRing, true, false>(a, ra, st);
+    } else {
+      if (r_leaf) launch_sum_t<kRing, false, true>(a, ra, st);
+      else launch_sum_t<kRing, false, false>(a, ra, st);
+    }
+    return;
+  }
   if (l_leaf) {
     if (r_leaf) launch_step_t<kRing, true, true>(a, ra, st);
     else launch_step_t<kRing, true, false>(a, ra, st);
@@ -830,7 +872,11 @@ uint32_t stream_span(const LaunchArgs& la, int np, uint32_t esize, uint64_t exte
   return ok ? span : 0;
 }
 
-void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
+// With fused_big >= 0 the step is fused: operand fused_big (never stored) is the one the
+// kernel would stage, the consumer warps compute it instead, and a stage holds only the
+// other operand's blocks (which must then be stageable).
+void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2],
+                   int fused_big = -1) {
   if (ring == TSG_RING_OR_AND) return;
   const TileArgs& t = la.t;
   const TileShape& sh = la.shape;
@@ -840,9 +886,11 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   if (sh.v != 4 || t.n_k > 16 || t.tile_bits != kStreamTileBits || !t.o_contig)
     return;
   if (sh.tiles * la.cnt < (uint64_t)device_sm_count() * 8) return;  // too small to stream
+  if (fused_big >= 0 && t.n_k > 4) return;
   int big = -1;
   for (int o = 0; o < 2; ++o) {
     const TileOperand& op = t.op[o];
+    if (fused_big >= 0 && o != fused_big) continue;
     if (op.leaf || op.has_e) continue;
     if (op.f_lo.n != 1 || op.f_lo.src[0] != 0 || op.f_lo.dst[0] != 0 ||
         op.f_lo.len[0] != kStreamTileBits)
@@ -863,7 +911,9 @@ void choose_stream(LaunchArgs& la, int ring, int np, const uint64_t extent[2]) {
   la.stream.work = sh.tiles * la.cnt;
   la.stream.chunk_bytes = kStreamTile * esize;
   la.stream.s_span = stream_span(la, np, esize, extent[1 - big]);
-  const uint64_t stage = stream_stage_bytes(sh.ne, std::min(t.n_k, 4), la.stream.chunk_bytes,
+  if (fused_big >= 0 && la.stream.s_span == 0) return;
+  const uint64_t stage = stream_stage_bytes(sh.ne, std::min(t.n_k, 4),
+                                            fused_big >= 0 ? 0u : la.stream.chunk_bytes,
                                             la.stream.s_span, esize);
   if (2 * stage > kStreamBlockSmem) return;  // fewer than two stages fit
   la.stream.stage_bytes = (uint32_t)stage;
@@ -991,6 +1041,8 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   const StepInfo& st = plan->steps[s];
   StepArgs& a = la->a;
   std::memset(&a, 0, sizeof(a));
+  std::memset(&la->f, 0, sizeof(la->f));
+  la->nkp = 0;
   la->cnt = (uint64_t)(st.dep ? cnt : 1);
   a.total = la->cnt << st.out_bits;
   a.k_bits = st.k_bits;
@@ -1020,7 +1072,14 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   if (c.lay->fused_from[s] >= 0) {
     if (!ok)
       return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused step outside the tile kernel");
-    return build_fused(c, s, base, tb, la);
+    TSG_TRY(build_fused(c, s, base, tb, la));
+    if (!(step_option(plan, c.lay->elem_bytes, s) & TSG_STEP_NO_STREAM)) {
+      uint64_t extent[2];
+      for (int o = 0; o < 2; ++o)
+        extent[o] = la->is_leaf[o] ? 0 : (uint64_t)c.lay->plane[-st.op[o] - 1];
+      choose_stream(*la, c.ring, c.ring == TSG_RING_MODP ? c.ra.np : 1, extent, la->f.fx);
+    }
+    return TSG_OK;
   }
   if (ok && !(step_option(plan, c.lay->elem_bytes, s) & TSG_STEP_NO_STREAM)) {
     uint64_t extent[2];
@@ -1034,19 +1093,25 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
 tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   LaunchArgs la;
   TSG_TRY(build_step(c, s, base, cnt, &la));
-  if (la.fused) {
-    if (c.ring == TSG_RING_U64) TSG_TRY(launch_fused_u64(la, c.ra, c.stream));
-    else if (c.ring == TSG_RING_OR_AND) TSG_TRY(launch_fused_or_and(la, c.ra, c.stream));
-    else TSG_TRY(launch_fused_modp(la, c.ra, c.stream));
-    TSG_CUDA_TRY(cudaGetLastError());
-    return TSG_OK;
-  }
   if (la.streamed) {
     TSG_TRY(device_error_address(&la.stream.error));
     la.stream.wait_ns = g_wait_limit_ns.load(std::memory_order_relaxed);
     la.stream.stop_after = g_stall_after.load(std::memory_order_relaxed);
-    if (c.ring == TSG_RING_U64) TSG_TRY(launch_stream_u64(la, c.ra, c.stream));
-    else TSG_TRY(launch_stream_modp(la, c.ra, c.stream));
+    if (la.fused) {
+      if (c.ring == TSG_RING_U64) TSG_TRY(launch_stream_fused_u64(la, c.ra, c.stream));
+      else TSG_TRY(launch_stream_fused_modp(la, c.ra, c.stream));
+    } else if (c.ring == TSG_RING_U64) {
+      TSG_TRY(launch_stream_u64(la, c.ra, c.stream));
+    } else {
+      TSG_TRY(launch_stream_modp(la, c.ra, c.stream));
+    }
+    TSG_CUDA_TRY(cudaGetLastError());
+    return TSG_OK;
+  }
+  if (la.fused) {
+    if (c.ring == TSG_RING_U64) TSG_TRY(launch_fused_u64(la, c.ra, c.stream));
+    else if (c.ring == TSG_RING_OR_AND) TSG_TRY(launch_fused_or_and(la, c.ra, c.stream));
+    else TSG_TRY(launch_fused_modp(la, c.ra, c.stream));
     TSG_CUDA_TRY(cudaGetLastError());
     return TSG_OK;
   }
@@ -1069,7 +1134,8 @@ tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   switch (c.ring) {
     case TSG_RING_OR_AND:
       // every OR_AND operand is uint8, leaf or not
-      launch_step_t<TSG_RING_OR_AND, true, true>(a, c.ra, c.stream);
+      if (use_sum_kernel(a)) launch_sum_t<TSG_RING_OR_AND, true, true>(a, c.ra, c.stream);
+      else launch_step_t<TSG_RING_OR_AND, true, true>(a, c.ra, c.stream);
       break;
     case TSG_RING_U64:
       launch_step_ring<TSG_RING_U64>(la.is_leaf[0], la.is_leaf[1], a, c.ra, c.stream);
@@ -1164,7 +1230,7 @@ struct RunTimer {
 void describe_launch(const LaunchArgs& la, int ring, int32_t* out) {
   if (la.fused) {
     out[0] = TSG_KERNEL_FUSED;
-    out[1] = la.shape.v;
+    out[1] = la.streamed ? 0 : la.shape.v;  // 0: the fused streaming kernel
     out[2] = la.shape.ne == 1 || la.shape.ne == 2 ? la.shape.ne : 4;
     out[3] = la.shape.nk;
   } else if (la.streamed) {
@@ -1179,6 +1245,9 @@ void describe_launch(const LaunchArgs& la, int ring, int32_t* out) {
     out[1] = la.shape.v;
     out[2] = la.shape.ne == 1 || la.shape.ne == 2 ? la.shape.ne : 4;
     out[3] = nk == 1 || nk == 2 ? nk : (nk == 4 && ring == TSG_RING_OR_AND ? 4 : 0);
+  } else if (use_sum_kernel(la.a)) {
+    out[0] = TSG_KERNEL_SUM;
+    out[1] = out[2] = out[3] = 0;
   } else {
     out[0] = TSG_KERNEL_GENERAL;
     out[1] = out[2] = out[3] = 0;

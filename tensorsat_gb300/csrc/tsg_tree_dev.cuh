@@ -150,6 +150,83 @@ __global__ void __launch_bounds__(kThreads) tree_step_kernel(StepArgs a, RingArg
   }
 }
 
+// Steps with few output entries and many summed combinations (the last steps of a small
+// network sum every wire nothing else needs): one block per output entry, the block's
+// threads split the summed combinations and combine them in shared memory, instead of one
+// thread looping over all of them. MODP terms are kept as residues (Montgomery products
+// reduced one by one, sums reduced before they pass 2^62); counts of two leaves are
+// brought into Montgomery form at the end.
+template <int kRing, bool kLLeaf, bool kRLeaf>
+__global__ void __launch_bounds__(kThreads) tree_step_sum_kernel(StepArgs a, RingArgs ring) {
+  constexpr int PP = kRing == TSG_RING_MODP ? TSG_MAX_PRIMES : 1;
+  constexpr int leaves = (kLLeaf ? 1 : 0) + (kRLeaf ? 1 : 0);
+  __shared__ uint64_t red[PP][kThreads];
+  const uint64_t nk = 1ull << a.k_bits;
+  for (uint64_t t = blockIdx.x; t < a.total; t += gridDim.x) {
+    const uint64_t lo = a.l_base + scatter_bits(a.lt, t);
+    const uint64_t ro = a.r_base + scatter_bits(a.rt, t);
+    uint64_t part[PP];
+#pragma unroll
+    for (int p = 0; p < PP; ++p) part[p] = 0;
+    for (uint64_t kk = threadIdx.x; kk < nk; kk += blockDim.x) {
+      const uint64_t lko = lo + scatter_bits(a.lk, kk);
+      const uint64_t rko = ro + scatter_bits(a.rk, kk);
+      if constexpr (kRing == TSG_RING_OR_AND) {
+        part[0] |= (uint64_t)(a.lhs[lko] & a.rhs[rko]);
+      } else if constexpr (kRing == TSG_RING_U64) {
+        part[0] += load_elem<kLLeaf, uint64_t>(a.lhs, lko) * load_elem<kRLeaf, uint64_t>(a.rhs, rko);
+      } else {
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+          if (p < ring.np) {
+            const uint64_t l = load_elem<kLLeaf, uint32_t>(a.lhs, lko + (kLLeaf ? 0 : p * a.l_plane));
+            const uint64_t r = load_elem<kRLeaf, uint32_t>(a.rhs, rko + (kRLeaf ? 0 : p * a.r_plane));
+            const uint64_t prod = l * r;
+            part[p] += leaves == 0 ? (uint64_t)mont_redc(prod, ring.p[p], ring.pinv[p]) : prod;
+            if (part[p] >> 62) part[p] = barrett_reduce(part[p], ring.p[p], ring.m[p]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < PP; ++p) {
+      if constexpr (kRing == TSG_RING_MODP) {
+        if (p < ring.np) part[p] = barrett_reduce(part[p], ring.p[p], ring.m[p]);
+      }
+      red[p][threadIdx.x] = part[p];
+    }
+    __syncthreads();
+    for (int half = blockDim.x / 2; half > 0; half >>= 1) {
+      if ((int)threadIdx.x < half) {
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+          if constexpr (kRing == TSG_RING_OR_AND) red[p][threadIdx.x] |= red[p][threadIdx.x + half];
+          else red[p][threadIdx.x] += red[p][threadIdx.x + half];  // MODP: 256 terms < 2^31
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      if constexpr (kRing == TSG_RING_OR_AND) {
+        a.out[t] = red[0][0] ? 1 : 0;
+      } else if constexpr (kRing == TSG_RING_U64) {
+        reinterpret_cast<uint64_t*>(a.out)[t] = red[0][0];
+      } else {
+        uint32_t* out = reinterpret_cast<uint32_t*>(a.out);
+#pragma unroll
+        for (int p = 0; p < PP; ++p) {
+          if (p < ring.np) {
+            uint64_t v = barrett_reduce(red[p][0], ring.p[p], ring.m[p]);
+            if (leaves == 2) v = barrett_reduce(v * ring.r1[p], ring.p[p], ring.m[p]);
+            out[t + p * a.o_plane] = (uint32_t)v;
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // Tile kernel: the common case where a slice's tensors have < 2^32 entries and at most
 // 4 wires are summed. Output bits split into three groups:
@@ -981,9 +1058,13 @@ __device__ __forceinline__ void stage_load(const TileOperand& op, const T* p, T 
   }
 }
 
-template <int kRing, int NE, int NK>
+// With NKP > 0 the kernel runs a fused step: the staged operand B is the result of a
+// step that is never stored, and the consumer warps compute its values from that step's
+// operands (FusedArgs, fused_x) instead of reading a staged tile; only the other operand
+// is staged.
+template <int kRing, int NE, int NK, int NKP>
 __global__ void __launch_bounds__(kStreamThreads, 3)
-    tree_step_stream_kernel(TileArgs a, RingArgs ring, StreamArgs sa) {
+    tree_step_stream_kernel(TileArgs a, RingArgs ring, StreamArgs sa, FusedArgs f) {
   using T = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
   constexpr int V = 4;
   constexpr int KU = NK;  // NK in {1, 2, 4}: 2^K summed combinations
@@ -995,7 +1076,7 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
   const TileOperand& B = a.op[sa.big];
   const TileOperand& S = a.op[1 - sa.big];
   const bool s_staged = sa.s_span != 0;
-  const uint32_t b_bytes = (uint32_t)KU * sa.chunk_bytes;
+  const uint32_t b_bytes = NKP > 0 ? 0u : (uint32_t)KU * sa.chunk_bytes;
   const uint32_t s_chunk = sa.s_span * (uint32_t)sizeof(T);
   const int nst = sa.stages;
   const uint64_t items = sa.work * (uint64_t)np;  // (tile, slice, residue plane)
@@ -1017,7 +1098,8 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
     // lanes issue the bulk copies (KU tiles of B, NE x KU blocks of the other operand)
     const T* bsrc = reinterpret_cast<const T*>(B.ptr);
     const T* ssrc = reinterpret_cast<const T*>(S.ptr);
-    const int ncopies = KU + (s_staged ? NE * KU : 0);
+    const int nb_copies = NKP > 0 ? 0 : KU;  // tiles of B per stage (none when fused)
+    const int ncopies = nb_copies + (s_staged ? NE * KU : 0);
     const uint64_t stride = gridDim.x;
     uint64_t i = 0;  // items issued by this block
     bool stop = false;
@@ -1068,11 +1150,11 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
           __syncwarp();
           const int kb = kc * KU;
           for (int c = lane; c < ncopies; c += 32) {
-            if (c < KU) {
+            if (c < nb_copies) {
               tma_load_1d(dst + c * sa.chunk_bytes, bsrc + bo + B.k_off[kb + c], sa.chunk_bytes,
                           &full[s]);
             } else {
-              const int j = c - KU;
+              const int j = c - nb_copies;
               const int e = j / KU, ku = j % KU;
               tma_load_1d(dst + b_bytes + j * s_chunk, ssrc + so + S.e_off[e] + S.k_off[kb + ku],
                           s_chunk, &full[s]);
@@ -1094,6 +1176,9 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
   // the other operand is read (its staged load mode, or global loads when not staged)
   const uint32_t f_lo = threadIdx.x * V;
   const uint64_t s_lo = scatter32(S.f_lo, f_lo);
+  // fused: the thread's position terms of the producer's operands
+  const uint64_t fa_lo = NKP > 0 ? scatter32(f.op[0].f_lo, f_lo) : 0;
+  const uint64_t fb_lo = NKP > 0 ? scatter32(f.op[1].f_lo, f_lo) : 0;
   const uint64_t o_lo = scatter32(a.of_lo, f_lo);
   // An item whose 2^K > 4 summed combinations span kchunks stages of KU = 4: partial sums
   // stay in registers (MODP: pairs of products reduced and added mod p; with a leaf
@@ -1198,7 +1283,7 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
     const int leaves = kSMode == kModeGlobal ? S.leaf : 0;
     uint64_t i = 0;  // stages consumed
     for (uint64_t w = blockIdx.x; w < items; w += gridDim.x, ++i) {
-      if constexpr (KU == 4) {
+      if constexpr (KU == 4 && NKP == 0) {
         if (sa.kchunks > 1) {  // the item spans kchunks stages
           if (!consume_chunked(i, leaves, mode_c)) return;
           --i;  // consume_chunked advanced i past the item's stages
@@ -1219,22 +1304,39 @@ __global__ void __launch_bounds__(kStreamThreads, 3)
       const PlaneConst pc = plane_const(ring, head[s].p);
       const uint8_t* st = smem + (size_t)s * sa.stage_bytes;
       T bv[KU][V];
+      if constexpr (NKP > 0) {
+        // fused: B's values for this item from the producer's operands (same item order
+        // as the producer warp: plane fastest, then tile, then slice)
+        const int pp = head[s].p;
+        const uint64_t tw = w / (uint64_t)np;
+        const uint32_t g = (uint32_t)(tw / sa.tiles);
+        const uint32_t f_hi = (uint32_t)(tw % sa.tiles) << kStreamTileBits;
+        const TileOperand& FA = f.op[0];
+        const TileOperand& FB = f.op[1];
+        const uint64_t a_p = FA.base + scatter_bits(FA.g, g) + scatter32(FA.f_hi, f_hi) + fa_lo +
+                             (FA.leaf ? 0 : pp * FA.plane);
+        const uint64_t b_p = FB.base + scatter_bits(FB.g, g) + scatter32(FB.f_hi, f_hi) + fb_lo +
+                             (FB.leaf ? 0 : pp * FB.plane);
 #pragma unroll
-      for (int ku = 0; ku < KU; ++ku) {
-        const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
-        if constexpr (sizeof(T) == 4) {
-          const uint4 x = *reinterpret_cast<const uint4*>(src);
-          bv[ku][0] = x.x;
-          bv[ku][1] = x.y;
-          bv[ku][2] = x.z;
-          bv[ku][3] = x.w;
-        } else {
-          const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
-          const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
-          bv[ku][0] = x0.x;
-          bv[ku][1] = x0.y;
-          bv[ku][2] = x1.x;
-          bv[ku][3] = x1.y;
+        for (int ku = 0; ku < KU; ++ku) fused_x<kRing, V, NKP>(f, a_p, b_p, ku, pc, bv[ku]);
+      } else {
+#pragma unroll
+        for (int ku = 0; ku < KU; ++ku) {
+          const T* src = reinterpret_cast<const T*>(st + ku * sa.chunk_bytes) + f_lo;
+          if constexpr (sizeof(T) == 4) {
+            const uint4 x = *reinterpret_cast<const uint4*>(src);
+            bv[ku][0] = x.x;
+            bv[ku][1] = x.y;
+            bv[ku][2] = x.z;
+            bv[ku][3] = x.w;
+          } else {
+            const ulonglong2 x0 = reinterpret_cast<const ulonglong2*>(src)[0];
+            const ulonglong2 x1 = reinterpret_cast<const ulonglong2*>(src)[1];
+            bv[ku][0] = x0.x;
+            bv[ku][1] = x0.y;
+            bv[ku][2] = x1.x;
+            bv[ku][3] = x1.y;
+          }
         }
       }
       const T* ss = reinterpret_cast<const T*>(st + b_bytes) + s_lo;
@@ -1386,6 +1488,8 @@ tsg_status launch_stream_u64(const LaunchArgs& la, const RingArgs& ra, cudaStrea
 tsg_status launch_fused_modp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_fused_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_fused_or_and(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
+tsg_status launch_stream_fused_modp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
+tsg_status launch_stream_fused_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 
 }  // namespace dev
 }  // namespace tsg

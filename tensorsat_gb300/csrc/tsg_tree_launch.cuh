@@ -62,9 +62,9 @@ void launch_tile_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st)
   else launch_tile_ne<kRing, 1>(la, ra, st);
 }
 
-template <int kRing, int NE, int NK>
+template <int kRing, int NE, int NK, int NKP = 0>
 tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  auto kernel = tree_step_stream_kernel<kRing, NE, NK>;
+  auto kernel = tree_step_stream_kernel<kRing, NE, NK, NKP>;
   const size_t smem = (size_t)la.stream.stages * la.stream.stage_bytes;
   if (la.stream.stages < 2 || la.stream.stages > kStreamMaxStages || smem > kStreamBlockSmem)
     return fail(TSG_ERR_INVALID_ARGUMENT, "stream kernel: stage ring outside its limits");
@@ -80,7 +80,7 @@ tsg_status launch_stream_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_
   const int np = kRing == TSG_RING_MODP ? ra.np : 1;
   const uint64_t blocks = std::min<uint64_t>(la.stream.work * np,
                                              (uint64_t)device_sm_count() * kStreamBlocksPerSm);
-  kernel<<<(unsigned)blocks, kStreamThreads, smem, st>>>(la.t, ra, la.stream);
+  kernel<<<(unsigned)blocks, kStreamThreads, smem, st>>>(la.t, ra, la.stream, la.f);
   return TSG_OK;
 }
 
@@ -90,6 +90,29 @@ tsg_status launch_stream_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream
     case 1: return launch_stream_t<kRing, NE, 1>(la, ra, st);
     case 2: return launch_stream_t<kRing, NE, 2>(la, ra, st);
     default: return launch_stream_t<kRing, NE, 4>(la, ra, st);
+  }
+}
+
+// Fused streaming steps: the consumer's summed count NK in {1, 2, 4} (one stage per item)
+// and the producer's NKP in {1, 2}.
+template <int kRing, int NE>
+tsg_status launch_stream_fused_nk(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  if (la.t.n_k > 4 || la.stream.kchunks != 1 || la.nkp < 1 || la.nkp > 2)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "fused stream kernel: shape outside its instantiations");
+  const bool two = la.nkp == 2;
+  switch (la.t.n_k) {
+    case 1: return two ? launch_stream_t<kRing, NE, 1, 2>(la, ra, st) : launch_stream_t<kRing, NE, 1, 1>(la, ra, st);
+    case 2: return two ? launch_stream_t<kRing, NE, 2, 2>(la, ra, st) : launch_stream_t<kRing, NE, 2, 1>(la, ra, st);
+    default: return two ? launch_stream_t<kRing, NE, 4, 2>(la, ra, st) : launch_stream_t<kRing, NE, 4, 1>(la, ra, st);
+  }
+}
+
+template <int kRing>
+tsg_status launch_stream_fused_ring(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
+  switch (la.shape.ne) {
+    case 1: return launch_stream_fused_nk<kRing, 1>(la, ra, st);
+    case 2: return launch_stream_fused_nk<kRing, 2>(la, ra, st);
+    default: return launch_stream_fused_nk<kRing, 4>(la, ra, st);
   }
 }
 

@@ -198,6 +198,8 @@ def _profiled_kernels():
         name, args = m.group(1), [int(x) for x in m.group(2).split(",")]
         if name == "tree_step_tile_kernel":
             kind = (_native.TSG_KERNEL_TILE, args[1], args[2], args[3])
+        elif name == "tree_step_sum_kernel":
+            kind = (_native.TSG_KERNEL_SUM, 0, 0, 0)
         elif name == "tree_step_fused_kernel":
             kind = (_native.TSG_KERNEL_FUSED, 4, args[1], args[2])
         elif name == "tree_step_stream_kernel":
@@ -231,7 +233,7 @@ def test_kernel_choice_matches_the_profiled_launches():
     kinds = got[_native.TSG_RING_MODP][:, 0]
     assert set(kinds) <= {_native.TSG_KERNEL_GENERAL, _native.TSG_KERNEL_TILE,
                           _native.TSG_KERNEL_STREAM, _native.TSG_KERNEL_FUSED,
-                          _native.TSG_KERNEL_NONE}
+                          _native.TSG_KERNEL_NONE, _native.TSG_KERNEL_SUM}
     with pytest.raises(_native.TsgValueError):
         npl.describe(_native.TSG_RING_OR_AND, (), c.num_slices + 1)
 
