@@ -6,7 +6,7 @@ contraction tree from the project's planner with every intermediate capped at 2^
 by slicing. The exact count is carried modulo three 31-bit primes (uint32 residue planes,
 CRT on the host); the SAT bit is the OR-AND contraction of the same tree.
 
-A *step* contracts one group of G slices of that instance in both rings (count and SAT
+A *step* contracts G slices of that instance in both rings (count and SAT
 bit). Every slice of an instance runs the same kernels on the same shapes, so
 ``instances/s = slices/s / slices per instance`` is exact for this instance. Inputs
 (leaves) are resident in HBM for ``value``; ``e2e`` goes through the public API
@@ -367,20 +367,31 @@ def run_gb300(args) -> None:
                       {"group": e["group"], "config": e["config"], "gain": round(e["gain"], 4),
                        "steps_changed": sum(1 for o in e["options"] if o)}
                       for r, e in entries.items()}
+    # slice groups: one per ring (the tuned ones when a tuning applies), and a step covers
+    # `group` slices (the larger of the two) in both rings
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(free * 0.75)
+
+    def fits(gm: int, go: int) -> bool:
+        return (npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, gm)
+                + npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, go)) <= budget
+
     if args.group:
-        group = args.group
+        g_modp = g_or = args.group
+    elif tuning is not None:
+        g_modp = min(ns, tuning["modp"]["group"])
+        g_or = min(ns, tuning["or_and"]["group"])
+        while g_or > g_modp and not fits(g_modp, g_or):
+            g_or //= 2
     else:
-        free, _ = torch.cuda.mem_get_info()
-        budget = int(free * 0.75)
-        group = min(ns, 256)
-        if tuning is not None:
-            group = min(group, tuning["modp"]["group"])
-        while group > 1 and (npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, group)
-                             + npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, group)) > budget:
-            group //= 2
-    ws_count = torch.empty(npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, group),
+        g_modp = min(ns, 256)
+        while g_modp > 1 and not fits(g_modp, g_modp):
+            g_modp //= 2
+        g_or = g_modp
+    group = max(g_modp, g_or)
+    ws_count = torch.empty(npl.workspace_bytes(_native.TSG_RING_MODP, NUM_PRIMES, g_modp),
                            dtype=torch.uint8, device=dev)
-    ws_sat = torch.empty(npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, group),
+    ws_sat = torch.empty(npl.workspace_bytes(_native.TSG_RING_OR_AND, 1, g_or),
                          dtype=torch.uint8, device=dev)
     pool_dev = contraction.leaf_pool(diagram)
     res_count = torch.zeros(NUM_PRIMES, dtype=torch.int32, device=dev)
@@ -395,9 +406,9 @@ def run_gb300(args) -> None:
 
     def step(i: int) -> None:
         b, e = slice_range(i)
-        npl.run(_native.TSG_RING_MODP, primes, pool_dev, b, e, group, ws_count, res_count,
+        npl.run(_native.TSG_RING_MODP, primes, pool_dev, b, e, g_modp, ws_count, res_count,
                 False, sh)
-        npl.run(_native.TSG_RING_OR_AND, (), pool_dev, b, e, group, ws_sat, res_sat, False, sh)
+        npl.run(_native.TSG_RING_OR_AND, (), pool_dev, b, e, g_or, ws_sat, res_sat, False, sh)
 
     for i in range(args.warmup):
         step(i)
@@ -421,9 +432,9 @@ def run_gb300(args) -> None:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed = float(t.item())
     value = world * args.steps * group / ns / elapsed
-    launches_per_step = (npl.launch_count(*slice_range(0), group, _native.TSG_RING_MODP,
+    launches_per_step = (npl.launch_count(*slice_range(0), g_modp, _native.TSG_RING_MODP,
                                           NUM_PRIMES)
-                         + npl.launch_count(*slice_range(0), group, _native.TSG_RING_OR_AND))
+                         + npl.launch_count(*slice_range(0), g_or, _native.TSG_RING_OR_AND))
 
     # Roofline of the dominant launch: one more pass over the next slice group with a CUDA
     # event after every launch (tsg_plan_run_timed); the tree step with the largest device
@@ -436,14 +447,15 @@ def run_gb300(args) -> None:
     timing_passes = 2
     acc_ms = {"modp": None, "or_and": None}
     for _ in range(timing_passes):
-        for name, ring, pr, ws, res in (("modp", _native.TSG_RING_MODP, primes, ws_count, res_count),
-                                        ("or_and", _native.TSG_RING_OR_AND, (), ws_sat, res_sat)):
-            ms = npl.run_timed(ring, pr, pool_dev, b, e, group, ws, res, False, sh)
+        for name, ring, pr, ws, res, g in (
+                ("modp", _native.TSG_RING_MODP, primes, ws_count, res_count, g_modp),
+                ("or_and", _native.TSG_RING_OR_AND, (), ws_sat, res_sat, g_or)):
+            ms = npl.run_timed(ring, pr, pool_dev, b, e, g, ws, res, False, sh)
             acc_ms[name] = ms if acc_ms[name] is None else [x + y for x, y in zip(acc_ms[name], ms)]
     # algorithmic bytes per step; a fused producer moves nothing, its consumer reads the
     # producer's operands instead of the producer's result
-    fused = {"modp": npl.fused_steps(_native.TSG_RING_MODP, primes, group, contraction.tree),
-             "or_and": npl.fused_steps(_native.TSG_RING_OR_AND, (), group, contraction.tree)}
+    fused = {"modp": npl.fused_steps(_native.TSG_RING_MODP, primes, g_modp, contraction.tree),
+             "or_and": npl.fused_steps(_native.TSG_RING_OR_AND, (), g_or, contraction.tree)}
     step_bytes = {"modp": sp.step_bytes_per_slice(4, NUM_PRIMES, fused["modp"]),
                   "or_and": sp.step_bytes_per_slice(1, 1, fused["or_and"])}
     nsteps = len(step_bytes["modp"])
@@ -453,7 +465,7 @@ def run_gb300(args) -> None:
     dom_bytes = step_bytes[ring_name][dom] * group
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     step_total_ms = sum(sum(v) for v in acc_ms.values()) / timing_passes
-    traffic = dominant_traffic(ring_name, dom, group)
+    traffic = dominant_traffic(ring_name, dom, g_modp if ring_name == "modp" else g_or)
     step_roofline = (sum(step_bytes["modp"]) + sum(step_bytes["or_and"])) * group / step_s / 1e9
 
     # end to end through the public API: host leaves in, host results out, every step
@@ -464,9 +476,9 @@ def run_gb300(args) -> None:
         b, e = slice_range(args.warmup + args.steps + k)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES, group=group,
+        contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES, group=g_modp,
                           slice_range=(b, e), cache_leaves=False)
-        bool(contraction.contract(diagram, group=group, slice_range=(b, e), cache_leaves=False))
+        bool(contraction.contract(diagram, group=g_or, slice_range=(b, e), cache_leaves=False))
         torch.cuda.synchronize()
         if k > 0:  # the first call allocates workspaces in torch's caching allocator
             e2e_times.append(time.perf_counter() - t0)
@@ -480,8 +492,8 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         full_count = contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES,
-                                       group=group, process_group=pg)
-        full_sat = bool(contraction.contract(diagram, group=group, process_group=pg))
+                                       group=g_modp, process_group=pg)
+        full_sat = bool(contraction.contract(diagram, group=g_or, process_group=pg))
         torch.cuda.synchronize()
         full_s = time.perf_counter() - t0
         instance = {"count": int(full_count), "sat": full_sat, "seconds": round(full_s, 3),
@@ -541,7 +553,8 @@ def run_gb300(args) -> None:
             "ms_per_step": 1000 * step_s, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32 residues mod 3 primes + u8 OR-AND",
             "data": "synthetic (seeded CNFInstance.random, no dataset)",
-            "config": workload_config(args, contraction, group),
+            "config": dict(workload_config(args, contraction, group),
+                           slice_groups={"modp": g_modp, "or_and": g_or}),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_kind,

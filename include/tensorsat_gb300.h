@@ -159,26 +159,34 @@ TSG_API tsg_status tsg_plan_launches(const tsg_plan* plan, int32_t ring, int32_t
                              int64_t slice_begin, int64_t slice_end, int64_t group_size,
                              int64_t* count_out);
 
-/* Fused steps, on (1, the default) or off (0), for plans whose layouts are made after the
- * call (layouts are made per plan, ring and group on first use and kept). In every ring
- * a step whose large result is read once, as the reused operand of its consumer's
- * tile form, is not launched: the consumer computes each entry it needs from the step's
- * two operands, so the result never exists in HBM (it is written and read back otherwise;
- * the conditions are in the library's choose_fusion). Results are identical either way;
- * fused plans need less workspace and move fewer bytes. Process-wide. No counterpart in
- * the reference, which runs one einsum per tree node (tensorsat/_autoray.py:31-62). */
+/* Fused steps, allowed (1, the default) or not (0), for plans whose layouts are made after
+ * the call (layouts are made per plan, ring and group on first use and kept). A step whose
+ * step options carry TSG_STEP_FUSE (tsg_plan_set_step_options; the autotuner sets it
+ * where fusing measured faster) and whose large result is read once, as the reused
+ * operand of its consumer's tile or streaming form, is not launched: the consumer computes
+ * each entry it needs from the step's two operands, so the result never exists in HBM
+ * (the structural conditions are in the library's choose_fusion). Results are identical
+ * either way; fused plans need less workspace and move fewer bytes, at the price of
+ * gathers in the consumer. Process-wide. No counterpart in the reference, which runs one
+ * einsum per tree node (tensorsat/_autoray.py:31-62). */
 TSG_API tsg_status tsg_set_fusion(int32_t enabled);
 TSG_API int32_t tsg_fusion_enabled(void);
 
 /* Per-step kernel options of a plan in one ring (the autotuner's choices): options[s] is
  * a bit set of TSG_STEP_NO_STREAM (run step s on the tile kernel even where the streaming
- * kernel applies) and TSG_STEP_NO_FUSE (never compute step s inside its consumer), for
- * every step (num_steps entries); options == NULL clears them. Later runs, workspace sizes
- * and descriptions of that ring follow them; results do not depend on them. Host only.
+ * kernel applies), TSG_STEP_NO_FUSE (never compute step s inside its consumer) and
+ * TSG_STEP_FUSE (compute step s inside its consumer where the structure allows it; no
+ * step is fused without it) and TSG_STEP_PLANE_LOOP, for every step (num_steps entries);
+ * options == NULL clears
+ * them. Later runs, workspace sizes and descriptions of that ring follow them; results do
+ * not depend on them. Host only.
  * No counterpart in the reference, whose path choice (cotengra's optimize/order kwargs,
  * tensorsat/contractions/cotengra.py:62-64,104-106) has no kernel to choose. */
 #define TSG_STEP_NO_STREAM 1
 #define TSG_STEP_NO_FUSE 2
+#define TSG_STEP_FUSE 4
+#define TSG_STEP_PLANE_LOOP 8 /* MODP tile kernel: every residue plane in one thread (default:
+                                 one plane per block) */
 TSG_API tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring,
                                      const int32_t* options);
 

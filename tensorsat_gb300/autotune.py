@@ -8,16 +8,17 @@ the tuner only looks for speed:
 
 1. For each candidate slice group (the largest that fits the memory budget and up to two
    halvings of it), it times one slice group of the plan with ``tsg_plan_run_timed`` (a
-   CUDA event after every launch) in two configurations: the executor's own choices, and
-   every step on the tile kernel with no fused step.
-2. Per step it keeps the faster kernel: a streamed step falls back to the tile kernel when
-   that was faster; a fused producer is unfused when its consumer alone (fused) took
-   longer than the producer plus its consumer unfused.
-3. It times the mixed configuration too and keeps the fastest of the three, per slice.
+   CUDA event after every launch) in four configurations: the executor's own choices; no
+   fused step; tile kernels only; every possible fusion (and, for residue counts, every
+   tile step with its residue planes in one thread instead of one plane per block).
+2. Per decision it keeps the faster alternative: a fusion when the fused consumer took
+   less than the producer plus its consumer unfused; a streamed step when it beat the
+   tile kernel; a tile step's plane split when it beat the in-thread plane loop.
+3. It times that mixed configuration too and keeps the fastest, per slice.
 
 The choice is a list of per-step options (``TSG_STEP_NO_STREAM``, ``TSG_STEP_NO_FUSE``,
-applied with ``tsg_plan_set_step_options``) and a group, stored with the timings under a
-key of the plan, the ring, the moduli and the GPU's name.
+``TSG_STEP_FUSE``, applied with ``tsg_plan_set_step_options``) and a group, stored with
+the timings under a key of the plan, the ring, the moduli and the GPU's name.
 """
 
 from __future__ import annotations
@@ -55,6 +56,12 @@ def set_options(contraction: Any, ring: int, options: Sequence[int] | None) -> N
         npl.handle, ring, None if arr is None else _native.ptr_i32(arr)))
 
 
+def fuse_all(contraction: Any, ring: int) -> None:
+    """Asks for every fusion the plan's structure allows in ``ring`` (TSG_STEP_FUSE on
+    every step)."""
+    set_options(contraction, ring, [_native.TSG_STEP_FUSE] * contraction.native_plan().num_steps)
+
+
 def _timed(contraction: Any, ring: int, primes: Sequence[int], pool: Any, begin: int,
            group: int, options: Sequence[int] | None, passes: int) -> tuple[list[float], list]:
     """Per-step device milliseconds (mean over ``passes`` after one warm-up pass) of one
@@ -86,7 +93,14 @@ def _timed(contraction: Any, ring: int, primes: Sequence[int], pool: Any, begin:
 def tune(contraction: Any, diagram: Any, ring: int, primes: Sequence[int] = (),
          budget_bytes: int | None = None, passes: int = 2, max_halvings: int = 2) -> dict:
     """Times the candidate configurations of ``contraction`` in ``ring`` on the current
-    GPU and returns the chosen entry (options, group, timings); the options stay applied."""
+    GPU and returns the chosen entry (options, group, timings); the options stay applied.
+
+    Configurations per candidate group: the executor's own choices; no fused step; no
+    fused and no streamed step (tile kernels only); every possible fusion (streamed fused
+    consumers included). Per decision the faster measured alternative is kept: a fusion
+    when its consumer took less time than producer plus consumer unfused, a streamed step
+    when it beat the tile kernel. The mixed configuration is timed too; the fastest
+    configuration per slice wins."""
     import torch
 
     npl = contraction.native_plan()
@@ -103,28 +117,47 @@ def tune(contraction: Any, diagram: Any, ring: int, primes: Sequence[int] = (),
         g //= 2
     n = npl.num_steps
     L = contraction.tree.num_leaves
-    plain = [_native.TSG_STEP_NO_STREAM | _native.TSG_STEP_NO_FUSE] * n
+    NS, NF, FU = _native.TSG_STEP_NO_STREAM, _native.TSG_STEP_NO_FUSE, _native.TSG_STEP_FUSE
+    PL = _native.TSG_STEP_PLANE_LOOP
+    configs = {"executor": [0] * n, "no_fuse": [NF] * n, "tile": [NS | NF] * n,
+               "fuse": [FU] * n}
+    if ring == _native.TSG_RING_MODP and len(primes) > 1:
+        configs["plane_loop"] = [NF | PL] * n
     trials = []
     for g in groups:
-        begin = 0
-        a_ms, a_kinds = _timed(contraction, ring, primes, pool, begin, g, None, passes)
-        b_ms, _ = _timed(contraction, ring, primes, pool, begin, g, plain, passes)
+        ms, kinds = {}, {}
+        for name, opts in configs.items():
+            ms[name], kinds[name] = _timed(contraction, ring, primes, pool, 0, g, opts, passes)
         mixed = [0] * n
+        # fusions: every pair the "fuse" configuration formed, kept when faster
         for s in range(n):
-            if a_kinds[s][0] == _native.TSG_KERNEL_STREAM and b_ms[s] < a_ms[s]:
-                mixed[s] |= _native.TSG_STEP_NO_STREAM
-            if a_kinds[s][0] == _native.TSG_KERNEL_FUSED:
-                prod = [x - L for x in contraction.tree.steps[s]
-                        if x >= L and a_kinds[x - L][0] == _native.TSG_KERNEL_NONE]
-                if prod and b_ms[s] + b_ms[prod[0]] < a_ms[s]:
-                    mixed[prod[0]] |= _native.TSG_STEP_NO_FUSE
-        c_ms, _ = _timed(contraction, ring, primes, pool, begin, g, mixed, passes)
+            if kinds["fuse"][s][0] != _native.TSG_KERNEL_FUSED:
+                continue
+            prod = [x - L for x in contraction.tree.steps[s]
+                    if x >= L and kinds["fuse"][x - L][0] == _native.TSG_KERNEL_NONE]
+            if not prod:
+                continue
+            p = prod[0]
+            if ms["fuse"][s] < ms["no_fuse"][s] + ms["no_fuse"][p]:
+                mixed[p] |= FU
+            else:
+                mixed[p] |= NF
+        # streaming: kept where it beat the tile kernel (unfused steps)
+        for s in range(n):
+            if kinds["no_fuse"][s][0] == _native.TSG_KERNEL_STREAM and \
+                    ms["tile"][s] < ms["no_fuse"][s]:
+                mixed[s] |= NS
+        # MODP tile steps: residue planes per block or all in one thread
+        if "plane_loop" in configs:
+            for s in range(n):
+                if kinds["no_fuse"][s][0] == _native.TSG_KERNEL_TILE and \
+                        ms["plane_loop"][s] < ms["no_fuse"][s] and not mixed[s] & NS:
+                    mixed[s] |= PL
+        ms["mixed"], _ = _timed(contraction, ring, primes, pool, 0, g, mixed, passes)
         slices = min(ns, g)
-        for name, opts, ms in (("executor", [0] * n, a_ms), ("tile", plain, b_ms),
-                               ("mixed", mixed, c_ms)):
+        for name, opts in list(configs.items()) + [("mixed", mixed)]:
             trials.append({"group": g, "config": name, "options": list(opts),
-                           "ms": sum(ms), "ms_per_slice": sum(ms) / slices,
-                           "step_ms": [round(x, 4) for x in ms]})
+                           "ms": sum(ms[name]), "ms_per_slice": sum(ms[name]) / slices})
     best = min(trials, key=lambda t: t["ms_per_slice"])
     base = next(t for t in trials if t["group"] == top and t["config"] == "executor")
     set_options(contraction, ring, best["options"])
@@ -134,7 +167,7 @@ def tune(contraction: Any, diagram: Any, ring: int, primes: Sequence[int] = (),
         "options": best["options"], "config": best["config"],
         "ms_per_slice": best["ms_per_slice"], "default_ms_per_slice": base["ms_per_slice"],
         "gain": base["ms_per_slice"] / best["ms_per_slice"],
-        "trials": [{k: v for k, v in t.items() if k != "step_ms"} for t in trials],
+        "trials": [{k: v for k, v in t.items() if k != "options"} for t in trials],
     }
 
 

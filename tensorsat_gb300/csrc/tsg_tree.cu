@@ -207,7 +207,9 @@ int live_bits(const tsg_plan* plan, int v) {
   return r;
 }
 
-// Fused steps of a layout (every ring): a step p whose result P is read by exactly
+// Fused steps of a layout (every ring), for producers whose step options ask for it
+// (TSG_STEP_FUSE; the autotuner sets it where fusing measured faster): a step p whose
+// result P is read by exactly
 // one consumer s is computed inside s, never stored, when
 //   - P carries every output bit of s but at most two (the enumerated E bits of s's tile
 //     form, so each entry of P is computed once per launch) and at least as many output
@@ -240,7 +242,8 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
       const int p = -v - 1;
       const StepInfo& ps = steps[p];
       if (ps.dep != cs.dep || ps.k_bits > 1 || fused_from[p] >= 0) continue;
-      if (step_option(plan, elem_bytes, p) & TSG_STEP_NO_FUSE) continue;
+      const int32_t popt = step_option(plan, elem_bytes, p);
+      if (popt & TSG_STEP_NO_FUSE) continue;
       if (ps.out_bits < 16) continue;
       if (!rank_ok(ps.op[0]) || !rank_ok(ps.op[1]) || !rank_ok(cs.op[1 - xo])) continue;
       int carried[2] = {0, 0};
@@ -269,7 +272,9 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
         }
         streamable = streamable && f == kStreamTileBits;
       }
-      if (!c_small && !streamable) continue;
+      // fused steps trade P's HBM round trip for gathers of A and B in the consumer: only
+      // where they were measured faster (TSG_STEP_FUSE on the producer, the autotuner's)
+      if (!(popt & TSG_STEP_FUSE) || (!c_small && !streamable)) continue;
       fused_from[s] = p;
       away[p] = 1;
       break;
@@ -1069,6 +1074,10 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   la->streamed = false;
   la->fused = false;
   if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
+  // MODP tile launches: one residue plane per block (more warps in flight) unless asked to
+  // keep the planes in one thread
+  la->t.plane_split = (ok && c.ring == TSG_RING_MODP && c.ra.np > 1 &&
+                       !(step_option(plan, c.lay->elem_bytes, s) & TSG_STEP_PLANE_LOOP)) ? 1 : 0;
   if (c.lay->fused_from[s] >= 0) {
     if (!ok)
       return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused step outside the tile kernel");
@@ -1637,7 +1646,8 @@ tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring, const int32_t
   const size_t ns = plan->steps.size();
   if (options) {
     for (size_t i = 0; i < ns; ++i)
-      if (options[i] & ~(TSG_STEP_NO_STREAM | TSG_STEP_NO_FUSE))
+      if (options[i] & ~(TSG_STEP_NO_STREAM | TSG_STEP_NO_FUSE | TSG_STEP_FUSE |
+                         TSG_STEP_PLANE_LOOP))
         return fail(TSG_ERR_INVALID_ARGUMENT, "set_step_options: unknown option bit");
     plan->options[ring].assign(options, options + ns);
   } else {

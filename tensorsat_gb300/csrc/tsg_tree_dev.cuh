@@ -290,6 +290,7 @@ struct TileArgs {
   int32_t tile_bits;
   int32_t n_k;             // summed combinations (2^k)
   int32_t o_contig;        // the V positions are consecutive outputs
+  int32_t plane_split;     // MODP: one residue plane per block (blockIdx.z), not all per thread
 };
 
 __device__ __forceinline__ uint32_t scatter32(const NarrowMap& m, uint32_t x) {
@@ -441,7 +442,8 @@ __device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t
 template <int kRing, int V, int NE, int NK>
 __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& ring,
                                             const TileOperand& X, const TileOperand& Y,
-                                            uint64_t x0, uint64_t y0, uint64_t oo) {
+                                            uint64_t x0, uint64_t y0, uint64_t oo,
+                                            int p_lo, int p_hi) {
   using T = typename std::conditional<kRing == TSG_RING_OR_AND, uint8_t,
             typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type>::type;
   using VT = typename std::conditional<kRing == TSG_RING_U64, uint64_t, uint32_t>::type;
@@ -505,10 +507,10 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
       }
     }
   } else {
-    // planes outermost; X of plane p+1 is loaded while plane p is combined
+    // planes [p_lo, p_hi) outermost; X of plane p+1 is loaded while plane p is combined
     constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
     constexpr bool kHoist = NK > 0 && NE * KU * V * sizeof(VT) <= 64;  // more spills registers
-    const int np = (kRing == TSG_RING_MODP) ? ring.np : 1;
+    const int np = p_hi;
     const int leaves = X.leaf + Y.leaf;
     VT xcur[KU][V], xnxt[KU][V];
     auto preload = [&](int p, VT (&xb)[KU][V]) {
@@ -516,9 +518,10 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
 #pragma unroll
       for (int ku = 0; ku < KU; ++ku) tile_load<T, VT, V>(X, xp + X.k_off[ku], xb[ku]);
     };
-    if (NK > 0) preload(0, xcur);
+    if (NK > 0) preload(p_lo, xcur);
 #pragma unroll
-    for (int p = 0; p < PP; ++p) {
+    for (int q = 0; q < PP; ++q) {
+      const int p = p_lo + q;
       if (p >= np) break;
       const PlaneConst pc = plane_const(ring, p);
       if (NK > 0 && p + 1 < np) preload(p + 1, xnxt);
@@ -652,11 +655,14 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
     xo[o] = op.base + scatter_bits(op.g, g) + scatter32(op.f_hi, f_hi) + scatter32(op.f_lo, f_lo);
   }
   const uint64_t oo = (uint64_t)g * a.n_out + scatter32(a.of_hi, f_hi) + scatter32(a.of_lo, f_lo);
+  const int np = kRing == TSG_RING_MODP ? ring.np : 1;
+  const int p_lo = a.plane_split ? (int)blockIdx.z : 0;
+  const int p_hi = a.plane_split ? p_lo + 1 : np;
   // at most one operand carries E bits (the other is the one E was chosen against)
   if (!a.op[0].has_e)
-    tile_thread<kRing, V, NE, NK>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo);
+    tile_thread<kRing, V, NE, NK>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo, p_lo, p_hi);
   else
-    tile_thread<kRing, V, NE, NK>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo);
+    tile_thread<kRing, V, NE, NK>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo, p_lo, p_hi);
 }
 
 // ------------------------------------------------------------------------------------

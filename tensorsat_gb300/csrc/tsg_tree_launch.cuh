@@ -11,7 +11,8 @@ namespace {
 
 template <int kRing, int V, int NE, int NK>
 void launch_tile_t(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st) {
-  dim3 grid((unsigned)la.shape.tiles, (unsigned)la.cnt);
+  dim3 grid((unsigned)la.shape.tiles, (unsigned)la.cnt,
+            la.t.plane_split ? (unsigned)ra.np : 1u);
   tree_step_tile_kernel<kRing, V, NE, NK><<<grid, la.shape.threads, 0, st>>>(la.t, ra);
 }
 

@@ -1,6 +1,6 @@
-"""The autotuner on the GPU: it times the executor's kernel choices against the tile-only
-configuration and a per-step mix, keeps the fastest per slice, caches the choice, and the
-tuned plan gives the exact answer."""
+"""The autotuner on the GPU: it times the executor's kernel choices against unfused,
+tile-only and fully fused configurations and a per-decision mix, keeps the fastest per
+slice, caches the choice, and the tuned plan gives the exact answer."""
 
 from __future__ import annotations
 
@@ -23,7 +23,8 @@ def test_tuned_plan_is_cached_and_exact(cuda, tmp_path):
     path = tmp_path / "plan.tune.json"
     try:
         entry = autotune.load_or_tune(path, c, d, ring, primes, budget_bytes=4 << 30)
-        assert {t["config"] for t in entry["trials"]} == {"executor", "tile", "mixed"}
+        assert {t["config"] for t in entry["trials"]} == {"executor", "no_fuse", "tile",
+                                                          "fuse", "plane_loop", "mixed"}
         assert entry["ms_per_slice"] <= entry["default_ms_per_slice"]
         assert len(entry["options"]) == c.native_plan().num_steps
         assert autotune.load_or_tune(path, c, d, ring, primes) == entry  # from the cache

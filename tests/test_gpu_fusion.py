@@ -1,7 +1,7 @@
 """Fused steps on the GPU: a step whose large result is read once, as its consumer's reused
-operand, is computed inside the consumer (tsg_set_fusion). Fused and unfused runs give
-identical results, and both equal the oracle's contraction of single slices along the same
-tree.
+operand, is computed inside the consumer (asked for with TSG_STEP_FUSE step options, in the
+tile and the streaming form). Fused and unfused runs give identical results, and both
+equal the oracle's contraction of single slices along the same tree.
 
 The leaves here are random {0,1} tensors on the wiring of CNF clause networks, so the
 per-slice counts are large and varied (a CNF network's counts are mostly zero), and every
@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from oracle import finrel_oracle as orc
-from tensorsat_gb300 import _native
+from tensorsat_gb300 import _native, autotune
 from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
 from tensorsat_gb300.diagrams import Diagram
 from tensorsat_gb300.lang.cuda_rel import CudaRel, leaf_array
@@ -31,6 +31,18 @@ def lib():
     lib = _native.lib()
     yield lib
     lib.tsg_set_fusion(1)
+
+
+RINGS = (_native.TSG_RING_MODP, _native.TSG_RING_U64, _native.TSG_RING_OR_AND)
+
+
+def _fuse(c, on):
+    """Asks for every fusion the structure allows (on) or clears the options (off)."""
+    for r in RINGS:
+        if on:
+            autotune.fuse_all(c, r)
+        else:
+            autotune.set_options(c, r, None)
 
 
 def _random_leaves(cnf, seed, density=0.99):
@@ -51,6 +63,7 @@ def test_fused_equals_unfused_and_the_oracle(cuda, lib, k, n, m, seed, target):
     primes = PRIMES_31[:3]
     ns = c.num_slices
     lib.tsg_set_fusion(1)
+    _fuse(c, True)
     for ring, pr in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_U64, ())):
         fused = npl.fused_steps(ring, pr, 4, c.tree)
         assert fused, "no fused step"
@@ -61,7 +74,7 @@ def test_fused_equals_unfused_and_the_oracle(cuda, lib, k, n, m, seed, target):
     probe = [0, ns // 2 + 1, ns - 1]
     results = {}
     for on in (1, 0):
-        lib.tsg_set_fusion(on)
+        _fuse(c, bool(on))
         results[on] = (
             c.count(d, ring="u64", group=4),
             c.count(d, ring="modp", num_primes=3, group=4),
@@ -87,6 +100,7 @@ def test_fused_cnf_counts_equal_dpll(cuda, lib):
         cnf = CNFInstance.random(k, n, m, rng=seed)
         d = cnf.clause_diagram()
         c = GpuContraction(CudaRel, d.wiring, target_bits=target, trials=2, seed=0)
+        _fuse(c, True)
         assert c.native_plan().fused_steps(_native.TSG_RING_MODP, PRIMES_31[:3], 16, c.tree)
         want = orc.dpll_count(n, cnf.clauses)[0]
         assert want > 0
@@ -103,12 +117,13 @@ def test_fused_or_and_bits_per_slice(cuda, lib):
     d = cnf.clause_diagram()
     c = GpuContraction(CudaRel, d.wiring, target_bits=22, trials=2, seed=0)
     lib.tsg_set_fusion(1)
+    _fuse(c, True)
     assert c.native_plan().fused_steps(_native.TSG_RING_OR_AND, (), 1, c.tree)
     ns = c.num_slices
     counts = [c.count(d, ring="u64", group=1, slice_range=(s, s + 1)) for s in range(ns)]
     assert 0 < sum(1 for x in counts if x) < ns
     bits = {}
     for on in (1, 0):
-        lib.tsg_set_fusion(on)
+        _fuse(c, bool(on))
         bits[on] = [bool(c.contract(d, group=1, slice_range=(s, s + 1))) for s in range(ns)]
     assert bits[1] == bits[0] == [x > 0 for x in counts]

@@ -239,10 +239,14 @@ def test_kernel_choice_matches_the_profiled_launches():
 
 
 def test_fusion_decisions_on_the_benchmark_tree():
-    """The n=60 benchmark tree fuses its expansion steps in every ring: each fused
-    producer is an operand of its consumer, launches nothing and needs no workspace;
-    switching fusion off restores the plain launches."""
+    """No step is fused unless its options ask for it. Asked for everywhere
+    (TSG_STEP_FUSE), the n=60 benchmark tree fuses its expansion steps in every ring: each
+    fused producer is an operand of its consumer, launches nothing and needs no
+    workspace, and the count rings' fused steps remove over 30% of their bytes; the
+    global switch off restores the plain launches."""
     import json
+
+    from tensorsat_gb300 import autotune
 
     plan = json.loads((HEADER.parent.parent / "plans" / "3sat_n60_m256_rng0_t26.json").read_text())
     cnf = CNFInstance.random(3, 60, 256, rng=0)
@@ -250,27 +254,33 @@ def test_fusion_decisions_on_the_benchmark_tree():
     npl = c.native_plan()
     lib = _native.lib()
     primes = PRIMES_31[:3]
+    rings = (_native.TSG_RING_MODP, _native.TSG_RING_U64, _native.TSG_RING_OR_AND)
     assert lib.tsg_fusion_enabled() == 1
-    fused = npl.fused_steps(_native.TSG_RING_MODP, primes, 64, c.tree)
-    assert fused and fused == npl.fused_steps(_native.TSG_RING_U64, (), 64, c.tree)
-    assert fused == npl.fused_steps(_native.TSG_RING_OR_AND, (), 64, c.tree)
-    L = c.tree.num_leaves
-    for s, p in fused.items():
-        assert L + p in c.tree.steps[s]
-    ws_on = npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64)
-    n_on = npl.launch_count(0, 64, 64, _native.TSG_RING_MODP, 3)
-    lib.tsg_set_fusion(0)
+    assert npl.fused_steps(_native.TSG_RING_MODP, primes, 64, c.tree) == {}
+    ws_plain = npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64)
+    n_plain = npl.launch_count(0, 64, 64, _native.TSG_RING_MODP, 3)
     try:
+        for r in rings:
+            autotune.fuse_all(c, r)
+        fused = npl.fused_steps(_native.TSG_RING_MODP, primes, 64, c.tree)
+        assert fused and fused == npl.fused_steps(_native.TSG_RING_U64, (), 64, c.tree)
+        assert set(npl.fused_steps(_native.TSG_RING_OR_AND, (), 64, c.tree)) <= set(fused)
+        L = c.tree.num_leaves
+        for s, p in fused.items():
+            assert L + p in c.tree.steps[s]
+        assert npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64) < ws_plain
+        assert npl.launch_count(0, 64, 64, _native.TSG_RING_MODP, 3) == n_plain - len(fused)
+        sp = c.sliced_plan
+        saved = sp.bytes_per_slice(4, 3) - sp.bytes_per_slice(4, 3, fused)
+        assert saved > 0.3 * sp.bytes_per_slice(4, 3)
+        lib.tsg_set_fusion(0)
         assert npl.fused_steps(_native.TSG_RING_MODP, primes, 64, c.tree) == {}
-        ws_off = npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64)
-        n_off = npl.launch_count(0, 64, 64, _native.TSG_RING_MODP, 3)
+        assert npl.workspace_bytes(_native.TSG_RING_MODP, 3, 64) == ws_plain
     finally:
         lib.tsg_set_fusion(1)
-    assert ws_on < ws_off and n_on == n_off - len(fused)
-    assert n_off == npl.launch_count(0, 64, 64)
-    sp = c.sliced_plan
-    saved = sp.bytes_per_slice(4, 3) - sp.bytes_per_slice(4, 3, fused)
-    assert saved > 0.3 * sp.bytes_per_slice(4, 3)
+        for r in rings:
+            autotune.set_options(c, r, None)
+    assert n_plain == npl.launch_count(0, 64, 64)
 
 
 def test_subset_dp_rejects_bad_sizes_and_nulls():
@@ -331,23 +341,25 @@ def test_step_options_change_kernel_choices_not_plans():
     base = npl.describe(ring, primes, 64)
     ws = npl.workspace_bytes(ring, 3, 64)
     streamed = [s for s in range(npl.num_steps) if base[s][0] == _native.TSG_KERNEL_STREAM]
-    fused = npl.fused_steps(ring, primes, 64, c.tree)
-    assert streamed and fused
-    opts = [0] * npl.num_steps
-    opts[streamed[0]] = _native.TSG_STEP_NO_STREAM
-    p = next(iter(fused.values()))
-    opts[p] = _native.TSG_STEP_NO_FUSE
+    assert streamed and npl.fused_steps(ring, primes, 64, c.tree) == {}
     try:
+        autotune.fuse_all(c, ring)
+        fused = npl.fused_steps(ring, primes, 64, c.tree)
+        assert fused and npl.workspace_bytes(ring, 3, 64) < ws
+        p = next(iter(fused.values()))
+        opts = [_native.TSG_STEP_FUSE] * npl.num_steps
+        opts[p] = _native.TSG_STEP_NO_FUSE
+        unfused_stream = [s for s in streamed if s not in fused]
+        opts[unfused_stream[0]] |= _native.TSG_STEP_NO_STREAM
         autotune.set_options(c, ring, opts)
         got = npl.describe(ring, primes, 64)
-        assert got[streamed[0]][0] == _native.TSG_KERNEL_TILE
+        assert got[unfused_stream[0]][0] == _native.TSG_KERNEL_TILE
         assert got[p][0] != _native.TSG_KERNEL_NONE
-        assert npl.workspace_bytes(ring, 3, 64) > ws
-        # other rings keep their own (empty) options
-        assert (npl.describe(_native.TSG_RING_U64, (), 64)[p][0]) == _native.TSG_KERNEL_NONE
+        # other rings keep their own (empty) options: nothing fused there
+        assert npl.fused_steps(_native.TSG_RING_U64, (), 64, c.tree) == {}
         npl.validate(ring, primes, 0, 128, 64)
         bad = list(opts)
-        bad[0] = 8
+        bad[0] = 16
         with pytest.raises(_native.TsgValueError):
             autotune.set_options(c, ring, bad)
     finally:
