@@ -246,6 +246,26 @@ TSG_API tsg_status tsg_batch_run_lanes(int32_t num_instances, const tsg_plan* co
                                int32_t lanes, void* workspace_dev, int64_t workspace_bytes,
                                void* const* results_dev, void* stream);
 
+/* Leaf variants of one plan in one run: num_variants (a power of two) copies of the leaf
+ * pool lie pool_stride bytes apart (a power of two, at least the plan's pool extent and
+ * 16); every tree step is launched once per slice group for all variants together (the
+ * variant index is an extra batch axis of the launch, beside the slices), and variant v's
+ * result goes to results_dev + v * (result size of tsg_plan_run). All slices are
+ * contracted, group_size per launch group and variant; the workspace must hold
+ * tsg_plan_variants_workspace_bytes. This is the reference's assignment-search idiom (one
+ * wiring, many unit-input diagrams: notebooks/02-random-ksat.ipynb cells 35-36,
+ * tensorsat/contractions/abc.py:91-97) with one launch sequence instead of one
+ * contraction per variant. */
+TSG_API tsg_status tsg_plan_variants_workspace_bytes(const tsg_plan* plan, int32_t ring,
+                                             int32_t num_primes, int64_t group_size,
+                                             int64_t num_variants, int64_t* bytes_out);
+TSG_API tsg_status tsg_plan_run_variants(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                                 const uint32_t* primes, const uint8_t* leaf_pools_dev,
+                                 int64_t pool_stride, int64_t num_variants,
+                                 int64_t group_size, void* workspace_dev,
+                                 int64_t workspace_bytes, void* results_dev,
+                                 int32_t accumulate, void* stream);
+
 /* tsg_plan_run that also measures: a CUDA event is recorded on `stream` before the first
  * launch and after every launch, and on return (the call waits for the run to finish)
  * step_ms[s] holds the device time of tree step s summed over the slice groups of the

@@ -731,6 +731,111 @@ class GpuContraction(Contraction):
             raise ValueError(f"unknown count ring {ring!r}")
         return self._counts_from_root(counts)
 
+    # -- leaf variants of one wiring ----------------------------------------------------
+
+    def run_variants(self, diagrams: Sequence[Diagram], ring: int, primes: Sequence[int] = (),
+                     group: int | None = None) -> list[np.ndarray]:
+        """Contracts many diagrams of this wiring (leaf variants: the assignment-search
+        idiom) in one launch sequence (``tsg_plan_run_variants``): every step runs once
+        per slice group for all variants, the variant index being an extra batch axis.
+        Returns each variant's root entries on the host, laid out as :meth:`run`'s."""
+        if not diagrams:
+            raise ValueError("run_variants needs at least one diagram")
+        for d in diagrams:
+            self.validate(d)
+        dev = _device.require_cuda()
+        npl = self.native_plan()
+        n = len(diagrams)
+        nv = 1 << (n - 1).bit_length()
+        stride = 1 << max(4, (npl.pool_bytes - 1).bit_length())
+        parts = [self._host_pool(d) for d in diagrams]
+        host = np.zeros(nv * stride, dtype=np.uint8)
+        for v in range(nv):  # padding variants repeat the first diagram
+            h, _ = parts[v] if v < n else parts[0]
+            host[v * stride: v * stride + h.size] = h
+        pool = torch.from_numpy(host).to(dev)
+        for v in range(nv):
+            dl = parts[v][1] if v < n else parts[0][1]
+            if dl:
+                self._finish_pool(pool[v * stride: v * stride + npl.pool_bytes], dl)
+        planes = len(primes) if ring == _native.TSG_RING_MODP else 1
+        if group is None:
+            group = self._variant_group(ring, planes, nv)
+        lib = _native.lib()
+        need = _native.c_int64()
+        _native.check(lib.tsg_plan_variants_workspace_bytes(npl.handle, ring, planes, group, nv,
+                                                            _native.ctypes.byref(need)))
+        ws = torch.empty(max(need.value, 256), dtype=torch.uint8, device=dev)
+        entries = 1 << len(self._leaves.out_unique)
+        esize = {_native.TSG_RING_OR_AND: 1, _native.TSG_RING_U64: 8}.get(ring, 4)
+        per = entries * esize * planes
+        res = torch.zeros(nv * per, dtype=torch.uint8, device=dev)
+        parr = (_native.c_uint32 * max(1, len(primes)))(*primes)
+        _native.check(lib.tsg_plan_run_variants(
+            npl.handle, ring, len(primes), parr, pool.data_ptr(), stride, nv, group,
+            ws.data_ptr(), ws.numel(), res.data_ptr(), 0, _device.stream_handle()))
+        self.check_device()
+        flat = res.cpu().numpy()
+        dt = {_native.TSG_RING_OR_AND: np.uint8, _native.TSG_RING_U64: np.uint64}.get(ring, np.uint32)
+        out = []
+        for v in range(n):
+            a = flat[v * per: (v + 1) * per].view(dt)
+            out.append(a.reshape(planes, -1) if ring == _native.TSG_RING_MODP else a)
+        return out
+
+    def _variant_group(self, ring: int, planes: int, variants: int) -> int:
+        """Largest power-of-two slice group whose variant workspace fits 40% of free device
+        memory."""
+        npl = self.native_plan()
+        if npl.num_sliced == 0:
+            return 1
+        free, _ = torch.cuda.mem_get_info()
+        budget = int(free * 0.4)
+        lib = _native.lib()
+        g = self.num_slices
+        need = _native.c_int64()
+        while g > 1:
+            _native.check(lib.tsg_plan_variants_workspace_bytes(
+                npl.handle, ring, planes, g, variants, _native.ctypes.byref(need)))
+            if need.value <= budget:
+                break
+            g //= 2
+        return g
+
+    def contract_variants(self, diagrams: Sequence[Diagram], *,
+                          group: int | None = None) -> list[CudaRel]:
+        """OR-AND contraction of many diagrams of this wiring in one launch sequence
+        (:meth:`run_variants`): one result box per diagram (``bool(box)`` is its SAT bit
+        for a closed network)."""
+        roots = self.run_variants(diagrams, _native.TSG_RING_OR_AND, group=group)
+        return [self._box_from_root(torch.from_numpy(r.copy())) for r in roots]
+
+    def count_variants(self, diagrams: Sequence[Diagram], *, num_primes: int | None = None,
+                       group: int | None = None) -> list[Any]:
+        """Exact model counts of many diagrams of this wiring in one launch sequence, modulo
+        31-bit primes with CRT (enough primes for the largest count bound, at most 4)."""
+        bounds = []
+        for d in diagrams:
+            arrays = []
+            for blk in d.blocks:
+                try:
+                    arrays.append(leaf_array(blk))
+                except TypeError:
+                    arrays.append(np.zeros((), dtype=np.uint8))
+            bounds.append(count_bound_bits(self._wiring, arrays))
+        need = 1
+        while sum(math.log2(p) for p in PRIMES_31[:need]) <= max(bounds):
+            need += 1
+        if num_primes is None:
+            num_primes = need
+        if num_primes < need or num_primes > _native.TSG_MAX_PRIMES:
+            raise OverflowError(f"the variants' count bounds need {need} primes (at most "
+                                f"{_native.TSG_MAX_PRIMES} per run)")
+        primes = PRIMES_31[:num_primes]
+        roots = self.run_variants(diagrams, _native.TSG_RING_MODP, primes, group=group)
+        return [self._counts_from_root(crt([r[p] for p in range(num_primes)], primes))
+                for r in roots]
+
     # -- plans and checkpoints --------------------------------------------------------
 
     def plan_dict(self) -> dict:

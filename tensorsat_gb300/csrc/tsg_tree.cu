@@ -83,6 +83,7 @@ struct Layout {
   int64_t elem_bytes;
   int planes;
   bool fusion;                  // fused steps enabled when the layout was made
+  bool all_dep;                 // every step per slot (leaf variants: no shared prologue)
   std::vector<int64_t> offset;  // byte offset of each step's output in the workspace
                                 // (-1: computed inside its consumer, never stored)
   std::vector<int64_t> plane;   // plane stride (elements) of each step's output
@@ -284,11 +285,11 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
 }
 
 tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int planes,
-                      const Layout** out) {
+                      const Layout** out, bool all_dep = false) {
   const bool fusion = g_fusion.load(std::memory_order_relaxed) != 0;
   for (const Layout& l : plan->layouts) {
     if (l.group == group && l.elem_bytes == elem_bytes && l.planes == planes &&
-        l.fusion == fusion) {
+        l.fusion == fusion && l.all_dep == all_dep) {
       *out = &l;
       return TSG_OK;
     }
@@ -300,6 +301,8 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
   lay.elem_bytes = elem_bytes;
   lay.planes = planes;
   lay.fusion = fusion;
+  lay.all_dep = all_dep;
+  auto dep = [&](int x) { return all_dep || steps[x].dep; };
   lay.offset.assign(ns, -1);
   lay.plane.assign(ns, 0);
   lay.fused_from = fusion ? choose_fusion(plan, group, elem_bytes) : std::vector<int>(ns, -1);
@@ -308,7 +311,7 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
     if (lay.fused_from[s] >= 0) lay.fused_away[lay.fused_from[s]] = 1;
   std::vector<int64_t> bytes(ns, 0);
   for (int s = 0; s < ns; ++s) {
-    const int64_t slices = steps[s].dep ? group : 1;
+    const int64_t slices = dep(s) ? group : 1;
     if (steps[s].out_bits + 64 - __builtin_clzll((unsigned long long)slices) > 62)
       return fail(TSG_ERR_TOO_LARGE, "plan_run: group * tensor size exceeds 2^62 entries");
     const int64_t elems = slices << steps[s].out_bits;
@@ -327,13 +330,13 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
       const int x = -v - 1;
       if (lay.fused_away[x]) continue;
       // an independent result read by a dependent step is re-read by every group
-      if (!steps[x].dep && steps[s].dep) continue;
+      if (!dep(x) && dep(s)) continue;
       arena.release(lay.offset[x], bytes[x]);
     }
   };
   for (int phase = 0; phase < 2; ++phase) {
     for (int s = 0; s < ns; ++s) {
-      if (steps[s].dep != (phase == 1) || lay.fused_away[s]) continue;
+      if (dep(s) != (phase == 1) || lay.fused_away[s]) continue;
       lay.offset[s] = arena.alloc(bytes[s]);
       arena.note();
       release_operands(s, s);
@@ -375,7 +378,15 @@ struct RunCtx {
   const uint8_t* pool;
   uint8_t* ws;
   cudaStream_t stream;
-  int g_bits;  // log2(group)
+  int g_bits;  // log2(slices per launch group)
+  // leaf variants (tsg_plan_run_variants): the launch's slots are variant * 2^g_bits +
+  // slice; every step runs per slot, and variant v's leaves sit v * 2^vstride_bits bytes
+  // further into the pool
+  bool all_dep = false;
+  int v_bits = 0;
+  int vstride_bits = 0;
+  uint64_t leaf_extra = 0;  // ((2^v_bits - 1) << vstride_bits): extra extent of every leaf
+  bool dep(const StepInfo& st) const { return all_dep || st.dep; }
 };
 
 template <int kRing, bool kL, bool kR>
@@ -451,7 +462,7 @@ tsg_status check_step_bounds(const RunCtx& c, int s, const StepArgs& a, const bo
     if (is_leaf[o]) {
       const LeafInfo& lf = plan->leaves[v];
       lo_ext = (uint64_t)lf.offset;
-      hi_ext = lo_ext + (1ull << lf.rank);
+      hi_ext = lo_ext + (1ull << lf.rank) + c.leaf_extra;
     } else {
       lo_ext = 0;
       hi_ext = (uint64_t)c.lay->plane[-v - 1];
@@ -474,7 +485,7 @@ struct OperandDesc {
 
 OperandDesc describe_operand(const RunCtx& c, const StepInfo& st, int o, int64_t base) {
   const tsg_plan* plan = c.plan;
-  const int gb = st.dep ? c.g_bits : 0;
+  const int gb = c.dep(st) ? c.g_bits : 0;
   OperandDesc d;
   const int v = st.op[o];
   for (int i = 0; i < st.out_bits; ++i)
@@ -486,21 +497,23 @@ OperandDesc describe_operand(const RunCtx& c, const StepInfo& st, int o, int64_t
     d.ptr = c.pool;
     d.base = (uint64_t)lf.offset;
     for (int j = 0; j < plan->num_sliced; ++j) {
-      if (lf.spos[j] < 0 || !st.dep) continue;
+      if (lf.spos[j] < 0 || !c.dep(st)) continue;
       if (j < gb) {
         d.gp.push_back({j, lf.spos[j]});
       } else {
         d.base += (uint64_t)((base >> j) & 1) << lf.spos[j];
       }
     }
+    // variant bits of the slot select the variant's copy of the pool
+    for (int i = 0; i < c.v_bits; ++i) d.gp.push_back({gb + i, c.vstride_bits + i});
     d.leaf = true;
   } else {
     const int x = -v - 1;
     const StepInfo& xs = plan->steps[x];
     d.ptr = (c.ws && c.lay->offset[x] >= 0) ? c.ws + c.lay->offset[x] : nullptr;
     d.plane = (uint64_t)c.lay->plane[x];
-    if (xs.dep)
-      for (int j = 0; j < gb; ++j) d.gp.push_back({j, xs.out_bits + j});
+    if (c.dep(xs))
+      for (int j = 0; j < gb + c.v_bits; ++j) d.gp.push_back({j, xs.out_bits + j});
   }
   return d;
 }
@@ -764,7 +777,7 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
                         narrow_max(op.f_lo, t.tile_bits, vbits) + tab + eo + ko;
     const int v = st.op[o];
     const uint64_t lo_ext = la.is_leaf[o] ? (uint64_t)plan->leaves[v].offset : 0;
-    const uint64_t hi_ext = la.is_leaf[o] ? lo_ext + (1ull << plan->leaves[v].rank)
+    const uint64_t hi_ext = la.is_leaf[o] ? lo_ext + (1ull << plan->leaves[v].rank) + c.leaf_extra
                                           : (uint64_t)c.lay->plane[-v - 1];
     if (op.base < lo_ext || hi >= hi_ext)
       return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: operand offset outside its tensor");
@@ -1030,7 +1043,7 @@ tsg_status build_fused(const RunCtx& c, int s, int64_t base, const TileBits& tb,
     }
     const int v = ps.op[o];
     const uint64_t lo_ext = dp.leaf ? (uint64_t)plan->leaves[v].offset : 0;
-    const uint64_t hi_ext = dp.leaf ? lo_ext + (1ull << plan->leaves[v].rank)
+    const uint64_t hi_ext = dp.leaf ? lo_ext + (1ull << plan->leaves[v].rank) + c.leaf_extra
                                     : (uint64_t)c.lay->plane[-v - 1];
     TSG_TRY(check_operand_tile(f.op[o], la->t, sh, la->cnt, extra_max, extra, lo_ext, hi_ext));
   }
@@ -1048,7 +1061,7 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   std::memset(&a, 0, sizeof(a));
   std::memset(&la->f, 0, sizeof(la->f));
   la->nkp = 0;
-  la->cnt = (uint64_t)(st.dep ? cnt : 1);
+  la->cnt = (uint64_t)(c.dep(st) ? cnt : 1);
   a.total = la->cnt << st.out_bits;
   a.k_bits = st.k_bits;
   a.out = c.ws ? c.ws + c.lay->offset[s] : nullptr;
@@ -1157,11 +1170,13 @@ tsg_status launch_step(const RunCtx& c, int s, int64_t base, int64_t cnt) {
   return TSG_OK;
 }
 
-tsg_status launch_reduce(const RunCtx& c, int64_t cnt, uint8_t* result, int accumulate) {
+tsg_status launch_reduce(const RunCtx& c, int64_t cnt, uint8_t* result, int accumulate,
+                         int64_t slot0 = 0) {
   const tsg_plan* plan = c.plan;
   const int root = (int)plan->steps.size() - 1;
   const uint64_t entries = 1ull << plan->root_bits;
-  const uint8_t* rp = c.ws + c.lay->offset[root];
+  // slots [slot0, slot0 + cnt) of the root (a variant's slices in a variant run)
+  const uint8_t* rp = c.ws + c.lay->offset[root] + (uint64_t)slot0 * entries * c.lay->elem_bytes;
   const uint64_t plane = (uint64_t)c.lay->plane[root];
   unsigned blocks = (unsigned)std::min<uint64_t>(entries, (uint64_t)device_sm_count() * 8);
   switch (c.ring) {
@@ -1268,12 +1283,20 @@ void describe_launch(const LaunchArgs& la, int ring, int32_t* out) {
 // every launch's arguments are built and bounds-checked only (and, with `kinds`, each
 // step's kernel of the first slice group is recorded). With a timer, every launch is
 // followed by an event record.
+// Leaf variants of one plan contracted together (tsg_plan_run_variants): `count` (a power
+// of two) copies of the leaf pool, 2^stride_bits bytes apart; results `result_bytes` apart.
+struct VariantSpec {
+  int64_t count;
+  int stride_bits;
+  int64_t result_bytes;
+};
+
 tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
                     const uint32_t* primes, const uint8_t* pool, int64_t slice_begin,
                     int64_t slice_end, int64_t group_size, void* workspace,
                     int64_t workspace_bytes, void* result_dev, int32_t accumulate,
                     cudaStream_t stream, bool dry, RunTimer* timer = nullptr,
-                    int32_t* kinds = nullptr) {
+                    int32_t* kinds = nullptr, const VariantSpec* vs = nullptr) {
   TSG_TRY(check_range(plan, slice_begin, slice_end, group_size));
   int64_t eb;
   int planes;
@@ -1295,8 +1318,15 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
       ra.r1[p] = (uint32_t)((1ull << 32) % primes[p]);
     }
   }
+  int v_bits = 0;
+  if (vs) {
+    while ((int64_t(1) << v_bits) < vs->count) v_bits++;
+    if (int64_t(1) << v_bits != vs->count)
+      return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run_variants: the variant count must be a power of two");
+  }
   const Layout* lay;
-  TSG_TRY(get_layout(const_cast<tsg_plan*>(plan), group_size, eb, planes, &lay));
+  TSG_TRY(get_layout(const_cast<tsg_plan*>(plan), group_size << v_bits, eb, planes, &lay,
+                     vs != nullptr));
   if (!dry) {
     if (!workspace || workspace_bytes < lay->bytes)
       return fail(TSG_ERR_WORKSPACE, "plan_run: workspace smaller than tsg_plan_workspace_bytes");
@@ -1313,6 +1343,12 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
   c.stream = stream;
   c.g_bits = 0;
   while ((int64_t(1) << c.g_bits) < group_size) c.g_bits++;
+  if (vs) {
+    c.all_dep = true;
+    c.v_bits = v_bits;
+    c.vstride_bits = vs->stride_bits;
+    c.leaf_extra = ((uint64_t(1) << v_bits) - 1) << vs->stride_bits;
+  }
   const int ns = (int)plan->steps.size();
   if (timer && !dry) TSG_TRY(timer->record(stream, -1));
   auto timed = [&](int id) -> tsg_status {
@@ -1329,7 +1365,7 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
     if (dry) {
       LaunchArgs la;
       TSG_TRY(build_step(c, s, base, cnt, &la));
-      if (kinds && (!plan->steps[s].dep || base == slice_begin))
+      if (kinds && (!c.dep(plan->steps[s]) || base == slice_begin))
         describe_launch(la, ring, kinds + 4 * s);
       return TSG_OK;
     }
@@ -1341,9 +1377,27 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
     TSG_TRY(launch_reduce(c, cnt, result, acc));
     return timed(ns);
   };
+  uint8_t* result = (uint8_t*)result_dev;
+  if (vs) {
+    // every step per slot (variant-major slots), then each variant's slices reduced into
+    // its own result
+    bool first = true;
+    for (int64_t base = slice_begin; base < slice_end; base += group_size) {
+      const int64_t cnt = std::min<int64_t>(group_size, slice_end - base);
+      for (int s = 0; s < ns; ++s) TSG_TRY(step(s, base, group_size << v_bits));
+      if (!dry) {
+        for (int64_t v = 0; v < vs->count; ++v) {
+          TSG_TRY(launch_reduce(c, cnt, result + v * vs->result_bytes,
+                                first ? accumulate : 1, v * group_size));
+          TSG_TRY(timed(ns));
+        }
+      }
+      first = false;
+    }
+    return TSG_OK;
+  }
   for (int s = 0; s < ns; ++s)
     if (!plan->steps[s].dep) TSG_TRY(step(s, 0, 1));
-  uint8_t* result = (uint8_t*)result_dev;
   if (!plan->steps.back().dep) return reduce(1, result, accumulate);
   bool first = true;
   for (int64_t base = slice_begin; base < slice_end; base += group_size) {
@@ -1659,6 +1713,57 @@ tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring, const int32_t
                                      [&](const Layout& l) { return l.elem_bytes == eb; }),
                       plan->layouts.end());
   return TSG_OK;
+}
+
+tsg_status tsg_plan_variants_workspace_bytes(const tsg_plan* plan, int32_t ring,
+                                             int32_t num_primes, int64_t group_size,
+                                             int64_t num_variants, int64_t* bytes_out) {
+  if (!plan || !bytes_out)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "variants_workspace_bytes: null pointer");
+  if (!is_pow2(group_size) || !is_pow2(num_variants))
+    return fail(TSG_ERR_INVALID_ARGUMENT,
+                "variants_workspace_bytes: group and variant count must be powers of two");
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  const Layout* lay;
+  TSG_TRY(get_layout(const_cast<tsg_plan*>(plan), group_size * num_variants, eb, planes, &lay,
+                     /*all_dep=*/true));
+  *bytes_out = lay->bytes;
+  return TSG_OK;
+}
+
+tsg_status tsg_plan_run_variants(const tsg_plan* plan, int32_t ring, int32_t num_primes,
+                                 const uint32_t* primes, const uint8_t* leaf_pools_dev,
+                                 int64_t pool_stride, int64_t num_variants, int64_t group_size,
+                                 void* workspace_dev, int64_t workspace_bytes,
+                                 void* results_dev, int32_t accumulate, void* stream) {
+  if (!plan || !leaf_pools_dev || !results_dev)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run_variants: null pointer");
+  if (!is_pow2(num_variants) || !is_pow2(pool_stride) || pool_stride < 16)
+    return fail(TSG_ERR_INVALID_ARGUMENT,
+                "plan_run_variants: variant count and pool stride must be powers of two "
+                "(stride >= 16 bytes)");
+  int64_t pool_end = 0;
+  for (const LeafInfo& lf : plan->leaves)
+    pool_end = std::max<int64_t>(pool_end, lf.offset + (int64_t(1) << lf.rank));
+  if (pool_stride < pool_end)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run_variants: pool stride smaller than one pool");
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  VariantSpec vs;
+  vs.count = num_variants;
+  vs.stride_bits = 0;
+  while ((int64_t(1) << vs.stride_bits) < pool_stride) vs.stride_bits++;
+  vs.result_bytes = (int64_t(1) << plan->root_bits) * eb * planes;
+  const int64_t ns = int64_t(1) << plan->num_sliced;
+  // every launch is built and bounds-checked on the host before the first one is issued
+  TSG_TRY(run_impl(plan, ring, num_primes, primes, nullptr, 0, ns, group_size, nullptr, 0,
+                   nullptr, 0, nullptr, /*dry=*/true, nullptr, nullptr, &vs));
+  return run_impl(plan, ring, num_primes, primes, leaf_pools_dev, 0, ns, group_size,
+                  workspace_dev, workspace_bytes, results_dev, accumulate,
+                  (cudaStream_t)stream, /*dry=*/false, nullptr, nullptr, &vs);
 }
 
 tsg_status tsg_set_fusion(int32_t enabled) {

@@ -397,3 +397,27 @@ def test_tuning_cache_round_trip(tmp_path):
     (tmp_path / "bad.json").write_text('{"format": "x"}')
     with pytest.raises(ValueError):
         autotune.load(tmp_path / "bad.json", c, ring, primes, gpu="GB300 test")
+
+
+def test_variant_runs_size_their_workspace_per_slot():
+    """A variant run lays out every step per slot (variant x slice): its workspace grows
+    with the variants and is at least that of a plain run of the same slices; counts and
+    strides that are not powers of two are rejected before any device work."""
+    c = _plan_for(CNFInstance.random(3, 20, 85, rng=2), 8)
+    npl = c.native_plan()
+    lib = _native.lib()
+    out = ctypes.c_int64()
+    ring = _native.TSG_RING_MODP
+    sizes = []
+    for nv in (1, 2, 8):
+        _native.check(lib.tsg_plan_variants_workspace_bytes(npl.handle, ring, 3, 2, nv,
+                                                            ctypes.byref(out)))
+        sizes.append(out.value)
+    assert sizes[0] >= npl.workspace_bytes(ring, 3, 2)
+    assert sizes[0] < sizes[1] < sizes[2]
+    assert lib.tsg_plan_variants_workspace_bytes(npl.handle, ring, 3, 2, 3,
+                                                 ctypes.byref(out)) == _native.TSG_ERR_INVALID_ARGUMENT
+    p = (ctypes.c_uint32 * 3)(*PRIMES_31[:3])
+    for nv, stride in ((3, 1 << 12), (2, 1000), (2, 8)):
+        assert lib.tsg_plan_run_variants(npl.handle, ring, 3, p, 16, stride, nv, 2, 256, 1 << 20,
+                                         16, 0, None) == _native.TSG_ERR_INVALID_ARGUMENT
