@@ -176,7 +176,7 @@ TSG_API int32_t tsg_fusion_enabled(void);
  * a bit set of TSG_STEP_NO_STREAM (run step s on the tile kernel even where the streaming
  * kernel applies), TSG_STEP_NO_FUSE (never compute step s inside its consumer) and
  * TSG_STEP_FUSE (compute step s inside its consumer where the structure allows it; no
- * step is fused without it) and TSG_STEP_PLANE_LOOP, for every step (num_steps entries);
+ * step is fused without it) and TSG_STEP_PLANE_SPLIT, for every step (num_steps entries);
  * options == NULL clears
  * them. Later runs, workspace sizes and descriptions of that ring follow them; results do
  * not depend on them. Host only.
@@ -185,8 +185,8 @@ TSG_API int32_t tsg_fusion_enabled(void);
 #define TSG_STEP_NO_STREAM 1
 #define TSG_STEP_NO_FUSE 2
 #define TSG_STEP_FUSE 4
-#define TSG_STEP_PLANE_LOOP 8 /* MODP tile kernel: every residue plane in one thread (default:
-                                 one plane per block) */
+#define TSG_STEP_PLANE_SPLIT 8 /* MODP tile kernel: one residue plane per block (default:
+                                  every plane in one thread) */
 TSG_API tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring,
                                      const int32_t* options);
 

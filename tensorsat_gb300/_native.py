@@ -38,7 +38,7 @@ TSG_KERNEL_SUM = 5
 TSG_STEP_NO_STREAM = 1
 TSG_STEP_NO_FUSE = 2
 TSG_STEP_FUSE = 4
-TSG_STEP_PLANE_LOOP = 8
+TSG_STEP_PLANE_SPLIT = 8
 
 EXPORTED_SYMBOLS = (
     "tsg_last_error",

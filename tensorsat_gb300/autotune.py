@@ -10,7 +10,7 @@ the tuner only looks for speed:
    halvings of it), it times one slice group of the plan with ``tsg_plan_run_timed`` (a
    CUDA event after every launch) in four configurations: the executor's own choices; no
    fused step; tile kernels only; every possible fusion (and, for residue counts, every
-   tile step with its residue planes in one thread instead of one plane per block).
+   tile step with one residue plane per block instead of all planes in one thread).
 2. Per decision it keeps the faster alternative: a fusion when the fused consumer took
    less than the producer plus its consumer unfused; a streamed step when it beat the
    tile kernel; a tile step's plane split when it beat the in-thread plane loop.
@@ -118,11 +118,11 @@ def tune(contraction: Any, diagram: Any, ring: int, primes: Sequence[int] = (),
     n = npl.num_steps
     L = contraction.tree.num_leaves
     NS, NF, FU = _native.TSG_STEP_NO_STREAM, _native.TSG_STEP_NO_FUSE, _native.TSG_STEP_FUSE
-    PL = _native.TSG_STEP_PLANE_LOOP
+    PS = _native.TSG_STEP_PLANE_SPLIT
     configs = {"executor": [0] * n, "no_fuse": [NF] * n, "tile": [NS | NF] * n,
                "fuse": [FU] * n}
     if ring == _native.TSG_RING_MODP and len(primes) > 1:
-        configs["plane_loop"] = [NF | PL] * n
+        configs["plane_split"] = [NF | PS] * n
     trials = []
     for g in groups:
         ms, kinds = {}, {}
@@ -147,12 +147,12 @@ def tune(contraction: Any, diagram: Any, ring: int, primes: Sequence[int] = (),
             if kinds["no_fuse"][s][0] == _native.TSG_KERNEL_STREAM and \
                     ms["tile"][s] < ms["no_fuse"][s]:
                 mixed[s] |= NS
-        # MODP tile steps: residue planes per block or all in one thread
-        if "plane_loop" in configs:
+        # MODP tile steps: all residue planes in one thread, or one plane per block
+        if "plane_split" in configs:
             for s in range(n):
                 if kinds["no_fuse"][s][0] == _native.TSG_KERNEL_TILE and \
-                        ms["plane_loop"][s] < ms["no_fuse"][s] and not mixed[s] & NS:
-                    mixed[s] |= PL
+                        ms["plane_split"][s] < ms["no_fuse"][s] and not mixed[s] & NS:
+                    mixed[s] |= PS
         ms["mixed"], _ = _timed(contraction, ring, primes, pool, 0, g, mixed, passes)
         slices = min(ns, g)
         for name, opts in list(configs.items()) + [("mixed", mixed)]:

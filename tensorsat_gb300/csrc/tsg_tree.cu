@@ -1087,10 +1087,10 @@ tsg_status build_step(const RunCtx& c, int s, int64_t base, int64_t cnt, LaunchA
   la->streamed = false;
   la->fused = false;
   if (ok) TSG_TRY(check_tile_bounds(c, s, *la));
-  // MODP tile launches: one residue plane per block (more warps in flight) unless asked to
-  // keep the planes in one thread
+  // MODP tile launches: every residue plane in one thread (the E-free operand of the next
+  // plane prefetched) unless the step's options ask for one plane per block
   la->t.plane_split = (ok && c.ring == TSG_RING_MODP && c.ra.np > 1 &&
-                       !(step_option(plan, c.lay->elem_bytes, s) & TSG_STEP_PLANE_LOOP)) ? 1 : 0;
+                       (step_option(plan, c.lay->elem_bytes, s) & TSG_STEP_PLANE_SPLIT)) ? 1 : 0;
   if (c.lay->fused_from[s] >= 0) {
     if (!ok)
       return fail(TSG_ERR_UNSUPPORTED, "plan_run: fused step outside the tile kernel");
@@ -1701,7 +1701,7 @@ tsg_status tsg_plan_set_step_options(tsg_plan* plan, int32_t ring, const int32_t
   if (options) {
     for (size_t i = 0; i < ns; ++i)
       if (options[i] & ~(TSG_STEP_NO_STREAM | TSG_STEP_NO_FUSE | TSG_STEP_FUSE |
-                         TSG_STEP_PLANE_LOOP))
+                         TSG_STEP_PLANE_SPLIT))
         return fail(TSG_ERR_INVALID_ARGUMENT, "set_step_options: unknown option bit");
     plan->options[ring].assign(options, options + ns);
   } else {

@@ -24,7 +24,7 @@ def test_tuned_plan_is_cached_and_exact(cuda, tmp_path):
     try:
         entry = autotune.load_or_tune(path, c, d, ring, primes, budget_bytes=4 << 30)
         assert {t["config"] for t in entry["trials"]} == {"executor", "no_fuse", "tile",
-                                                          "fuse", "plane_loop", "mixed"}
+                                                          "fuse", "plane_split", "mixed"}
         assert entry["ms_per_slice"] <= entry["default_ms_per_slice"]
         assert len(entry["options"]) == c.native_plan().num_steps
         assert autotune.load_or_tune(path, c, d, ring, primes) == entry  # from the cache
