@@ -517,7 +517,7 @@ def run_gb300(args) -> None:
             "metric": RAGGED_METRIC, "value": r["value"], "unit": UNIT,
             "workload": ragged_workload_text(len(instances), lo, hi),
             "form": f"captured CUDA graphs ({r['graphs']}: one per {RAGGED_CHUNK}-instance "
-                    f"chunk and ring) replayed, inputs resident",
+                    f"chunk and ring, {RAGGED_LANES} concurrent lanes) replayed, inputs resident",
             "steps": args.batched_steps, "ms_per_step": statistics.mean(r["step_ms"]),
             "plain": {"value": r["plain_value"], "unit": UNIT, "instances": len(instances),
                       "form": "GpuContraction.count + contract per instance, host leaves "
@@ -583,7 +583,8 @@ def run_gb300(args) -> None:
 
 
 RAGGED_METRIC = "exact instances/s (SAT bit + model count), ragged batch of random 3-SAT"
-RAGGED_CHUNK = 64  # instances per captured graph
+RAGGED_CHUNK = 512  # instances per captured graph (the whole default batch: one per ring)
+RAGGED_LANES = 32  # concurrent lanes of a batch
 
 
 def ragged_instances(count: int, n_lo: int, n_hi: int):
@@ -679,11 +680,11 @@ def ragged_measure(instances, trees, expected, steps: int, warmup: int, e2e_step
     diagrams = [cnf.clause_diagram() for cnf in instances]
     primes = PRIMES_31[:NUM_PRIMES]
     chunks = [BatchContraction(CudaRel, diagrams[i: i + RAGGED_CHUNK],
-                               trees=trees[i: i + RAGGED_CHUNK])
+                               trees=trees[i: i + RAGGED_CHUNK], lanes=RAGGED_LANES)
               for i in range(0, len(diagrams), RAGGED_CHUNK)]
     # one workspace for every graph (they replay in order on one stream); slice groups
-    # sized to a fixed budget
-    budget = 8 << 30
+    # sized to a fixed budget, shared by the lanes
+    budget = 32 << 30
     plans = []
     for b in chunks:
         for ring, pr in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ())):
