@@ -508,6 +508,9 @@ def run_gb300(args) -> None:
 
     batched = None
     if ragged is not None:
+        # the headline's workspaces are no longer needed: give their memory to the batch
+        del ws_count, ws_sat
+        torch.cuda.empty_cache()
         instances, trees, expected, plan_s = ragged
         lo, hi = args.n_range
         r = ragged_measure(instances, trees, expected, args.batched_steps, args.warmup,
@@ -684,7 +687,7 @@ def ragged_measure(instances, trees, expected, steps: int, warmup: int, e2e_step
               for i in range(0, len(diagrams), RAGGED_CHUNK)]
     # one workspace for every graph (they replay in order on one stream); slice groups
     # sized to a fixed budget, shared by the lanes
-    budget = 32 << 30
+    budget = 16 << 30
     plans = []
     for b in chunks:
         for ring, pr in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ())):
@@ -739,7 +742,10 @@ def ragged_measure(instances, trees, expected, steps: int, warmup: int, e2e_step
     answers = []
     for b, i in zip(chunks, range(0, len(diagrams), RAGGED_CHUNK)):
         b.load(diagrams[i: i + RAGGED_CHUNK])
-        answers.append((b.count(num_primes=NUM_PRIMES), [bool(x) for x in b.contract()]))
+        gm = b.groups(_native.TSG_RING_MODP, NUM_PRIMES, budget)
+        go = b.groups(_native.TSG_RING_OR_AND, 1, budget)
+        answers.append((b.count(num_primes=NUM_PRIMES, groups=gm, workspace=ws),
+                        [bool(x) for x in b.contract(groups=go, workspace=ws)]))
     torch.cuda.synchronize()
     uncaptured_value = len(diagrams) / (time.perf_counter() - t0)
     got_counts = [int(x) for counts, _ in answers for x in counts]

@@ -382,6 +382,25 @@ TSG_API tsg_status tsg_plan_run_static(const tsg_plan* plan, int32_t ring, int32
                                int64_t slice_begin, int64_t slice_end, int64_t group_size,
                                void* result_dev, int32_t accumulate, void* stream);
 
+/* ---------------------------------------------------------------------------------
+ * Learned cost model (tensorsat_gb300/costmodel.py): a message-passing network over
+ * contraction trees that predicts a tree's device time and ranks candidate trees. Its
+ * answers never reach a contraction's result. No counterpart in the reference, whose tree
+ * search is cotengra's hyper-optimiser (tensorsat/contractions/cotengra.py:78-85).
+ * ------------------------------------------------------------------------------- */
+
+/* out[M x N] = a[M x K] * b[N x K]^T (+ bias[N]) (ReLU if relu != 0), on the tensor cores
+ * (tcgen05.mma kind::f16: BF16 a and b, row-major with K contiguous, 16-byte aligned; FP32
+ * accumulation in tensor memory); out is FP32 (out_f32 != 0) or BF16, row stride ldo
+ * elements. M a multiple of 128, K of 64, N 64 or 128. */
+TSG_API tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void* a_dev,
+                            const void* b_dev, const float* bias_dev, int32_t relu,
+                            void* out_dev, int64_t ldo, int32_t out_f32, void* stream);
+
+/* Synchronizes `stream` and reports (then clears) a bounded wait of the cost model's
+ * kernels that gave up (TSG_ERR_TIMEOUT). */
+TSG_API tsg_status tsg_cm_take_error(void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -74,6 +74,8 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_set_step_options",
     "tsg_plan_variants_workspace_bytes",
     "tsg_plan_run_variants",
+    "tsg_cm_gemm_bf16",
+    "tsg_cm_take_error",
 )
 
 
@@ -171,6 +173,11 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_plan_run_variants.argtypes = [c_void_p, c_int32, c_int32, POINTER(c_uint32),
                                           c_void_p, c_int64, c_int64, c_int64, c_void_p,
                                           c_int64, c_void_p, c_int32, c_void_p]
+    lib.tsg_cm_gemm_bf16.restype = c_int32
+    lib.tsg_cm_gemm_bf16.argtypes = [c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p,
+                                     c_int32, c_void_p, c_int64, c_int32, c_void_p]
+    lib.tsg_cm_take_error.restype = c_int32
+    lib.tsg_cm_take_error.argtypes = [c_void_p]
     lib.tsg_plan_set_step_options.restype = c_int32
     lib.tsg_plan_set_step_options.argtypes = [c_void_p, c_int32, _i32p]
     lib.tsg_plan_launches.restype = c_int32

@@ -1,0 +1,240 @@
+// Kernels of the learned cost model (tensorsat_gb300/costmodel.py): a message-passing
+// network over contraction trees that predicts a tree's device time, used to rank the
+// planner's candidate trees. None of this touches the answers of a contraction.
+//
+// The dense layers run on the 5th-generation tensor cores: tcgen05.mma (kind::f16, BF16
+// operands, FP32 accumulation in tensor memory), one elected thread issuing the MMAs of a
+// 128-row tile, operands staged in shared memory in the canonical K-major layout without
+// swizzling (8-row x 16-byte core matrices), the accumulator read back with tcgen05.ld
+// for a fused epilogue (bias, ReLU, BF16 or FP32 store). The remaining training kernels
+// (child aggregation and its transpose, weight gradients, Adam) are plain CUDA.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "tsg_common.cuh"
+
+namespace tsg {
+namespace cm {
+
+constexpr int kTileM = 128;  // rows of one CTA tile = TMEM lanes
+constexpr int kTileK = 64;   // K staged per round (4 MMAs of K = 16)
+constexpr int kThreads = 128;
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__device__ int g_cm_error = 0;  // set when a bounded wait for the MMAs gives up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading-dimension byte offset
+// (between core matrices adjacent in K), stride byte offset (between 8-row groups),
+// descriptor version 1, no swizzling.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // version
+  return d;                // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major,
+// N columns, M = 128 rows.
+__host__ __device__ constexpr uint32_t instr_desc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(kTileM >> 4) << 24);
+}
+
+// Byte offset of element (r, k) of a rows x kTileK tile in the canonical K-major layout:
+// core matrix (r / 8, k / 8) of 8 rows x 16 bytes, K-adjacent core matrices 128 bytes
+// apart (LBO), 8-row groups kTileK / 8 * 128 bytes apart (SBO).
+__device__ __forceinline__ uint32_t tile_offset(int r, int k) {
+  return (uint32_t)((r >> 3) * (kTileK / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ bool wait_mbar(uint64_t* bar, uint32_t parity) {
+  const uint32_t addr = smem_u32(bar);
+  uint64_t t0;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity), "r"(20000u)
+        : "memory");
+    if (ok) return true;
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (t - t0 > kWaitNs) return false;
+  }
+}
+
+// D[M x N] = A[M x K] * B[N x K]^T (+ bias[N], ReLU): A and B row-major BF16 (K
+// contiguous), K a multiple of 64, M a multiple of 128, N in {64, 128}. One CTA per
+// 128-row tile, all N columns in tensor memory.
+template <int N>
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_bf16_tn_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B,
+                        const float* __restrict__ bias, void* out, int K, int ldo, int relu,
+                        int out_f32) {
+  __shared__ __align__(128) uint8_t sa[kTileM * kTileK * 2];
+  __shared__ __align__(128) uint8_t sb[N * kTileK * 2];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int m0 = blockIdx.x * kTileM;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"((uint32_t)N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = instr_desc(N);
+  const int ktiles = K / kTileK;
+  bool ok = true;
+  for (int kt = 0; kt < ktiles && ok; ++kt) {
+    // stage the A and B tiles: 16-byte chunks (8 consecutive K values) per thread
+    const int k0 = kt * kTileK;
+    for (int c = tid; c < kTileM * (kTileK / 8); c += kThreads) {
+      const int r = c / (kTileK / 8), kc = (c % (kTileK / 8)) * 8;
+      const uint4 v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * K + k0 + kc);
+      *reinterpret_cast<uint4*>(sa + tile_offset(r, kc)) = v;
+    }
+    for (int c = tid; c < N * (kTileK / 8); c += kThreads) {
+      const int r = c / (kTileK / 8), kc = (c % (kTileK / 8)) * 8;
+      const uint4 v = *reinterpret_cast<const uint4*>(B + (size_t)r * K + k0 + kc);
+      *reinterpret_cast<uint4*>(sb + tile_offset(r, kc)) = v;
+    }
+    // the generic-proxy stores must be visible to the tensor cores' async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < kTileK / 16; ++kk) {
+        // K = 16 per MMA: two core matrices along K (2 x 128 bytes) further each time
+        const uint64_t ad = smem_desc(smem_u32(sa) + kk * 256, 128, (kTileK / 8) * 128);
+        const uint64_t bd = smem_desc(smem_u32(sb) + kk * 256, 128, (kTileK / 8) * 128);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar))
+          : "memory");
+    }
+    // the MMAs read the staged tiles: wait before the next round overwrites them
+    if (!wait_mbar(&mbar, (uint32_t)(kt & 1))) {
+      if (tid == 0) atomicExch(&g_cm_error, TSG_ERR_TIMEOUT);
+      ok = false;
+    }
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    // epilogue: warp w reads TMEM lanes 32w..32w+31 (rows), 32 columns per load
+    const int row = m0 + warp * 32 + (tid & 31);
+#pragma unroll 1
+    for (int c0 = 0; c0 < N; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+            "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+            "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
+            "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+            "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        float x = __uint_as_float(v[j]);
+        if (bias) x += bias[c0 + j];
+        if (relu) x = fmaxf(x, 0.f);
+        if (out_f32)
+          reinterpret_cast<float*>(out)[(size_t)row * ldo + c0 + j] = x;
+        else
+          reinterpret_cast<__nv_bfloat16*>(out)[(size_t)row * ldo + c0 + j] = __float2bfloat16(x);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)N)
+                 : "memory");
+}
+
+}  // namespace cm
+}  // namespace tsg
+
+using namespace tsg;
+
+extern "C" {
+
+tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void* a_dev,
+                            const void* b_dev, const float* bias_dev, int32_t relu,
+                            void* out_dev, int64_t ldo, int32_t out_f32, void* stream) {
+  if (!a_dev || !b_dev || !out_dev) return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: null pointer");
+  if (m <= 0 || m % cm::kTileM || k <= 0 || k % cm::kTileK || (n != 64 && n != 128) ||
+      ldo < n || m / cm::kTileM > 0x7fffffff)
+    return fail(TSG_ERR_INVALID_ARGUMENT,
+                "cm_gemm: M must be a multiple of 128, K of 64, N 64 or 128, ldo >= N");
+  if (((uintptr_t)a_dev | (uintptr_t)b_dev) & 15)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: operands must be 16-byte aligned");
+  const dim3 grid((unsigned)(m / cm::kTileM));
+  cudaStream_t st = (cudaStream_t)stream;
+  const auto* a = (const __nv_bfloat16*)a_dev;
+  const auto* b = (const __nv_bfloat16*)b_dev;
+  switch (n) {
+    case 64:
+      cm::gemm_bf16_tn_kernel<64><<<grid, cm::kThreads, 0, st>>>(a, b, bias_dev, out_dev, (int)k,
+                                                                 (int)ldo, relu, out_f32);
+      break;
+    default:
+      cm::gemm_bf16_tn_kernel<128><<<grid, cm::kThreads, 0, st>>>(a, b, bias_dev, out_dev, (int)k,
+                                                                  (int)ldo, relu, out_f32);
+      break;
+  }
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status tsg_cm_take_error(void* stream) {
+  int err = 0;
+  const int zero = 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  TSG_CUDA_TRY(cudaMemcpyFromSymbolAsync(&err, cm::g_cm_error, sizeof(int), 0,
+                                         cudaMemcpyDeviceToHost, st));
+  TSG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (err == 0) return TSG_OK;
+  TSG_CUDA_TRY(cudaMemcpyToSymbolAsync(cm::g_cm_error, &zero, sizeof(int), 0,
+                                       cudaMemcpyHostToDevice, st));
+  TSG_CUDA_TRY(cudaStreamSynchronize(st));
+  return fail(TSG_ERR_TIMEOUT, "cost model: a bounded wait for the tensor-core MMAs gave up");
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+"""The cost model's tensor-core GEMM (tcgen05.mma kind::f16, BF16 operands, FP32
+accumulation in tensor memory) against the same product on the host: BF16-rounded inputs,
+FP32 reference; relative tolerance 1e-3 of the largest output for FP32 outputs (the
+accumulation order differs), one BF16 ulp more for BF16 outputs."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from tensorsat_gb300 import _device, _native
+
+pytestmark = pytest.mark.gpu
+
+
+def _gemm(a, b, bias=None, relu=False, out_f32=True):
+    lib = _native.lib()
+    m, k = a.shape
+    n = b.shape[0]
+    out = torch.empty((m, n), dtype=torch.float32 if out_f32 else torch.bfloat16, device=a.device)
+    _native.check(lib.tsg_cm_gemm_bf16(m, n, k, a.data_ptr(), b.data_ptr(),
+                                       None if bias is None else bias.data_ptr(), int(relu),
+                                       out.data_ptr(), n, int(out_f32), _device.stream_handle()))
+    _native.check(lib.tsg_cm_take_error(_device.stream_handle()))
+    return out
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 64, 64), (128, 128, 64), (256, 128, 256), (1024, 128, 128)])
+def test_gemm_matches_host_product(cuda, m, n, k):
+    g = torch.Generator().manual_seed(m + n + k)
+    a = torch.randn(m, k, generator=g).to(torch.bfloat16)
+    b = torch.randn(n, k, generator=g).to(torch.bfloat16)
+    bias = torch.randn(n, generator=g)
+    want = a.float() @ b.float().T + bias
+    got = _gemm(a.to(cuda), b.to(cuda), bias.to(cuda)).cpu()
+    scale = float(want.abs().max())
+    assert float((got - want).abs().max()) <= 1e-3 * scale
+    got_relu = _gemm(a.to(cuda), b.to(cuda), bias.to(cuda), relu=True, out_f32=False).cpu().float()
+    want_relu = want.clamp(min=0)
+    assert float((got_relu - want_relu).abs().max()) <= 1e-3 * scale + 8e-3 * float(want_relu.abs().max())
+
+
+def test_gemm_rejects_bad_shapes(cuda):
+    lib = _native.lib()
+    a = torch.zeros(128, 64, dtype=torch.bfloat16, device=cuda)
+    out = torch.zeros(128, 256, dtype=torch.float32, device=cuda)
+    for m, n, k in [(100, 64, 64), (128, 96, 64), (128, 64, 48), (128, 256, 64)]:
+        assert lib.tsg_cm_gemm_bf16(m, n, k, a.data_ptr(), a.data_ptr(), None, 0, out.data_ptr(),
+                                    256, 1, None) == _native.TSG_ERR_INVALID_ARGUMENT
