@@ -66,7 +66,11 @@ def parse_args():
     p.add_argument("--trials", type=int, default=8)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", default="n60", choices=["n60", "ragged"],
+    p.add_argument("--cm-train", type=int, default=160, help="costmodel: training instances")
+    p.add_argument("--cm-heldout", type=int, default=32, help="costmodel: held-out n=60 instances")
+    p.add_argument("--cm-epochs", type=int, default=150, help="costmodel: training epochs")
+    p.add_argument("--cm-out", default="", help="costmodel: write the trained weights (.npz)")
+    p.add_argument("--workload", default="n60", choices=["n60", "ragged", "costmodel"],
                    help="n60: the single-instance headline workload; ragged: a batch of "
                         "random instances of uneven sizes (batched runs, CUDA graphs)")
     p.add_argument("--instances", type=int, default=512, help="ragged: batch size")
@@ -477,8 +481,9 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES, group=g_modp,
-                          slice_range=(b, e), cache_leaves=False)
-        bool(contraction.contract(diagram, group=g_or, slice_range=(b, e), cache_leaves=False))
+                          slice_range=(b, e), cache_leaves=False, workspace=ws_count)
+        bool(contraction.contract(diagram, group=g_or, slice_range=(b, e), cache_leaves=False,
+                                  workspace=ws_sat))
         torch.cuda.synchronize()
         if k > 0:  # the first call allocates workspaces in torch's caching allocator
             e2e_times.append(time.perf_counter() - t0)
@@ -492,8 +497,9 @@ def run_gb300(args) -> None:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         full_count = contraction.count(diagram, ring="modp", num_primes=NUM_PRIMES,
-                                       group=g_modp, process_group=pg)
-        full_sat = bool(contraction.contract(diagram, group=g_or, process_group=pg))
+                                       group=g_modp, process_group=pg, workspace=ws_count)
+        full_sat = bool(contraction.contract(diagram, group=g_or, process_group=pg,
+                                             workspace=ws_sat))
         torch.cuda.synchronize()
         full_s = time.perf_counter() - t0
         instance = {"count": int(full_count), "sat": full_sat, "seconds": round(full_s, 3),
@@ -849,12 +855,133 @@ def run_ragged(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------------------
+# Learned cost model: trained on the solver's own measurements, evaluated on n=60
+
+
+def _candidates_job(args):
+    num_vars, clauses, count = args
+    from tensorsat_gb300 import costmodel
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    return costmodel.candidate_trees(CNFInstance(num_vars, clauses).clause_diagram().wiring,
+                                     count)
+
+
+def run_costmodel(args) -> None:
+    """Trains the cost model on measured candidate trees of random 3-SAT instances (n
+    uniform in [24, 56]) and evaluates it on held-out n=60, m=256 instances: prediction
+    error of the device time per slice, and the measured time of the tree it picks per
+    instance against the planner's pick and the best candidate."""
+    import numpy as np
+
+    from tensorsat_gb300 import _native
+
+    _native.lib()
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    g = np.random.default_rng(1)
+    train = []
+    for i in range(args.cm_train):
+        n = int(g.integers(24, 57))
+        m = round(float(g.uniform(3.8, 4.6)) * n)
+        train.append(CNFInstance.random(3, n, m, rng=1000 + i))
+    held = [CNFInstance.random(3, N_VARS, N_CLAUSES, rng=10_000 + j) for j in range(args.cm_heldout)]
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with cpu_pool(cores) as pool:
+        cand_train = pool.map(_candidates_job, [(c.num_vars, c.clauses, 5) for c in train])
+        cand_held = pool.map(_candidates_job, [(c.num_vars, c.clauses, 4) for c in held])
+        dpll_held = pool.map(_dpll_instance, [(c.num_vars, c.clauses) for c in held[:4]])
+    plan_s = time.perf_counter() - t0
+
+    import torch
+
+    from tensorsat_gb300 import costmodel
+    from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+
+    torch.cuda.set_device(0)
+    primes = PRIMES_31[:NUM_PRIMES]
+    group = 16
+
+    def measured(instances, cands):
+        rows = []
+        for inst, cs in zip(instances, cands):
+            d = inst.clause_diagram()
+            per = []
+            for tree, sl in cs:
+                c = GpuContraction(CudaRel, d.wiring, tree=tree, sliced=sl)
+                ms = costmodel.measure(c, d, primes, group, passes=1)
+                per.append((c, costmodel.tree_graph(c, min(group, c.num_slices), primes), ms))
+            rows.append(per)
+        return rows
+
+    t0 = time.perf_counter()
+    rows_train = measured(train, cand_train)
+    rows_held = measured(held, cand_held)
+    measure_s = time.perf_counter() - t0
+    graphs = [gph for per in rows_train for _, gph, _ in per]
+    y = [math.log(ms) for per in rows_train for _, _, ms in per]
+    model = costmodel.CostModel(seed=0)
+    t0 = time.perf_counter()
+    hist = model.fit(graphs, y, epochs=args.cm_epochs, batch_trees=64, lr=2e-3)
+    train_s = time.perf_counter() - t0
+    # held-out: per-tree prediction error, per-instance choice
+    hg = [gph for per in rows_held for _, gph, _ in per]
+    hy = np.asarray([math.log(ms) for per in rows_held for _, _, ms in per])
+    pred = np.concatenate([model.predict(costmodel.make_batch(hg[i: i + 64], model.device))
+                           for i in range(0, len(hg), 64)])
+    err = np.abs(pred - hy)
+    picks = []
+    k = 0
+    for per in rows_held:
+        cost_pred = [math.exp(pred[k + j]) * per[j][0].num_slices for j in range(len(per))]
+        cost_meas = [per[j][2] * per[j][0].num_slices for j in range(len(per))]
+        k += len(per)
+        best = min(cost_meas)
+        picks.append((cost_meas[int(np.argmin(cost_pred))] / best, cost_meas[0] / best))
+    # the picked trees' answers are the DPLL counts (any tree gives the same answer)
+    exact = []
+    k = 0
+    for inst, per, want in zip(held[:4], rows_held[:4], dpll_held):
+        cost_pred = [math.exp(pred[k + j]) * per[j][0].num_slices for j in range(len(per))]
+        k += len(per)
+        c = per[int(np.argmin(cost_pred))][0]
+        exact.append(int(c.count(inst.clause_diagram(), ring="modp", num_primes=NUM_PRIMES))
+                     == want)
+    out_path = args.cm_out
+    if out_path:
+        np.savez(out_path, **model.state())
+    line = {
+        "metric": "learned cost model: |log predicted - log measured| device time per slice, "
+                  "held-out 3-SAT n=60 m=256 trees",
+        "value": float(err.mean()), "unit": "mean abs log error", "higher_is_better": False,
+        "median_abs_log_error": float(np.median(err)),
+        "within_20pct": float(np.mean(err < math.log(1.2))),
+        "train_trees": len(graphs), "heldout_instances": len(held), "heldout_trees": len(hg),
+        "model_pick_over_best": float(np.mean([a for a, _ in picks])),
+        "planner_pick_over_best": float(np.mean([b for _, b in picks])),
+        "model_pick_beats_planner": float(np.mean([a < b for a, b in picks])),
+        "picked_trees_exact": exact,
+        "loss_first_last": [hist[0], hist[-1]],
+        "seconds": {"planning": round(plan_s, 1), "measuring": round(measure_s, 1),
+                    "training": round(train_s, 1)},
+        "config": {"hidden": costmodel.HIDDEN, "layers": costmodel.LAYERS, "epochs": args.cm_epochs,
+                   "dtype": "bf16 weights/activations, fp32 accumulation (tcgen05 kind::f16)",
+                   "measure": f"tsg_plan_run_timed, {group} slices, 3-prime count + OR-AND"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "ragged":
         run_ragged(args)
+    elif args.workload == "costmodel":
+        run_costmodel(args)
     else:
         run_gb300(args)
 

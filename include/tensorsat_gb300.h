@@ -397,6 +397,27 @@ TSG_API tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void*
                             const void* b_dev, const float* bias_dev, int32_t relu,
                             void* out_dev, int64_t ldo, int32_t out_f32, void* stream);
 
+/* out[v] = sum of h[u] over the children u of node v (BF16 rows of `width`; children of v
+ * are child[cstart[v] .. cstart[v+1]); out row stride ldo). */
+TSG_API tsg_status tsg_cm_child_sum(const void* h_dev, const int32_t* cstart_dev,
+                            const int32_t* child_dev, void* out_dev, int64_t n,
+                            int32_t width, int32_t ldo, void* stream);
+
+/* dh[u] += dc[parent[u]] for every node with parent[u] >= 0 (FP32 rows; dc row stride ldc):
+ * the transpose of tsg_cm_child_sum, for the backward pass. */
+TSG_API tsg_status tsg_cm_parent_add(const float* dc_dev, int32_t ldc, const int32_t* parent_dev,
+                             float* dh_dev, int64_t n, int32_t width, void* stream);
+
+/* out[p x q] = a[n x p]^T * b[n x q] (FP32, row-major): weight gradients, a reduction over
+ * the n nodes. */
+TSG_API tsg_status tsg_cm_gemm_at_b(const float* a_dev, int32_t p, const float* b_dev,
+                            int32_t q, int64_t n, float* out_dev, void* stream);
+
+/* One Adam step on n FP32 parameters (moments m, v; step >= 1 for the bias correction). */
+TSG_API tsg_status tsg_cm_adam(float* w_dev, const float* g_dev, float* m_dev, float* v_dev,
+                       int64_t n, float lr, float beta1, float beta2, float eps, int32_t step,
+                       void* stream);
+
 /* Synchronizes `stream` and reports (then clears) a bounded wait of the cost model's
  * kernels that gave up (TSG_ERR_TIMEOUT). */
 TSG_API tsg_status tsg_cm_take_error(void* stream);

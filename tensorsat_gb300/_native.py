@@ -76,6 +76,10 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_run_variants",
     "tsg_cm_gemm_bf16",
     "tsg_cm_take_error",
+    "tsg_cm_child_sum",
+    "tsg_cm_parent_add",
+    "tsg_cm_gemm_at_b",
+    "tsg_cm_adam",
 )
 
 
@@ -176,6 +180,18 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_cm_gemm_bf16.restype = c_int32
     lib.tsg_cm_gemm_bf16.argtypes = [c_int64, c_int64, c_int64, c_void_p, c_void_p, c_void_p,
                                      c_int32, c_void_p, c_int64, c_int32, c_void_p]
+    lib.tsg_cm_child_sum.restype = c_int32
+    lib.tsg_cm_child_sum.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int32,
+                                     c_int32, c_void_p]
+    lib.tsg_cm_parent_add.restype = c_int32
+    lib.tsg_cm_parent_add.argtypes = [c_void_p, c_int32, c_void_p, c_void_p, c_int64, c_int32,
+                                      c_void_p]
+    lib.tsg_cm_gemm_at_b.restype = c_int32
+    lib.tsg_cm_gemm_at_b.argtypes = [c_void_p, c_int32, c_void_p, c_int32, c_int64, c_void_p,
+                                     c_void_p]
+    lib.tsg_cm_adam.restype = c_int32
+    lib.tsg_cm_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, ctypes.c_float,
+                                ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int32, c_void_p]
     lib.tsg_cm_take_error.restype = c_int32
     lib.tsg_cm_take_error.argtypes = [c_void_p]
     lib.tsg_plan_set_step_options.restype = c_int32

@@ -570,7 +570,8 @@ class GpuContraction(Contraction):
     def contract(self, diagram: Diagram, *, progbar: bool = False, order: Any = None,
                  autojit: Any = "auto", group: int | None = None,
                  slice_range: tuple[int, int] | None = None,
-                 cache_leaves: bool = True, process_group: Any = None) -> CudaRel:
+                 cache_leaves: bool = True, process_group: Any = None,
+                 workspace: torch.Tensor | None = None) -> CudaRel:
         """Validates and contracts the diagram in the OR-AND semiring; returns the result
         box (a scalar box for a SAT network: ``bool(box)`` is the SAT bit).
 
@@ -578,12 +579,15 @@ class GpuContraction(Contraction):
         slices only). With a ``torch.distributed`` ``process_group`` every rank of the
         group contracts its own contiguous share of the slices and one all-reduce ORs the
         shares, so every rank returns the whole result (see :meth:`shard_range`).
-        ``progbar``, ``order`` and ``autojit`` are accepted for signature parity with
-        ``CotengraContraction.contract`` and have no effect."""
+        ``workspace`` (uint8 device buffer of at least ``tsg_plan_workspace_bytes``) is
+        used instead of a new allocation. ``progbar``, ``order`` and ``autojit`` are
+        accepted for signature parity with ``CotengraContraction.contract`` and have no
+        effect."""
         self.validate(diagram)
         if process_group is None:
             res = self.run(diagram, _native.TSG_RING_OR_AND, group=group,
-                           slice_range=slice_range, cache_leaves=cache_leaves)
+                           slice_range=slice_range, cache_leaves=cache_leaves,
+                           workspace=workspace)
             self.check_device()
             return self._box_from_root(res)
         group = self._shard_group(_native.TSG_RING_OR_AND, 1, group, process_group)
@@ -591,7 +595,7 @@ class GpuContraction(Contraction):
         entries = 1 << len(self._leaves.out_unique)
         if local[0] < local[1]:
             root = self._ring_root(diagram, _native.TSG_RING_OR_AND, (), local, group,
-                                   cache_leaves)
+                                   cache_leaves, workspace)
         else:
             root = np.zeros(entries, dtype=np.uint8)
         root = sharding.allreduce_or(torch.from_numpy(root.astype(np.int32)).to(
@@ -633,12 +637,13 @@ class GpuContraction(Contraction):
         return g
 
     def _ring_root(self, diagram: Diagram, ring: int, primes: Sequence[int],
-                   slice_range: tuple[int, int], group: int, cache_leaves: bool) -> np.ndarray:
+                   slice_range: tuple[int, int], group: int, cache_leaves: bool,
+                   workspace: torch.Tensor | None = None) -> np.ndarray:
         """Root entries of one device run over ``slice_range``, on the host: uint8 [entries]
         (OR-AND), uint64 [entries] (U64) or uint32 [planes, entries] (MODP, plain
         residues). Raises if a kernel recorded a device-side failure."""
         res = self.run(diagram, ring, primes=primes, group=group, slice_range=slice_range,
-                       cache_leaves=cache_leaves)
+                       cache_leaves=cache_leaves, workspace=workspace)
         self.check_device()
         host = res.cpu().numpy()
         if ring == _native.TSG_RING_U64:
@@ -658,7 +663,8 @@ class GpuContraction(Contraction):
 
     def count(self, diagram: Diagram, *, ring: str = "auto", num_primes: int | None = None,
               group: int | None = None, slice_range: tuple[int, int] | None = None,
-              cache_leaves: bool = True, process_group: Any = None) -> Any:
+              cache_leaves: bool = True, process_group: Any = None,
+              workspace: torch.Tensor | None = None) -> Any:
         """Exact model count (``int``) of a closed network, or a numpy object array of
         counts indexed by the out wires.
 
@@ -670,7 +676,9 @@ class GpuContraction(Contraction):
         ``process_group`` (one rank per GPU) every rank counts its own contiguous share
         of the slices (:meth:`shard_range`) with no exchange while contracting, and one
         all-reduce adds the shares (per prime mod p, or mod 2^64), so every rank returns
-        the whole count.
+        the whole count. ``workspace`` (uint8 device buffer of at least
+        ``tsg_plan_workspace_bytes`` for the ring and group) is used instead of a new
+        allocation.
         """
         self.validate(diagram)
         arrays = []
@@ -690,7 +698,7 @@ class GpuContraction(Contraction):
             local = self.shard_range(slice_range, g, process_group)
             if local[0] < local[1]:
                 vals = self._ring_root(diagram, _native.TSG_RING_U64, (), local, g,
-                                       cache_leaves)
+                                       cache_leaves, workspace)
             else:
                 vals = np.zeros(entries, dtype=np.uint64)
             if process_group is not None:
@@ -716,7 +724,7 @@ class GpuContraction(Contraction):
                 chunk = primes[i: i + _native.TSG_MAX_PRIMES]
                 if local[0] < local[1]:
                     planes = self._ring_root(diagram, _native.TSG_RING_MODP, chunk, local, g,
-                                             cache_leaves)
+                                             cache_leaves, workspace)
                 else:
                     planes = np.zeros((len(chunk), entries), dtype=np.uint32)
                 if process_group is not None:

@@ -11,6 +11,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "tsg_common.cuh"
@@ -188,6 +189,80 @@ __global__ void __launch_bounds__(kThreads, 1)
                  : "memory");
 }
 
+// Sum of each node's children's rows: out[v] = sum over children u of h[u] (BF16 rows of
+// width w, FP32 sum; the tree's child lists in CSR form: child[cstart[v] .. cstart[v+1])).
+__global__ void child_sum_kernel(const __nv_bfloat16* __restrict__ h, const int32_t* __restrict__ cstart,
+                                 const int32_t* __restrict__ child, __nv_bfloat16* __restrict__ out,
+                                 int64_t n, int w, int ldo) {
+  const int64_t v = blockIdx.x;
+  if (v >= n) return;
+  for (int j = threadIdx.x; j < w; j += blockDim.x) {
+    float acc = 0.f;
+    for (int32_t e = cstart[v]; e < cstart[v + 1]; ++e) acc += __bfloat162float(h[(int64_t)child[e] * w + j]);
+    out[v * ldo + j] = __float2bfloat16(acc);
+  }
+}
+
+// Transpose of child_sum for the backward pass: dh[u] += dc[parent[u]] (FP32 rows), for
+// every node u with a parent (parent[u] >= 0).
+__global__ void parent_add_kernel(const float* __restrict__ dc, int ldc,
+                                  const int32_t* __restrict__ parent, float* __restrict__ dh,
+                                  int64_t n, int w) {
+  const int64_t u = blockIdx.x;
+  if (u >= n) return;
+  const int32_t p = parent[u];
+  if (p < 0) return;
+  for (int j = threadIdx.x; j < w; j += blockDim.x) dh[u * w + j] += dc[(int64_t)p * ldc + j];
+}
+
+// out[i][j] = sum_n a[n][i] * b[n][j] (FP32; a: n x p, b: n x q, row-major): the weight
+// gradients, a reduction over the nodes. 32 x 32 output tiles, the node range split over
+// gridDim.z slabs accumulated with atomics (out cleared by the caller).
+__global__ void __launch_bounds__(256)
+    gemm_at_b_kernel(const float* __restrict__ a, int p, const float* __restrict__ b, int q,
+                     int64_t n, float* __restrict__ out) {
+  __shared__ float sa[32][33], sb[32][33];
+  const int ti = threadIdx.x / 32, tj = threadIdx.x % 32;  // 8 x 32 threads
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int64_t slab = (n + gridDim.z - 1) / gridDim.z;
+  const int64_t n0 = blockIdx.z * slab, n1 = n0 + slab < n ? n0 + slab : n;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int64_t k0 = n0; k0 < n1; k0 += 32) {
+    for (int r = ti; r < 32; r += 8) {
+      const int64_t row = k0 + r;
+      sa[r][tj] = (row < n1 && i0 + tj < p) ? a[row * p + i0 + tj] : 0.f;
+      sb[r][tj] = (row < n1 && j0 + tj < q) ? b[row * q + j0 + tj] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int r = 0; r < 32; ++r) {
+      const float bv = sb[r][tj];
+#pragma unroll
+      for (int x = 0; x < 4; ++x) acc[x] += sa[r][ti + 8 * x] * bv;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int x = 0; x < 4; ++x) {
+    const int i = i0 + ti + 8 * x, j = j0 + tj;
+    if (i < p && j < q) atomicAdd(&out[(int64_t)i * q + j], acc[x]);
+  }
+}
+
+// One Adam step (Kingma & Ba, 2015) on FP32 parameters with bias-corrected moments.
+__global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
+                            float* __restrict__ m, float* __restrict__ v, int64_t n, float lr,
+                            float b1, float b2, float eps, float c1, float c2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
 }  // namespace cm
 }  // namespace tsg
 
@@ -219,6 +294,54 @@ tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void* a_dev,
                                                                   (int)ldo, relu, out_f32);
       break;
   }
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status tsg_cm_child_sum(const void* h_dev, const int32_t* cstart_dev, const int32_t* child_dev,
+                            void* out_dev, int64_t n, int32_t width, int32_t ldo, void* stream) {
+  if (!h_dev || !cstart_dev || !child_dev || !out_dev || n < 0 || width <= 0 || ldo < width)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_child_sum: bad arguments");
+  if (n == 0) return TSG_OK;
+  cm::child_sum_kernel<<<(unsigned)n, 128, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)h_dev, cstart_dev, child_dev, (__nv_bfloat16*)out_dev, n, width, ldo);
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status tsg_cm_parent_add(const float* dc_dev, int32_t ldc, const int32_t* parent_dev,
+                             float* dh_dev, int64_t n, int32_t width, void* stream) {
+  if (!dc_dev || !parent_dev || !dh_dev || n < 0 || width <= 0 || ldc < width)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_parent_add: bad arguments");
+  if (n == 0) return TSG_OK;
+  cm::parent_add_kernel<<<(unsigned)n, 128, 0, (cudaStream_t)stream>>>(dc_dev, ldc, parent_dev,
+                                                                       dh_dev, n, width);
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status tsg_cm_gemm_at_b(const float* a_dev, int32_t p, const float* b_dev, int32_t q,
+                            int64_t n, float* out_dev, void* stream) {
+  if (!a_dev || !b_dev || !out_dev || p <= 0 || q <= 0 || n < 0)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm_at_b: bad arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  TSG_CUDA_TRY(cudaMemsetAsync(out_dev, 0, sizeof(float) * (size_t)p * q, st));
+  if (n == 0) return TSG_OK;
+  const unsigned slabs = (unsigned)std::max<int64_t>(1, std::min<int64_t>(64, n / 4096));
+  const dim3 grid((unsigned)((q + 31) / 32), (unsigned)((p + 31) / 32), slabs);
+  cm::gemm_at_b_kernel<<<grid, 256, 0, st>>>(a_dev, p, b_dev, q, n, out_dev);
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status tsg_cm_adam(float* w_dev, const float* g_dev, float* m_dev, float* v_dev, int64_t n,
+                       float lr, float beta1, float beta2, float eps, int32_t step, void* stream) {
+  if (!w_dev || !g_dev || !m_dev || !v_dev || n < 0 || step < 1)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_adam: bad arguments");
+  if (n == 0) return TSG_OK;
+  const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+  cm::adam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      w_dev, g_dev, m_dev, v_dev, n, lr, beta1, beta2, eps, c1, c2);
   TSG_CUDA_TRY(cudaGetLastError());
   return TSG_OK;
 }

@@ -1,0 +1,41 @@
+"""Host parts of the learned cost model: candidate trees, tree graphs and batches (no
+GPU needed)."""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from tensorsat_gb300 import costmodel
+from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction, plan_tree
+from tensorsat_gb300.lang.cuda_rel import CudaRel
+from tensorsat_gb300.lib.sat import CNFInstance
+
+
+def test_candidates_graphs_and_batches():
+    cnf = CNFInstance.random(3, 24, 100, rng=3)
+    w = cnf.clause_diagram().wiring
+    cands = costmodel.candidate_trees(w, 4)
+    assert 2 <= len(cands) <= 4
+    assert len({tuple(t.steps) for t, _ in cands}) == len(cands)
+    # the first candidate is the planner's usual choice
+    tree, sl = plan_tree(w, target_bits=26, trials=8, seed=0)
+    assert tuple(cands[0][0].steps) == tuple(tree.steps) and cands[0][1] == sl
+    graphs = []
+    for t, s in cands:
+        c = GpuContraction(CudaRel, w, tree=t, sliced=s)
+        g = costmodel.tree_graph(c, 1, PRIMES_31[:3])
+        L = t.num_leaves
+        assert g["x"].shape == (L + len(t.steps), costmodel.FEATURES)
+        assert all(g["children"][L + i] == t.steps[i] for i in range(len(t.steps)))
+        assert np.all(g["x"][:L, 0] == 1) and np.all(g["x"][L:, 1] == 1)
+        graphs.append(g)
+    b = costmodel.make_batch(graphs, torch.device("cpu"))
+    n = sum(g["x"].shape[0] for g in graphs)
+    assert b.nodes == n and b.x.shape[0] % 128 == 0 and b.graphs == len(graphs)
+    cstart, child, parent = b.cstart.numpy(), b.child.numpy(), b.parent.numpy()
+    # every child edge appears once and points back to its parent
+    for v in range(n):
+        for e in range(cstart[v], cstart[v + 1]):
+            assert parent[child[e]] == v
+    assert int((parent >= 0).sum()) == cstart[-1] == sum(2 * (len(g["x"]) - 1) // 2 for g in graphs)

@@ -48,3 +48,50 @@ def test_gemm_rejects_bad_shapes(cuda):
     for m, n, k in [(100, 64, 64), (128, 96, 64), (128, 64, 48), (128, 256, 64)]:
         assert lib.tsg_cm_gemm_bf16(m, n, k, a.data_ptr(), a.data_ptr(), None, 0, out.data_ptr(),
                                     256, 1, None) == _native.TSG_ERR_INVALID_ARGUMENT
+
+
+def _reference_forward(model, graphs):
+    """The same network in plain FP32 torch (operands rounded to BF16 like the kernels)."""
+    from tensorsat_gb300 import costmodel as cm
+
+    r = lambda t: t.to(torch.bfloat16).float()
+    out = []
+    for g in graphs:
+        x = r(torch.from_numpy(g["x"]).cuda())
+        h = r(torch.relu(x @ r(model.params["w_in"]).T + model.params["b_in"]))
+        for l in range(cm.LAYERS):
+            c = torch.zeros_like(h)
+            for v, ch in enumerate(g["children"]):
+                for u in ch:
+                    c[v] += h[u]
+            hc = torch.cat([h, r(c)], 1)
+            h = r(torch.relu(hc @ r(model.params[f"w{l}"]).T + model.params[f"b{l}"]))
+        out.append(float(h.sum(0) @ model.params["w_out"] + model.params["b_out"]))
+    return np.asarray(out)
+
+
+def test_cost_model_forward_and_training(cuda):
+    """The message-passing network on the tensor cores equals the same network in FP32
+    torch within BF16 rounding, and its training kernels (children sums and their
+    transpose, weight gradients, Adam) fit a synthetic target: the loss falls well below
+    its start."""
+    from tensorsat_gb300 import costmodel as cm
+    from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    graphs = []
+    for seed in range(24):
+        cnf = CNFInstance.random(3, 16 + seed % 8, 4 * (16 + seed % 8), rng=seed)
+        c = GpuContraction(CudaRel, cnf.clause_diagram().wiring, target_bits=10, trials=1)
+        graphs.append(cm.tree_graph(c, min(4, c.num_slices), PRIMES_31[:3]))
+    model = cm.CostModel(seed=1)
+    batch = cm.make_batch(graphs[:6], model.device)
+    got = model.predict(batch) - model.y_mean
+    want = _reference_forward(model, graphs[:6])
+    assert np.allclose(got, want, rtol=0.03, atol=0.03 * float(np.abs(want).max()))
+    # synthetic target: log of the trees' total index space (a function of the features)
+    y = [float(np.log(sum(2.0 ** (32 * g["x"][v, 4]) for v in range(len(g["x"]))
+                          if g["x"][v, 1] > 0))) for g in graphs]
+    hist = model.fit(graphs, y, epochs=60, batch_trees=8, lr=3e-3)
+    assert hist[-1] < 0.25 * hist[0], hist[::10]
