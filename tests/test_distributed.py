@@ -49,7 +49,8 @@ def _worker(rank: int, world: int, store_file: str, q) -> None:
         steps, sliced = list(c.tree.steps), list(c.sliced_wires)
         shares = []
 
-        def host_root(self, diagram, ring, primes, slice_range, group, cache_leaves):
+        def host_root(self, diagram, ring, primes, slice_range, group, cache_leaves,
+                      workspace=None):
             # the device run of one rank's share, replaced by the oracle's contraction of
             # the same slices along the same tree
             shares.append(tuple(slice_range))
