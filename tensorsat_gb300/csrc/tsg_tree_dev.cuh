@@ -439,7 +439,9 @@ __device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t
 // so the kernel passes (lhs, rhs) or (rhs, lhs). With a fixed summed count (NK > 0) the
 // thread gathers all of Y's values of a plane before its first store: loads placed after
 // a store to a possibly aliasing address would each wait out their own latency.
-template <int kRing, int V, int NE, int NK>
+// kNoLeaf: neither operand is a leaf (the common large step), so every product is a
+// product of two Montgomery residues and the arithmetic needs no per-thread leaf checks.
+template <int kRing, int V, int NE, int NK, bool kNoLeaf = false>
 __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& ring,
                                             const TileOperand& X, const TileOperand& Y,
                                             uint64_t x0, uint64_t y0, uint64_t oo,
@@ -511,7 +513,9 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
     constexpr int PP = (kRing == TSG_RING_MODP) ? TSG_MAX_PRIMES : 1;
     constexpr bool kHoist = NK > 0 && NE * KU * V * sizeof(VT) <= 64;  // more spills registers
     const int np = p_hi;
-    const int leaves = X.leaf + Y.leaf;
+    const int leaves = kNoLeaf ? 0 : X.leaf + Y.leaf;
+    // partial sums are reduced pairwise only with more than two summed combinations
+    constexpr bool kPairs = NK == 0 || NK > 2;
     VT xcur[KU][V], xnxt[KU][V];
     auto preload = [&](int p, VT (&xb)[KU][V]) {
       const uint64_t xp = x0 + (X.leaf ? 0 : p * X.plane);
@@ -589,7 +593,7 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
                 acc[j] += (AT)xv[j] * (AT)yv[j];
               }
             }
-            if constexpr (kRing == TSG_RING_MODP) {
+            if constexpr (kRing == TSG_RING_MODP && kPairs) {
               // two Montgomery products stay below p 2^32: reduce every pair of sums
               if (leaves == 0 && (kk & 1) && kk + 1 < nk) {
 #pragma unroll
@@ -618,7 +622,8 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
           uint32_t r[V];
 #pragma unroll
           for (int j = 0; j < V; ++j)
-            r[j] = add_mod(done[j], mont_finish_c(acc[j], leaves, pc), pc.p);
+            r[j] = kPairs ? add_mod(done[j], mont_finish_c(acc[j], leaves, pc), pc.p)
+                          : mont_finish_c(acc[j], leaves, pc);
           if (V == 4 && a.o_contig) {
             *reinterpret_cast<uint4*>(out + oe) = make_uint4(r[0], r[1 % V], r[2 % V], r[3 % V]);
           } else {
@@ -658,11 +663,20 @@ __global__ void __launch_bounds__(kThreads, 4) tree_step_tile_kernel(TileArgs a,
   const int np = kRing == TSG_RING_MODP ? ring.np : 1;
   const int p_lo = a.plane_split ? (int)blockIdx.z : 0;
   const int p_hi = a.plane_split ? p_lo + 1 : np;
-  // at most one operand carries E bits (the other is the one E was chosen against)
-  if (!a.op[0].has_e)
-    tile_thread<kRing, V, NE, NK>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo, p_lo, p_hi);
-  else
-    tile_thread<kRing, V, NE, NK>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo, p_lo, p_hi);
+  // at most one operand carries E bits (the other is the one E was chosen against); the
+  // count rings take a leaf-free path when neither operand is a leaf
+  const bool no_leaf = kRing == TSG_RING_MODP && !a.op[0].leaf && !a.op[1].leaf;
+  if (!a.op[0].has_e) {
+    if (no_leaf)
+      tile_thread<kRing, V, NE, NK, true>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo, p_lo, p_hi);
+    else
+      tile_thread<kRing, V, NE, NK>(a, ring, a.op[0], a.op[1], xo[0], xo[1], oo, p_lo, p_hi);
+  } else {
+    if (no_leaf)
+      tile_thread<kRing, V, NE, NK, true>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo, p_lo, p_hi);
+    else
+      tile_thread<kRing, V, NE, NK>(a, ring, a.op[1], a.op[0], xo[1], xo[0], oo, p_lo, p_hi);
+  }
 }
 
 // ------------------------------------------------------------------------------------
