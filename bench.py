@@ -66,11 +66,16 @@ def parse_args():
     p.add_argument("--trials", type=int, default=8)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--learned-instances", type=int, default=8,
+                   help="held-out n=60 instances of the learned-path leg of the default run")
+    p.add_argument("--learned-candidates", type=int, default=64,
+                   help="planner candidate trees the cost model ranks per instance")
     p.add_argument("--cm-train", type=int, default=160, help="costmodel: training instances")
     p.add_argument("--cm-heldout", type=int, default=32, help="costmodel: held-out n=60 instances")
     p.add_argument("--cm-epochs", type=int, default=150, help="costmodel: training epochs")
     p.add_argument("--cm-out", default="", help="costmodel: write the trained weights (.npz)")
-    p.add_argument("--workload", default="n60", choices=["n60", "ragged", "costmodel"],
+    p.add_argument("--workload", default="n60",
+                   choices=["n60", "ragged", "costmodel", "costmodel-gemm"],
                    help="n60: the single-instance headline workload; ragged: a batch of "
                         "random instances of uneven sizes (batched runs, CUDA graphs)")
     p.add_argument("--instances", type=int, default=512, help="ragged: batch size")
@@ -343,6 +348,12 @@ def run_gb300(args) -> None:
     if want_batched:
         lo, hi = args.n_range
         ragged = ragged_prepare(pool, args.instances, lo, hi)
+    learned_prep = None
+    if want_batched and args.learned_instances > 0:
+        held = costmodel_heldout(args.learned_instances)
+        cands = candidates_parallel(pool, held, args.learned_candidates)
+        dpll_held = pool.map(_dpll_instance, [(c.num_vars, c.clauses) for c in held])
+        learned_prep = (held, cands, dpll_held)
     cnf, diagram, contraction = build_workload(args)
     # the checker's exact count of the whole instance (DPLL, in a spawned worker)
     dpll = pool.apply_async(_dpll_instance, ((cnf.num_vars, cnf.clauses),)) if pool else None
@@ -546,6 +557,8 @@ def run_gb300(args) -> None:
             "step_ms": [round(x, 3) for x in r["step_ms"]],
         }
 
+    learned = learned_leg(*learned_prep) if learned_prep is not None else None
+
     cpu = None
     if want_cpu:
         dt, _ = cpu_sample(pool, cores, cnf, contraction, 0)
@@ -581,6 +594,7 @@ def run_gb300(args) -> None:
             "tuning": tuning,
             "instance": instance,
             "batched": batched,
+            "learned": learned,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -860,12 +874,150 @@ def run_ragged(args) -> None:
 
 
 def _candidates_job(args):
-    num_vars, clauses, count = args
+    num_vars, clauses, count = args[:3]
+    settings = args[3] if len(args) > 3 else None
     from tensorsat_gb300 import costmodel
     from tensorsat_gb300.lib.sat import CNFInstance
 
     return costmodel.candidate_trees(CNFInstance(num_vars, clauses).clause_diagram().wiring,
-                                     count)
+                                     count, settings=settings)
+
+
+def candidates_parallel(pool, instances, count: int, parts: int = 8):
+    """The planner candidates of every instance, each instance's settings split over
+    ``parts`` workers (the planner's usual choice stays first)."""
+    from tensorsat_gb300 import costmodel
+
+    settings = costmodel.candidate_settings(count)
+    jobs = [(c.num_vars, c.clauses, count, settings[p::parts])
+            for c in instances for p in range(parts)]
+    res = pool.map(_candidates_job, jobs, chunksize=1)
+    out = []
+    for i in range(len(instances)):
+        share = res[i * parts:(i + 1) * parts]
+        merged = [t for k in range(max(len(x) for x in share))
+                  for x in share if k < len(x) for t in [x[k]]]
+        out.append(costmodel.distinct(merged))
+    return out
+
+
+COSTMODEL_FILE = ROOT / "plans" / "costmodel_n60.npz"
+
+
+def costmodel_heldout(count: int):
+    """Held-out n=60, m=256 instances of the cost model's evaluation (seeds 10000 on)."""
+    from tensorsat_gb300.lib.sat import CNFInstance
+
+    return [CNFInstance.random(3, N_VARS, N_CLAUSES, rng=10_000 + j) for j in range(count)]
+
+
+def costmodel_measure(instances, cands, group: int):
+    """Every candidate tree of every instance: (contraction, tree graph, measured device
+    ms per slice) per candidate, per instance."""
+    from tensorsat_gb300 import costmodel
+    from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+
+    primes = PRIMES_31[:NUM_PRIMES]
+    rows = []
+    for inst, cs in zip(instances, cands):
+        d = inst.clause_diagram()
+        per = []
+        for tree, sl in cs:
+            c = GpuContraction(CudaRel, d.wiring, tree=tree, sliced=sl)
+            ms = costmodel.measure(c, d, primes, group, passes=1)
+            per.append((c, costmodel.tree_graph(c, min(group, c.num_slices), primes), ms))
+        rows.append(per)
+    return rows
+
+
+def costmodel_evaluate(model, held, rows, dpll, exact_checks: int) -> dict:
+    """Prediction error on the held-out trees, and per instance the measured device time
+    of the tree the model picks against the planner's pick (candidate 0) and the best."""
+    import numpy as np
+
+    from tensorsat_gb300 import costmodel
+
+    hg = [gph for per in rows for _, gph, _ in per]
+    hy = np.asarray([math.log(ms) for per in rows for _, _, ms in per])
+    pred = np.concatenate([model.predict(costmodel.make_batch(hg[i: i + 64], model.device))
+                           for i in range(0, len(hg), 64)])
+    err = np.abs(pred - hy)
+    picks, chosen = [], []
+    k = 0
+    for per in rows:
+        cost_pred = [math.exp(pred[k + j]) * per[j][0].num_slices for j in range(len(per))]
+        cost_meas = [per[j][2] * per[j][0].num_slices for j in range(len(per))]
+        k += len(per)
+        j = int(np.argmin(cost_pred))
+        chosen.append(per[j][0])
+        picks.append((cost_meas[j], cost_meas[0], min(cost_meas)))
+    exact = [int(c.count(inst.clause_diagram(), ring="modp", num_primes=NUM_PRIMES)) == want
+             for inst, c, want in list(zip(held, chosen, dpll))[:exact_checks]]
+    return {
+        "mean_abs_log_error": float(err.mean()), "median_abs_log_error": float(np.median(err)),
+        "within_20pct": float(np.mean(err < math.log(1.2))),
+        "heldout_instances": len(held), "heldout_trees": len(hg),
+        "model_pick_over_best": float(np.mean([m / b for m, _, b in picks])),
+        "planner_pick_over_best": float(np.mean([p / b for _, p, b in picks])),
+        "learned_over_plain": float(np.mean([p / m for m, p, _ in picks])),
+        "learned_over_plain_total": float(sum(p for _, p, _ in picks) / sum(m for m, _, _ in picks)),
+        "picked_trees_exact": exact,
+    }
+
+
+def learned_leg(held, cands, dpll_held, group: int = 16) -> dict:
+    """The learned path on held-out n=60 instances: the committed cost model ranks each
+    instance's planner candidates by predicted device time (per-slice prediction x slices)
+    and picks the cheapest; the planner's own tree (candidate 0) is the plain path and the
+    fallback whenever the model ranks it first. Both picks are measured on the device and
+    the picked tree's full count is checked against DPLL on two instances."""
+    import numpy as np
+
+    from tensorsat_gb300 import costmodel
+    from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
+    from tensorsat_gb300.lang.cuda_rel import CudaRel
+
+    primes = PRIMES_31[:NUM_PRIMES]
+    model = costmodel.CostModel(seed=0)
+    model.load_state(dict(np.load(COSTMODEL_FILE)))
+    rows, err, exact = [], [], []
+    t0 = time.perf_counter()
+    for i, (inst, cs) in enumerate(zip(held, cands)):
+        d = inst.clause_diagram()
+        cons = [GpuContraction(CudaRel, d.wiring, tree=t, sliced=sl) for t, sl in cs]
+        graphs = [costmodel.tree_graph(c, min(group, c.num_slices), primes) for c in cons]
+        pred = model.predict(costmodel.make_batch(graphs, model.device))
+        cost_pred = [math.exp(p) * c.num_slices for p, c in zip(pred, cons)]
+        j = int(np.argmin(cost_pred))
+        ms = {k: costmodel.measure(cons[k], d, primes, group, passes=1) for k in {0, j}}
+        err += [abs(pred[k] - math.log(v)) for k, v in ms.items()]
+        plain, learned = ms[0] * cons[0].num_slices, ms[j] * cons[j].num_slices
+        rows.append((plain, learned, j, cons[j], d))
+    # the picked trees of the two instances with the shortest learned runs count exactly
+    for i in sorted(range(len(rows)), key=lambda i: rows[i][1])[:2]:
+        _, _, _, c, d = rows[i]
+        got = c.count(d, ring="modp", num_primes=NUM_PRIMES)
+        exact.append({"instance": 10_000 + i, "count": int(got), "dpll": int(dpll_held[i]),
+                      "equal": int(got) == int(dpll_held[i])})
+    rows = [r[:3] for r in rows]
+    return {
+        "metric": "device ms per instance, learned tree vs planner tree (3-SAT n=60 m=256)",
+        "instances": len(held), "candidates_per_instance": [len(cs) for cs in cands],
+        "learned_over_plain": float(np.mean([p / q for p, q, _ in rows])),
+        "learned_over_plain_total": float(sum(p for p, _, _ in rows) / sum(q for _, q, _ in rows)),
+        "picked_planner_tree": sum(1 for *_, j in rows if j == 0),
+        "plain_ms_per_instance": [round(p, 1) for p, _, _ in rows],
+        "learned_ms_per_instance": [round(q, 1) for _, q, _ in rows],
+        "abs_log_error_measured_picks": float(np.mean(err)),
+        "picked_trees_exact": exact, "target_ratio": 1.5,
+        "meets_target": bool(sum(p for p, _, _ in rows) >= 1.5 * sum(q for _, q, _ in rows)),
+        "seconds": round(time.perf_counter() - t0, 1),
+        "form": "committed cost model (plans/costmodel_n60.npz) ranks the planner's candidate "
+                "trees per held-out instance (seeds 10000 on); device time per instance = "
+                f"measured ms per slice (tsg_plan_run_timed, {group} slices, 3-prime count + "
+                "OR-AND) x slices",
+    }
 
 
 def run_costmodel(args) -> None:
@@ -886,7 +1038,7 @@ def run_costmodel(args) -> None:
         n = int(g.integers(24, 57))
         m = round(float(g.uniform(3.8, 4.6)) * n)
         train.append(CNFInstance.random(3, n, m, rng=1000 + i))
-    held = [CNFInstance.random(3, N_VARS, N_CLAUSES, rng=10_000 + j) for j in range(args.cm_heldout)]
+    held = costmodel_heldout(args.cm_heldout)
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
     with cpu_pool(cores) as pool:
@@ -898,28 +1050,12 @@ def run_costmodel(args) -> None:
     import torch
 
     from tensorsat_gb300 import costmodel
-    from tensorsat_gb300.contractions.gpu import PRIMES_31, GpuContraction
-    from tensorsat_gb300.lang.cuda_rel import CudaRel
 
     torch.cuda.set_device(0)
-    primes = PRIMES_31[:NUM_PRIMES]
     group = 16
-
-    def measured(instances, cands):
-        rows = []
-        for inst, cs in zip(instances, cands):
-            d = inst.clause_diagram()
-            per = []
-            for tree, sl in cs:
-                c = GpuContraction(CudaRel, d.wiring, tree=tree, sliced=sl)
-                ms = costmodel.measure(c, d, primes, group, passes=1)
-                per.append((c, costmodel.tree_graph(c, min(group, c.num_slices), primes), ms))
-            rows.append(per)
-        return rows
-
     t0 = time.perf_counter()
-    rows_train = measured(train, cand_train)
-    rows_held = measured(held, cand_held)
+    rows_train = costmodel_measure(train, cand_train, group)
+    rows_held = costmodel_measure(held, cand_held, group)
     measure_s = time.perf_counter() - t0
     graphs = [gph for per in rows_train for _, gph, _ in per]
     y = [math.log(ms) for per in rows_train for _, _, ms in per]
@@ -927,49 +1063,84 @@ def run_costmodel(args) -> None:
     t0 = time.perf_counter()
     hist = model.fit(graphs, y, epochs=args.cm_epochs, batch_trees=64, lr=2e-3)
     train_s = time.perf_counter() - t0
-    # held-out: per-tree prediction error, per-instance choice
-    hg = [gph for per in rows_held for _, gph, _ in per]
-    hy = np.asarray([math.log(ms) for per in rows_held for _, _, ms in per])
-    pred = np.concatenate([model.predict(costmodel.make_batch(hg[i: i + 64], model.device))
-                           for i in range(0, len(hg), 64)])
-    err = np.abs(pred - hy)
-    picks = []
-    k = 0
-    for per in rows_held:
-        cost_pred = [math.exp(pred[k + j]) * per[j][0].num_slices for j in range(len(per))]
-        cost_meas = [per[j][2] * per[j][0].num_slices for j in range(len(per))]
-        k += len(per)
-        best = min(cost_meas)
-        picks.append((cost_meas[int(np.argmin(cost_pred))] / best, cost_meas[0] / best))
-    # the picked trees' answers are the DPLL counts (any tree gives the same answer)
-    exact = []
-    k = 0
-    for inst, per, want in zip(held[:4], rows_held[:4], dpll_held):
-        cost_pred = [math.exp(pred[k + j]) * per[j][0].num_slices for j in range(len(per))]
-        k += len(per)
-        c = per[int(np.argmin(cost_pred))][0]
-        exact.append(int(c.count(inst.clause_diagram(), ring="modp", num_primes=NUM_PRIMES))
-                     == want)
-    out_path = args.cm_out
-    if out_path:
-        np.savez(out_path, **model.state())
+    ev = costmodel_evaluate(model, held, rows_held, dpll_held, 4)
+    if args.cm_out:
+        np.savez(args.cm_out, **model.state())
     line = {
         "metric": "learned cost model: |log predicted - log measured| device time per slice, "
                   "held-out 3-SAT n=60 m=256 trees",
-        "value": float(err.mean()), "unit": "mean abs log error", "higher_is_better": False,
-        "median_abs_log_error": float(np.median(err)),
-        "within_20pct": float(np.mean(err < math.log(1.2))),
-        "train_trees": len(graphs), "heldout_instances": len(held), "heldout_trees": len(hg),
-        "model_pick_over_best": float(np.mean([a for a, _ in picks])),
-        "planner_pick_over_best": float(np.mean([b for _, b in picks])),
-        "model_pick_beats_planner": float(np.mean([a < b for a, b in picks])),
-        "picked_trees_exact": exact,
+        "value": ev["mean_abs_log_error"], "unit": "mean abs log error",
+        "higher_is_better": False, **ev, "train_trees": len(graphs),
         "loss_first_last": [hist[0], hist[-1]],
         "seconds": {"planning": round(plan_s, 1), "measuring": round(measure_s, 1),
                     "training": round(train_s, 1)},
         "config": {"hidden": costmodel.HIDDEN, "layers": costmodel.LAYERS, "epochs": args.cm_epochs,
                    "dtype": "bf16 weights/activations, fp32 accumulation (tcgen05 kind::f16)",
                    "measure": f"tsg_plan_run_timed, {group} slices, 3-prime count + OR-AND"},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_costmodel_gemm(args) -> None:
+    """Times the cost model's tensor-core layer GEMM (node rows x 128 weights, K = 128,
+    bias + ReLU, BF16 out) at 2^19 node rows (operands and result larger than L2), and
+    the same product through cuBLAS (torch.nn.functional.linear) for comparison."""
+    import torch
+
+    from tensorsat_gb300 import _device, _native
+
+    lib = _native.lib()
+    torch.cuda.set_device(0)
+    m, n, k = 1 << 19, 128, 128
+    g = torch.Generator(device="cuda").manual_seed(0)
+    a = torch.randn(m, k, device="cuda", generator=g).to(torch.bfloat16)
+    w = torch.randn(n, k, device="cuda", generator=g).to(torch.bfloat16)
+    bias = torch.randn(n, device="cuda", generator=g)
+    out = torch.empty(m, n, device="cuda", dtype=torch.bfloat16)
+    stream = _device.stream_handle()
+
+    def ours():
+        _native.check(lib.tsg_cm_gemm_bf16(m, n, k, a.data_ptr(), w.data_ptr(), bias.data_ptr(),
+                                           1, out.data_ptr(), n, 0, stream))
+
+    bias16 = bias.to(torch.bfloat16)
+
+    def cublas():
+        torch.relu(torch.nn.functional.linear(a, w, bias16))
+
+    def timed(fn, steps):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    steps = max(args.steps, 20)
+    ms = timed(ours, steps)
+    _native.check(lib.tsg_cm_take_error(stream))
+    want = torch.relu(a.float() @ w.float().T + bias)
+    err = float((out.float() - want).abs().max() / want.abs().max())
+    ms_cublas = timed(cublas, steps)
+    flops = 2.0 * m * n * k
+    nbytes = 2.0 * (m * k + n * k + m * n) + 4 * n
+    peak, kind = measured_peaks()
+    line = {
+        "metric": "cost-model layer GEMM (tcgen05.mma kind::f16, TMEM accumulator, bias+ReLU "
+                  "epilogue), node rows x 128 x 128",
+        "value": nbytes / ms / 1e6, "unit": "GB/s", "higher_is_better": True,
+        "ms_per_launch": ms, "steps": steps, "warmup": max(3, args.warmup),
+        "tflops": flops / ms / 1e9, "cublas_ms_per_launch": ms_cublas,
+        "over_cublas": ms_cublas / ms, "max_rel_error_vs_fp32": err,
+        "roofline": {"bound": "hbm", "achieved": nbytes / ms / 1e6, "peak": peak,
+                     "unit": "GB/s", "frac": nbytes / ms / 1e6 / peak, "peak_source": kind,
+                     "algorithmic_bytes": nbytes},
+        "config": {"workload": f"{m} x {n} x {k} BF16, FP32 accumulation, BF16 out",
+                   "l2": "operands and result larger than L2"},
     }
     print(json.dumps(line), flush=True)
 
@@ -982,6 +1153,8 @@ def main() -> None:
         run_ragged(args)
     elif args.workload == "costmodel":
         run_costmodel(args)
+    elif args.workload == "costmodel-gemm":
+        run_costmodel_gemm(args)
     else:
         run_gb300(args)
 

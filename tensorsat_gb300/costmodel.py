@@ -305,15 +305,30 @@ CANDIDATE_SETTINGS = [
 ]
 
 
-def candidate_trees(wiring: Any, count: int, target_bits: int = 26) -> list[tuple[Any, tuple]]:
+def candidate_settings(count: int) -> list[tuple[int, int, int, int]]:
+    """``count`` planner settings: the fixed list above, then single randomised orders with
+    seeds 8, 9, ... cycling through slicing caps 26/25/24 and reconfiguration sizes 10/6/0."""
+    out = list(CANDIDATE_SETTINGS[:count])
+    seed = len(CANDIDATE_SETTINGS)
+    while len(out) < count:
+        out.append(((26, 25, 24)[seed % 3], 1, (10, 6, 0)[(seed // 3) % 3], seed))
+        seed += 1
+    return out
+
+
+def candidate_trees(wiring: Any, count: int, target_bits: int = 26,
+                    settings: Sequence[tuple[int, int, int, int]] | None = None
+                    ) -> list[tuple[Any, tuple]]:
     """Up to ``count`` distinct (tree, sliced wires) of the planner for ``wiring``, from
     varied settings (randomised elimination orders, with and without subtree
-    reconfiguration, tighter slicing caps); the first is the planner's usual choice."""
+    reconfiguration, tighter slicing caps); the first is the planner's usual choice.
+    ``settings`` replaces :func:`candidate_settings` (a share of them, for parallel
+    workers whose lists are merged with :func:`distinct`)."""
     from .contractions.gpu import _network, _prepare
 
     net = _network(_prepare(wiring))
     out, seen = [], set()
-    for tb, trials, reconf, seed in CANDIDATE_SETTINGS:
+    for tb, trials, reconf, seed in (candidate_settings(count) if settings is None else settings):
         if len(out) >= count:
             break
         tree, sl = planner.optimize(net, target_bits=min(tb, target_bits), trials=trials,
@@ -323,6 +338,17 @@ def candidate_trees(wiring: Any, count: int, target_bits: int = 26) -> list[tupl
             continue
         seen.add(key)
         out.append((tree, tuple(sorted(sl))))
+    return out
+
+
+def distinct(trees: Sequence[tuple[Any, tuple]]) -> list[tuple[Any, tuple]]:
+    """The (tree, sliced wires) pairs without repeats, in their first order."""
+    out, seen = [], set()
+    for tree, sl in trees:
+        key = (tuple(tree.steps), tuple(sorted(sl)))
+        if key not in seen:
+            seen.add(key)
+            out.append((tree, sl))
     return out
 
 

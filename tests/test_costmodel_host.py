@@ -39,3 +39,19 @@ def test_candidates_graphs_and_batches():
         for e in range(cstart[v], cstart[v + 1]):
             assert parent[child[e]] == v
     assert int((parent >= 0).sum()) == cstart[-1] == sum(2 * (len(g["x"]) - 1) // 2 for g in graphs)
+
+
+def test_candidate_settings_split_and_merge():
+    """64 settings (the fixed list first), split over workers and merged back without
+    repeats: the merged list is the single-worker list, planner's choice first."""
+    st = costmodel.candidate_settings(64)
+    assert len(st) == 64 and st[:len(costmodel.CANDIDATE_SETTINGS)] == costmodel.CANDIDATE_SETTINGS
+    assert len({s[3] for s in st}) == 64
+    w = CNFInstance.random(3, 20, 85, rng=5).clause_diagram().wiring
+    whole = costmodel.candidate_trees(w, 12)
+    parts = [costmodel.candidate_trees(w, 12, settings=costmodel.candidate_settings(12)[p::3])
+             for p in range(3)]
+    merged = costmodel.distinct([x[k] for k in range(4) for x in parts if k < len(x)])
+    key = lambda ts: [(tuple(t.steps), s) for t, s in ts]
+    assert key(merged)[0] == key(whole)[0]
+    assert sorted(key(merged)) == sorted(key(whole))
