@@ -537,8 +537,14 @@ def run_gb300(args) -> None:
             "metric": RAGGED_METRIC, "value": r["value"], "unit": UNIT,
             "workload": ragged_workload_text(len(instances), lo, hi),
             "form": f"captured CUDA graphs ({r['graphs']}: one per {RAGGED_CHUNK}-instance "
-                    f"chunk and ring, {RAGGED_LANES} concurrent lanes) replayed, inputs resident",
+                    f"chunk and ring, {RAGGED_LANES} concurrent lanes, small steps of a tree "
+                    "level packed across instances) replayed, inputs resident",
             "steps": args.batched_steps, "ms_per_step": statistics.mean(r["step_ms"]),
+            "unpacked": {"value": r["unpacked_value"], "unit": UNIT,
+                         "gpu_launches_per_pass": r["unpacked_launches"],
+                         "ms_per_step": statistics.mean(r["unpacked_step_ms"]),
+                         "form": "the same graphs with one launch per tree step "
+                                 "(tsg_batch_run_lanes)"},
             "plain": {"value": r["plain_value"], "unit": UNIT, "instances": len(instances),
                       "form": "GpuContraction.count + contract per instance, host leaves "
                               "uploaded and results read back by every call"},
@@ -709,32 +715,53 @@ def ragged_measure(instances, trees, expected, steps: int, warmup: int, e2e_step
     # sized to a fixed budget, shared by the lanes
     budget = 16 << 30
     plans = []
+    need = 0
     for b in chunks:
         for ring, pr in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ())):
             groups = b.groups(ring, max(1, len(pr)), budget)
-            plans.append((b, ring, pr, groups, b.workspace_bytes(ring, max(1, len(pr)), groups)))
-    ws = torch.empty(max(p[4] for p in plans), dtype=torch.uint8, device=dev)
-    graphs = [b.capture(ring, pr, groups, workspace=ws) for b, ring, pr, groups, _ in plans]
-    torch.cuda.synchronize()
+            plans.append((b, ring, pr, groups))
+            for packed in (True, False):
+                b.packed = packed
+                need = max(need, b.workspace_bytes(ring, max(1, len(pr)), groups))
+            b.packed = True
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def step():
-        for g in graphs:
-            g.replay()
-
-    for _ in range(warmup):
-        step()
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    with ClockSampler(device_index) as clocks:
-        ev[0].record(stream)
-        for k in range(steps):
-            step()
-            ev[k + 1].record(stream)
+    def timed_graphs(packed: bool):
+        """Captures one graph per chunk and ring (packed or one launch per step) and
+        times `steps` passes over all of them after `warmup` passes."""
+        for b in chunks:
+            b.packed = packed
+        graphs = [b.capture(ring, pr, groups, workspace=ws) for b, ring, pr, groups in plans]
+        for b in chunks:
+            b.packed = True
         torch.cuda.synchronize()
-    step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+        for _ in range(warmup):
+            for g in graphs:
+                g.replay()
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        with ClockSampler(device_index) as clocks:
+            ev[0].record(stream)
+            for k in range(steps):
+                for g in graphs:
+                    g.replay()
+                ev[k + 1].record(stream)
+            torch.cuda.synchronize()
+        GpuContraction.check_device()
+        step_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+        return graphs, step_ms, clocks
+
+    graphs_u, step_ms_u, _ = timed_graphs(False)
+    results_u = [r.cpu() for g in graphs_u for r in g.results]
+    launches_u = sum(g.launches for g in graphs_u)
+    del graphs_u
+    graphs, step_ms, clocks = timed_graphs(True)
+    results_p = [r.cpu() for g in graphs for r in g.results]
+    if not all(torch.equal(a, b) for a, b in zip(results_p, results_u)):
+        raise RuntimeError("packed and per-step batch runs differ")
     value = len(instances) * steps / (sum(step_ms) / 1000.0)
-    GpuContraction.check_device()
+    unpacked_value = len(instances) * steps / (sum(step_ms_u) / 1000.0)
 
     # plain form: one instance per call through the public API (count + SAT bit), host
     # leaves uploaded by every call, the same instances
@@ -809,6 +836,8 @@ def ragged_measure(instances, trees, expected, steps: int, warmup: int, e2e_step
     return {
         "value": value, "step_ms": step_ms, "clocks": clocks.summary(),
         "launches": sum(g.launches for g in graphs), "graphs": len(graphs),
+        "unpacked_value": unpacked_value, "unpacked_launches": launches_u,
+        "unpacked_step_ms": step_ms_u,
         "plain_value": plain_value, "uncaptured_value": uncaptured_value,
         "e2e_value": e2e_value, "e2e_passes": len(e2e_times), "h2d": h2d,
     }
@@ -863,6 +892,9 @@ def run_ragged(args) -> None:
         "e2e_uncaptured": {"value": r["uncaptured_value"], "unit": UNIT,
                            "form": "BatchContraction.count + contract per chunk, no graph"},
         "gpu_launches": r["launches"] * args.steps,
+        "unpacked": {"value": r["unpacked_value"], "unit": UNIT,
+                     "gpu_launches_per_pass": r["unpacked_launches"],
+                     "form": "the same graphs with one launch per tree step"},
         "clocks": r["clocks"],
         "step_ms": [round(x, 3) for x in r["step_ms"]],
     }

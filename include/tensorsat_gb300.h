@@ -246,6 +246,32 @@ TSG_API tsg_status tsg_batch_run_lanes(int32_t num_instances, const tsg_plan* co
                                int32_t lanes, void* workspace_dev, int64_t workspace_bytes,
                                void* const* results_dev, void* stream);
 
+/* tsg_batch_run_lanes with the instances' small steps packed across instances: each lane's
+ * instances whose group holds all their slices are grouped into packs whose workspaces
+ * fit side by side in the lane's region (the region holds the lane's largest instance;
+ * instances are placed largest first). A pack runs level by level of its members' trees:
+ * every step of the level with at most 2^16 output entries (slots included) and 2^5 summed
+ * combinations, of every member, goes into shared launches of one packed kernel (up to
+ * 240 steps per launch, described in the launch parameters); the level's other steps
+ * follow as their own launches; each member ends with its root reduction. Such a pack
+ * uses the level-order buffer placement, whose size tsg_batch_packed_workspace_bytes
+ * includes. An instance run in several slice groups runs alone, as in tsg_batch_run.
+ * Results equal tsg_batch_run's. Checks every launch of every pack before the first,
+ * neither allocates nor synchronises, and can be captured into a CUDA graph.
+ * *launches_out (if not null) receives the number of kernel launches issued. No
+ * counterpart in the reference (one instance per call, one einsum per tree node:
+ * tensorsat/contractions/abc.py:92, tensorsat/_autoray.py:31-62). */
+TSG_API tsg_status tsg_batch_packed_workspace_bytes(int32_t num_instances,
+                                            const tsg_plan* const* plans, int32_t ring,
+                                            int32_t num_primes, const int64_t* group_sizes,
+                                            int32_t lanes, int64_t* bytes_out);
+TSG_API tsg_status tsg_batch_run_packed(int32_t num_instances, const tsg_plan* const* plans,
+                                int32_t ring, int32_t num_primes, const uint32_t* primes,
+                                const uint8_t* const* leaf_pools, const int64_t* group_sizes,
+                                int32_t lanes, void* workspace_dev, int64_t workspace_bytes,
+                                void* const* results_dev, void* stream,
+                                int64_t* launches_out);
+
 /* Leaf variants of one plan in one run: num_variants (a power of two) copies of the leaf
  * pool lie pool_stride bytes apart (a power of two, at least the plan's pool extent and
  * 16); every tree step is launched once per slice group for all variants together (the

@@ -71,6 +71,8 @@ EXPORTED_SYMBOLS = (
     "tsg_fusion_enabled",
     "tsg_batch_lanes_workspace_bytes",
     "tsg_batch_run_lanes",
+    "tsg_batch_packed_workspace_bytes",
+    "tsg_batch_run_packed",
     "tsg_plan_set_step_options",
     "tsg_plan_variants_workspace_bytes",
     "tsg_plan_run_variants",
@@ -170,6 +172,13 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_batch_run_lanes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
                                         POINTER(c_uint32), POINTER(c_void_p), _i64p, c_int32,
                                         c_void_p, c_int64, POINTER(c_void_p), c_void_p]
+    lib.tsg_batch_packed_workspace_bytes.restype = c_int32
+    lib.tsg_batch_packed_workspace_bytes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
+                                                     _i64p, c_int32, _i64p]
+    lib.tsg_batch_run_packed.restype = c_int32
+    lib.tsg_batch_run_packed.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
+                                         POINTER(c_uint32), POINTER(c_void_p), _i64p, c_int32,
+                                         c_void_p, c_int64, POINTER(c_void_p), c_void_p, _i64p]
     lib.tsg_plan_variants_workspace_bytes.restype = c_int32
     lib.tsg_plan_variants_workspace_bytes.argtypes = [c_void_p, c_int32, c_int32, c_int64,
                                                       c_int64, _i64p]

@@ -83,18 +83,23 @@ class BatchContraction:
     def __init__(self, box_class: type[CudaRel], diagrams: Sequence[Diagram], *,
                  target_bits: int | None = 26, trials: int = 2, seed: int = 0,
                  trees: Sequence[tuple[Any, Sequence[int]]] | None = None,
-                 lanes: int = 16) -> None:
+                 lanes: int = 16, packed: bool = True) -> None:
         """``trees`` optionally gives each diagram's (tree, sliced wires), for example from
         :func:`~tensorsat_gb300.contractions.gpu.plan_tree` run in worker processes;
         otherwise every diagram is planned here with ``target_bits``, ``trials`` and
         ``seed``. ``lanes`` (1..32) is the number of concurrent lanes the batch's
         instances are spread over (``tsg_batch_run_lanes``): each lane is a stream with its
-        own workspace region, so the small launches of different instances overlap."""
+        own workspace region, so the small launches of different instances overlap.
+        ``packed`` (default) runs each lane's instances in packs, level by level of their
+        trees, with the small steps of every pack member in shared launches
+        (``tsg_batch_run_packed``); otherwise every step of every instance is its own
+        launch (``tsg_batch_run_lanes``). Both give the same answers."""
         if not diagrams:
             raise ValueError("A batch needs at least one diagram.")
         if not 1 <= lanes <= 32:
             raise ValueError("lanes must lie in 1..32")
         self.lanes = min(lanes, len(diagrams))
+        self.packed = bool(packed)
         self._diagrams = list(diagrams)
         if trees is not None and len(trees) != len(self._diagrams):
             raise ValueError(f"expected {len(self._diagrams)} trees, got {len(trees)}")
@@ -108,6 +113,7 @@ class BatchContraction:
             c.validate(d)
         self._pools: list[torch.Tensor] | None = None
         self._graphs: dict[tuple, BatchGraph] = {}
+        self.last_launches = 0  # kernel launches of the last run (or capture)
         self._staging: torch.Tensor | None = None    # pinned host copy of the leaf pools
         self._staged: torch.cuda.Event | None = None  # the staging buffer's last copies
 
@@ -176,9 +182,10 @@ class BatchContraction:
         lib = _native.lib()
         handles = _ptr_array([c.native_plan().handle.value for c in self._contractions])
         out = ctypes.c_int64()
-        _native.check(lib.tsg_batch_lanes_workspace_bytes(
-            len(self), handles, ring, planes, _native.i64_array(list(groups)), self.lanes,
-            ctypes.byref(out)))
+        fn = lib.tsg_batch_packed_workspace_bytes if self.packed else \
+            lib.tsg_batch_lanes_workspace_bytes
+        _native.check(fn(len(self), handles, ring, planes, _native.i64_array(list(groups)),
+                         self.lanes, ctypes.byref(out)))
         return int(out.value)
 
     def _results(self, ring: int, planes: int) -> list[torch.Tensor]:
@@ -211,9 +218,20 @@ class BatchContraction:
             _native.i64_array(list(groups)),
             _ptr_array([r.data_ptr() for r in results]),
         ]
-        st = lib.tsg_batch_run_lanes(len(self), args[0], ring, len(primes), args[1], args[2],
-                                     args[3], self.lanes, workspace.data_ptr(),
-                                     workspace.numel(), args[4], stream)
+        if self.packed:
+            launches = ctypes.c_int64()
+            st = lib.tsg_batch_run_packed(len(self), args[0], ring, len(primes), args[1],
+                                          args[2], args[3], self.lanes, workspace.data_ptr(),
+                                          workspace.numel(), args[4], stream,
+                                          ctypes.byref(launches))
+            self.last_launches = int(launches.value)
+        else:
+            st = lib.tsg_batch_run_lanes(len(self), args[0], ring, len(primes), args[1],
+                                         args[2], args[3], self.lanes, workspace.data_ptr(),
+                                         workspace.numel(), args[4], stream)
+            self.last_launches = sum(
+                c.native_plan().launch_count(0, c.num_slices, g, ring, max(1, len(primes)))
+                for c, g in zip(self._contractions, groups))
         _native.check(st)
         return args
 
@@ -257,9 +275,7 @@ class BatchContraction:
         with torch.cuda.graph(graph):
             args = self._call(ring, primes, groups, ws, results,
                               torch.cuda.current_stream(dev).cuda_stream)
-        launches = sum(c.native_plan().launch_count(0, c.num_slices, g, ring, max(1, planes))
-                       for c, g in zip(self._contractions, groups))
-        return BatchGraph(graph, results, list(groups), launches,
+        return BatchGraph(graph, results, list(groups), self.last_launches,
                           [ws, self.pools(), args, list(primes)])
 
     def _replay(self, ring: int, primes: Sequence[int], groups: Sequence[int] | None,

@@ -21,8 +21,10 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <deque>
 #include <type_traits>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -84,6 +86,8 @@ struct Layout {
   int planes;
   bool fusion;                  // fused steps enabled when the layout was made
   bool all_dep;                 // every step per slot (leaf variants: no shared prologue)
+  bool levels;                  // buffers placed for level-order execution (packed runs)
+  std::vector<int> level;       // tree level of each step (1 + its operands' highest)
   std::vector<int64_t> offset;  // byte offset of each step's output in the workspace
                                 // (-1: computed inside its consumer, never stored)
   std::vector<int64_t> plane;   // plane stride (elements) of each step's output
@@ -160,7 +164,9 @@ struct tsg_plan {
   int num_sliced = 0;
   int root_bits = 0;
   int64_t max_entry_bits = 0;
-  std::vector<tsg::Layout> layouts;  // cache keyed by (group, elem_bytes, planes, fusion)
+  // cache keyed by (group, elem_bytes, planes, fusion, all_dep, levels); a deque keeps the
+  // addresses of cached layouts valid while new ones are added
+  std::deque<tsg::Layout> layouts;
   // per-step kernel options of each ring (TSG_STEP_*; tsg_plan_set_step_options), indexed
   // by ring; empty = none set
   std::vector<int32_t> options[3];
@@ -284,12 +290,16 @@ std::vector<int> choose_fusion(const tsg_plan* plan, int64_t group, int64_t elem
   return fused_from;
 }
 
+// Buffer placement of a plan for one slice group, element type and plane count. Steps
+// run in step order (prologue of slice-independent steps, then each group), or, for
+// `levels` (packed runs, one group holding every slice), level by level: all steps of a
+// level may run at once, so a level's outputs are placed before its operands are freed.
 tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int planes,
-                      const Layout** out, bool all_dep = false) {
+                      const Layout** out, bool all_dep = false, bool levels = false) {
   const bool fusion = g_fusion.load(std::memory_order_relaxed) != 0;
   for (const Layout& l : plan->layouts) {
     if (l.group == group && l.elem_bytes == elem_bytes && l.planes == planes &&
-        l.fusion == fusion && l.all_dep == all_dep) {
+        l.fusion == fusion && l.all_dep == all_dep && l.levels == levels) {
       *out = &l;
       return TSG_OK;
     }
@@ -302,7 +312,17 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
   lay.planes = planes;
   lay.fusion = fusion;
   lay.all_dep = all_dep;
+  lay.levels = levels;
   auto dep = [&](int x) { return all_dep || steps[x].dep; };
+  lay.level.assign(ns, 1);
+  int max_level = 0;
+  for (int s = 0; s < ns; ++s) {
+    int l = 0;
+    for (int o = 0; o < 2; ++o)
+      if (steps[s].op[o] < 0) l = std::max(l, lay.level[-steps[s].op[o] - 1]);
+    lay.level[s] = l + 1;
+    max_level = std::max(max_level, l + 1);
+  }
   lay.offset.assign(ns, -1);
   lay.plane.assign(ns, 0);
   lay.fused_from = fusion ? choose_fusion(plan, group, elem_bytes) : std::vector<int>(ns, -1);
@@ -334,13 +354,35 @@ tsg_status get_layout(tsg_plan* plan, int64_t group, int64_t elem_bytes, int pla
       arena.release(lay.offset[x], bytes[x]);
     }
   };
-  for (int phase = 0; phase < 2; ++phase) {
-    for (int s = 0; s < ns; ++s) {
-      if (dep(s) != (phase == 1) || lay.fused_away[s]) continue;
-      lay.offset[s] = arena.alloc(bytes[s]);
-      arena.note();
-      release_operands(s, s);
-      if (lay.fused_from[s] >= 0) release_operands(s, lay.fused_from[s]);
+  if (levels) {
+    // one group: every operand is read once, by the level after its own or later
+    auto release_all = [&](int r) {
+      for (int o = 0; o < 2; ++o) {
+        const int v = steps[r].op[o];
+        if (v < 0 && !lay.fused_away[-v - 1]) arena.release(lay.offset[-v - 1], bytes[-v - 1]);
+      }
+    };
+    for (int l = 1; l <= max_level; ++l) {
+      for (int s = 0; s < ns; ++s) {
+        if (lay.level[s] != l || lay.fused_away[s]) continue;
+        lay.offset[s] = arena.alloc(bytes[s]);
+        arena.note();
+      }
+      for (int s = 0; s < ns; ++s) {
+        if (lay.level[s] != l || lay.fused_away[s]) continue;
+        release_all(s);
+        if (lay.fused_from[s] >= 0) release_all(lay.fused_from[s]);
+      }
+    }
+  } else {
+    for (int phase = 0; phase < 2; ++phase) {
+      for (int s = 0; s < ns; ++s) {
+        if (dep(s) != (phase == 1) || lay.fused_away[s]) continue;
+        lay.offset[s] = arena.alloc(bytes[s]);
+        arena.note();
+        release_operands(s, s);
+        if (lay.fused_from[s] >= 0) release_operands(s, lay.fused_from[s]);
+      }
     }
   }
   lay.bytes = std::max<int64_t>(arena.peak(), 256);
@@ -1285,6 +1327,28 @@ void describe_launch(const LaunchArgs& la, int ring, int32_t* out) {
 // followed by an event record.
 // Leaf variants of one plan contracted together (tsg_plan_run_variants): `count` (a power
 // of two) copies of the leaf pool, 2^stride_bits bytes apart; results `result_bytes` apart.
+// Ring constants of a run: for MODP the moduli with their Barrett and Montgomery constants.
+tsg_status make_ring_args(int32_t ring, int32_t num_primes, const uint32_t* primes,
+                          RingArgs* out) {
+  RingArgs& ra = *out;
+  std::memset(&ra, 0, sizeof(ra));
+  if (ring != TSG_RING_MODP) return TSG_OK;
+  if (!primes) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: MODP needs primes");
+  ra.np = num_primes;
+  for (int p = 0; p < num_primes; ++p) {
+    if (primes[p] <= (1u << 31) - (1u << 26) || primes[p] >= (1u << 31) || (primes[p] % 2) == 0)
+      return fail(TSG_ERR_INVALID_ARGUMENT,
+                  "plan_run: moduli must be odd and in (2^31 - 2^26, 2^31)");
+    ra.p[p] = primes[p];
+    ra.m[p] = UINT64_MAX / primes[p];
+    uint32_t inv = primes[p];  // Newton iteration for p^-1 mod 2^32 (5 steps: 2^32 bits)
+    for (int it = 0; it < 5; ++it) inv *= 2u - primes[p] * inv;
+    ra.pinv[p] = 0u - inv;
+    ra.r1[p] = (uint32_t)((1ull << 32) % primes[p]);
+  }
+  return TSG_OK;
+}
+
 struct VariantSpec {
   int64_t count;
   int stride_bits;
@@ -1302,22 +1366,7 @@ tsg_status run_impl(const tsg_plan* plan, int32_t ring, int32_t num_primes,
   int planes;
   TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
   RingArgs ra;
-  std::memset(&ra, 0, sizeof(ra));
-  if (ring == TSG_RING_MODP) {
-    if (!primes) return fail(TSG_ERR_INVALID_ARGUMENT, "plan_run: MODP needs primes");
-    ra.np = num_primes;
-    for (int p = 0; p < num_primes; ++p) {
-      if (primes[p] <= (1u << 31) - (1u << 26) || primes[p] >= (1u << 31) || (primes[p] % 2) == 0)
-        return fail(TSG_ERR_INVALID_ARGUMENT,
-                    "plan_run: moduli must be odd and in (2^31 - 2^26, 2^31)");
-      ra.p[p] = primes[p];
-      ra.m[p] = UINT64_MAX / primes[p];
-      uint32_t inv = primes[p];  // Newton iteration for p^-1 mod 2^32 (5 steps: 2^32 bits)
-      for (int it = 0; it < 5; ++it) inv *= 2u - primes[p] * inv;
-      ra.pinv[p] = 0u - inv;
-      ra.r1[p] = (uint32_t)((1ull << 32) % primes[p]);
-    }
-  }
+  TSG_TRY(make_ring_args(ring, num_primes, primes, &ra));
   int v_bits = 0;
   if (vs) {
     while ((int64_t(1) << v_bits) < vs->count) v_bits++;
@@ -1497,6 +1546,207 @@ tsg_status lane_set(int lanes, LaneSet** out) {
     ls.joins.push_back(ev);
   }
   *out = &ls;
+  return TSG_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Packed batches (tsg_batch_run_packed). The instances of a lane are grouped into packs
+// whose workspaces fit side by side in the lane's region; a pack runs level by level: the
+// small steps of one tree level of every member go into shared packed launches
+// (tree_pack_kernel), the member's other steps follow as their own launches, and each
+// member ends with its root reduction. An instance whose slices need several groups runs
+// alone, step by step.
+
+// The packed form of a launch, or false when the step is not small (more than
+// 2^kPackTBits entries or 2^kPackKBits summed combinations) or runs on the streaming or
+// fused kernel.
+bool pack_item(const LaunchArgs& la, PackItem* it) {
+  const StepArgs& a = la.a;
+  if (la.streamed || la.fused) return false;
+  if (a.total == 0 || (a.total & (a.total - 1)) != 0) return false;
+  const int tb = bit_width(a.total - 1);
+  if (tb > kPackTBits || a.k_bits < 0 || a.k_bits > kPackKBits) return false;
+  std::memset(it, 0, sizeof(*it));
+  for (int o = 0; o < 2; ++o) {
+    PackOperand& op = it->op[o];
+    const BitMap& tm = o == 0 ? a.lt : a.rt;
+    const BitMap& km = o == 0 ? a.lk : a.rk;
+    std::memset(op.tdst, kPackNone, sizeof(op.tdst));
+    std::memset(op.kdst, kPackNone, sizeof(op.kdst));
+    for (int r = 0; r < tm.n; ++r)
+      for (int b = 0; b < tm.len[r]; ++b) {
+        if (tm.src[r] + b >= tb) return false;
+        op.tdst[tm.src[r] + b] = (uint8_t)(tm.dst[r] + b);
+      }
+    for (int r = 0; r < km.n; ++r)
+      for (int b = 0; b < km.len[r]; ++b) {
+        if (km.src[r] + b >= a.k_bits) return false;
+        op.kdst[km.src[r] + b] = (uint8_t)(km.dst[r] + b);
+      }
+    op.ptr = o == 0 ? a.lhs : a.rhs;
+    op.base = o == 0 ? a.l_base : a.r_base;
+    op.plane = o == 0 ? a.l_plane : a.r_plane;
+  }
+  it->out = a.out;
+  it->o_plane = a.o_plane;
+  it->t_bits = (uint8_t)tb;
+  it->k_bits = (uint8_t)a.k_bits;
+  it->leaves = (uint8_t)((la.is_leaf[0] ? 1 : 0) | (la.is_leaf[1] ? 2 : 0));
+  return true;
+}
+
+struct PackMember {
+  const tsg_plan* plan;
+  const uint8_t* pool;
+  uint8_t* ws;
+  void* result;
+  int64_t group;  // every slice of the instance
+};
+
+// Runs one pack (dry: builds and checks every launch, issues none) and adds its launch
+// count to *launches.
+tsg_status run_pack(const std::vector<PackMember>& mem, int32_t ring, const RingArgs& ra,
+                    int64_t eb, int planes, cudaStream_t stream, bool dry, int64_t* launches) {
+  const int n = (int)mem.size();
+  std::vector<RunCtx> ctx(n);
+  int max_level = 0;
+  for (int i = 0; i < n; ++i) {
+    const Layout* lay;
+    TSG_TRY(get_layout(const_cast<tsg_plan*>(mem[i].plan), mem[i].group, eb, planes, &lay,
+                       /*all_dep=*/false, /*levels=*/true));
+    RunCtx& c = ctx[i];
+    c.plan = mem[i].plan;
+    c.lay = lay;
+    c.ring = ring;
+    c.ra = ra;
+    c.pool = mem[i].pool;
+    c.ws = mem[i].ws;
+    c.stream = stream;
+    c.g_bits = 0;
+    while ((int64_t(1) << c.g_bits) < mem[i].group) c.g_bits++;
+    for (int l : lay->level) max_level = std::max(max_level, l);
+  }
+  std::unique_ptr<PackArgs> pa(new PackArgs);
+  pa->n_items = 0;
+  pa->n_warps = 0;
+  int64_t count = 0;
+  auto flush = [&]() -> tsg_status {
+    if (pa->n_items == 0) return TSG_OK;
+    if (!dry) TSG_TRY(launch_pack(ring, *pa, ra, stream));
+    count++;
+    pa->n_items = 0;
+    pa->n_warps = 0;
+    return TSG_OK;
+  };
+  std::vector<std::pair<int, int>> singles;
+  for (int l = 1; l <= max_level; ++l) {
+    singles.clear();
+    for (int i = 0; i < n; ++i) {
+      const RunCtx& c = ctx[i];
+      const int ns = (int)c.plan->steps.size();
+      for (int s = 0; s < ns; ++s) {
+        if (c.lay->level[s] != l || c.lay->fused_away[s]) continue;
+        LaunchArgs la;
+        TSG_TRY(build_step(c, s, 0, mem[i].group, &la));
+        PackItem& it = pa->items[pa->n_items];
+        if (!pack_item(la, &it)) {
+          singles.push_back({i, s});
+          continue;
+        }
+        it.warp0 = pa->n_warps;
+        pa->n_warps += (uint32_t)((la.a.total + 31) / 32);
+        if (++pa->n_items == kPackItems) TSG_TRY(flush());
+      }
+    }
+    TSG_TRY(flush());
+    for (const auto& is : singles) {
+      if (!dry) TSG_TRY(launch_step(ctx[is.first], is.second, 0, mem[is.first].group));
+      count++;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    const int64_t cnt = ctx[i].plan->steps.back().dep ? mem[i].group : 1;
+    if (!dry) TSG_TRY(launch_reduce(ctx[i], cnt, (uint8_t*)mem[i].result, 0));
+    count++;
+  }
+  if (launches) *launches += count;
+  return TSG_OK;
+}
+
+// Lanes, packs and workspace regions of a packed batch.
+struct PackSchedule {
+  int used = 1;
+  std::vector<int> lane;                              // lane of every instance
+  std::vector<std::vector<std::vector<int>>> packs;  // per lane, its packs in run order
+  std::vector<char> packed;        // the instance runs in a pack (one group of all slices)
+  std::vector<int64_t> inst_off;   // workspace offset of the instance in its lane's region
+  std::vector<int64_t> inst_bytes;
+  std::vector<int64_t> lane_off, lane_bytes;
+  int64_t total = 0;
+};
+
+// Lanes by estimated cost (assign_lanes); each lane's region holds its largest instance;
+// the lane's instances, largest workspace first, fill packs first-fit within the region.
+tsg_status plan_packs(int32_t n, const tsg_plan* const* plans, int32_t ring,
+                      int32_t num_primes, const int64_t* group_sizes, int lanes,
+                      PackSchedule* ps) {
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  ps->used = std::max(1, std::min<int>(lanes, n));
+  ps->lane = assign_lanes(n, plans, ps->used);
+  ps->packed.assign(n, 0);
+  ps->inst_off.assign(n, 0);
+  ps->inst_bytes.assign(n, 0);
+  for (int i = 0; i < n; ++i) {
+    const int64_t ns = int64_t(1) << plans[i]->num_sliced;
+    TSG_TRY(check_range(plans[i], 0, ns, group_sizes[i]));
+    if (group_sizes[i] == ns) {
+      const Layout* lay;
+      TSG_TRY(get_layout(const_cast<tsg_plan*>(plans[i]), ns, eb, planes, &lay, false, true));
+      ps->inst_bytes[i] = align256(lay->bytes);
+      ps->packed[i] = 1;
+    } else {
+      int64_t b = 0;
+      TSG_TRY(tsg_plan_workspace_bytes(plans[i], ring, num_primes, group_sizes[i], &b));
+      ps->inst_bytes[i] = align256(b);
+    }
+  }
+  ps->lane_bytes.assign(ps->used, 0);
+  for (int i = 0; i < n; ++i)
+    ps->lane_bytes[ps->lane[i]] = std::max(ps->lane_bytes[ps->lane[i]], ps->inst_bytes[i]);
+  ps->packs.assign(ps->used, {});
+  for (int l = 0; l < ps->used; ++l) {
+    std::vector<int> order;
+    for (int i = 0; i < n; ++i)
+      if (ps->lane[i] == l) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return ps->inst_bytes[a] > ps->inst_bytes[b]; });
+    std::vector<int> cur;
+    int64_t used_bytes = 0;
+    for (int i : order) {
+      if (!ps->packed[i]) {
+        ps->packs[l].push_back({i});
+        continue;
+      }
+      if (!cur.empty() && used_bytes + ps->inst_bytes[i] > ps->lane_bytes[l]) {
+        ps->packs[l].push_back(cur);
+        cur.clear();
+        used_bytes = 0;
+      }
+      ps->inst_off[i] = used_bytes;
+      used_bytes += ps->inst_bytes[i];
+      cur.push_back(i);
+    }
+    if (!cur.empty()) ps->packs[l].push_back(cur);
+  }
+  ps->lane_off.assign(ps->used, 0);
+  int64_t off = 0;
+  for (int l = 0; l < ps->used; ++l) {
+    ps->lane_off[l] = off;
+    off += align256(ps->lane_bytes[l]);
+  }
+  ps->total = std::max<int64_t>(off, 256);
   return TSG_OK;
 }
 
@@ -1936,6 +2186,111 @@ tsg_status tsg_batch_run_lanes(int32_t num_instances, const tsg_plan* const* pla
     TSG_CUDA_TRY(cudaEventRecord(ls->joins[l], ls->streams[l]));
     TSG_CUDA_TRY(cudaStreamWaitEvent(origin, ls->joins[l], 0));
   }
+  return TSG_OK;
+}
+
+tsg_status tsg_batch_packed_workspace_bytes(int32_t num_instances,
+                                            const tsg_plan* const* plans, int32_t ring,
+                                            int32_t num_primes, const int64_t* group_sizes,
+                                            int32_t lanes, int64_t* bytes_out) {
+  if (num_instances < 0 || (num_instances > 0 && (!plans || !group_sizes)) || !bytes_out)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_packed_workspace_bytes: null pointer or negative count");
+  if (lanes < 1 || lanes > kMaxLanes)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_packed_workspace_bytes: lanes outside 1..32");
+  for (int32_t i = 0; i < num_instances; ++i)
+    if (!plans[i]) return fail(TSG_ERR_INVALID_ARGUMENT, "batch_packed_workspace_bytes: null plan");
+  if (num_instances == 0) {
+    *bytes_out = 256;
+    return TSG_OK;
+  }
+  PackSchedule ps;
+  TSG_TRY(plan_packs(num_instances, plans, ring, num_primes, group_sizes, lanes, &ps));
+  *bytes_out = ps.total;
+  return TSG_OK;
+}
+
+tsg_status tsg_batch_run_packed(int32_t num_instances, const tsg_plan* const* plans,
+                                int32_t ring, int32_t num_primes, const uint32_t* primes,
+                                const uint8_t* const* leaf_pools, const int64_t* group_sizes,
+                                int32_t lanes, void* workspace_dev, int64_t workspace_bytes,
+                                void* const* results_dev, void* stream, int64_t* launches_out) {
+  if (num_instances < 0 ||
+      (num_instances > 0 && (!plans || !leaf_pools || !group_sizes || !results_dev)))
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_run_packed: null pointer or negative count");
+  if (lanes < 1 || lanes > kMaxLanes)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "batch_run_packed: lanes outside 1..32");
+  if (launches_out) *launches_out = 0;
+  if (num_instances == 0) return TSG_OK;
+  for (int32_t i = 0; i < num_instances; ++i)
+    if (!plans[i] || !leaf_pools[i] || !results_dev[i])
+      return fail(TSG_ERR_INVALID_ARGUMENT,
+                  "batch_run_packed: null plan, pool or result of instance " + std::to_string(i));
+  PackSchedule ps;
+  TSG_TRY(plan_packs(num_instances, plans, ring, num_primes, group_sizes, lanes, &ps));
+  if (!workspace_dev || workspace_bytes < ps.total)
+    return fail(TSG_ERR_WORKSPACE,
+                "batch_run_packed: workspace smaller than tsg_batch_packed_workspace_bytes");
+  if (((uintptr_t)workspace_dev & 255) != 0)
+    return fail(TSG_ERR_WORKSPACE, "batch_run_packed: workspace must be 256-byte aligned");
+  int64_t eb;
+  int planes;
+  TSG_TRY(elem_info(ring, num_primes, &eb, &planes));
+  RingArgs ra;
+  TSG_TRY(make_ring_args(ring, num_primes, primes, &ra));
+  uint8_t* ws = (uint8_t*)workspace_dev;
+  // one pass that checks every launch of every pack before anything runs, one that runs
+  int64_t launches = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool dry = pass == 0;
+    LaneSet* ls = nullptr;
+    cudaStream_t origin = (cudaStream_t)stream;
+    if (!dry && ps.used > 1) {
+      TSG_TRY(lane_set(ps.used, &ls));
+      // fork: every lane waits for the work issued before this call on the caller's stream
+      TSG_CUDA_TRY(cudaEventRecord(ls->fork, origin));
+      for (int l = 0; l < ps.used; ++l)
+        TSG_CUDA_TRY(cudaStreamWaitEvent(ls->streams[l], ls->fork, 0));
+    }
+    for (int l = 0; l < ps.used; ++l) {
+      cudaStream_t st = ls ? ls->streams[l] : origin;
+      uint8_t* region = ws + ps.lane_off[l];
+      for (const std::vector<int>& pack : ps.packs[l]) {
+        const int first = pack[0];
+        if (!ps.packed[first]) {
+          const int64_t ns = int64_t(1) << plans[first]->num_sliced;
+          tsg_status sst = run_impl(plans[first], ring, num_primes, primes,
+                                    dry ? nullptr : leaf_pools[first], 0, ns, group_sizes[first],
+                                    dry ? nullptr : region, dry ? 0 : ps.lane_bytes[l],
+                                    dry ? nullptr : results_dev[first], 0, st, dry);
+          if (sst != TSG_OK)
+            return fail(sst, "batch_run_packed: instance " + std::to_string(first) + ": " +
+                                 tsg_last_error());
+          if (!dry) {
+            int64_t c = 0;
+            TSG_TRY(tsg_plan_launches(plans[first], ring, num_primes, 0, ns, group_sizes[first], &c));
+            launches += c;
+          }
+          continue;
+        }
+        std::vector<PackMember> mem;
+        for (int i : pack)
+          mem.push_back(PackMember{plans[i], leaf_pools[i], dry ? nullptr : region + ps.inst_off[i],
+                                   results_dev[i], group_sizes[i]});
+        tsg_status sst = run_pack(mem, ring, ra, eb, planes, st, dry, dry ? nullptr : &launches);
+        if (sst != TSG_OK)
+          return fail(sst, "batch_run_packed: pack of instance " + std::to_string(first) + ": " +
+                               tsg_last_error());
+      }
+    }
+    if (ls) {
+      // join: the caller's stream waits for every lane
+      for (int l = 0; l < ps.used; ++l) {
+        TSG_CUDA_TRY(cudaEventRecord(ls->joins[l], ls->streams[l]));
+        TSG_CUDA_TRY(cudaStreamWaitEvent(origin, ls->joins[l], 0));
+      }
+    }
+  }
+  if (launches_out) *launches_out = launches;
   return TSG_OK;
 }
 

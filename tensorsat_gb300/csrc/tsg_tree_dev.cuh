@@ -1511,5 +1511,136 @@ tsg_status launch_fused_or_and(const LaunchArgs& la, const RingArgs& ra, cudaStr
 tsg_status launch_stream_fused_modp(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 tsg_status launch_stream_fused_u64(const LaunchArgs& la, const RingArgs& ra, cudaStream_t st);
 
+// ------------------------------------------------------------------------------------
+// Packed steps (tsg_batch_run_packed): the small steps of one tree level, of several
+// instances at once, in one launch. A small step has at most 2^kPackTBits output entries
+// (slots included) and 2^kPackKBits summed combinations; it is described by per-bit index
+// maps instead of runs, and the whole launch's steps travel in the kernel parameters, so a
+// packed launch needs no device-side table and records into a graph like any launch.
+// One warp computes 32 consecutive entries of one step.
+
+constexpr int kPackTBits = 16;
+constexpr int kPackKBits = 5;
+constexpr int kPackItems = 240;  // steps per launch (the parameters stay under 32 KB)
+constexpr uint8_t kPackNone = 0xff;
+
+struct PackOperand {
+  const uint8_t* ptr;
+  uint64_t base;   // constant element offset
+  uint64_t plane;  // residue-plane stride (elements); unused for leaves
+  uint8_t tdst[kPackTBits];  // operand bit of output-index bit b, kPackNone if absent
+  uint8_t kdst[8];           // operand bit of summed bit b (first kPackKBits used)
+};
+
+struct PackItem {
+  PackOperand op[2];
+  uint8_t* out;
+  uint64_t o_plane;  // residue-plane stride of the output (elements)
+  uint32_t warp0;    // first warp of this step in the launch
+  uint8_t t_bits;    // log2(output entries)
+  uint8_t k_bits;
+  uint8_t leaves;    // bit 0: lhs is a leaf (uint8 0/1), bit 1: rhs
+  uint8_t pad;
+};
+
+struct PackArgs {
+  int32_t n_items;
+  uint32_t n_warps;
+  PackItem items[kPackItems];
+};
+static_assert(sizeof(PackArgs) + sizeof(RingArgs) < 32000, "packed launch parameters over 32 KB");
+
+__device__ __forceinline__ uint64_t pack_offset(const uint8_t* dst, int bits, uint64_t x) {
+  uint64_t r = 0;
+#pragma unroll 1
+  for (int b = 0; b < bits; ++b) {
+    const uint32_t d = dst[b];
+    if (d != kPackNone) r |= ((x >> b) & 1ull) << d;
+  }
+  return r;
+}
+
+// Entry t of a packed step, the general kernel's arithmetic (tree_step_kernel).
+template <int kRing, bool kLLeaf, bool kRLeaf>
+__device__ __forceinline__ void pack_entry(const PackItem& it, uint64_t t, const RingArgs& ring) {
+  const uint64_t lo = it.op[0].base + pack_offset(it.op[0].tdst, it.t_bits, t);
+  const uint64_t ro = it.op[1].base + pack_offset(it.op[1].tdst, it.t_bits, t);
+  const uint32_t nk = 1u << it.k_bits;
+  const uint8_t* lhs = it.op[0].ptr;
+  const uint8_t* rhs = it.op[1].ptr;
+  if constexpr (kRing == TSG_RING_OR_AND) {
+    uint32_t acc = 0;
+    for (uint32_t kk = 0; kk < nk; ++kk) {
+      acc |= (uint32_t)lhs[lo + pack_offset(it.op[0].kdst, it.k_bits, kk)] &
+             (uint32_t)rhs[ro + pack_offset(it.op[1].kdst, it.k_bits, kk)];
+    }
+    it.out[t] = acc ? 1 : 0;
+  } else if constexpr (kRing == TSG_RING_U64) {
+    uint64_t acc = 0;
+    for (uint32_t kk = 0; kk < nk; ++kk) {
+      acc += load_elem<kLLeaf, uint64_t>(lhs, lo + pack_offset(it.op[0].kdst, it.k_bits, kk)) *
+             load_elem<kRLeaf, uint64_t>(rhs, ro + pack_offset(it.op[1].kdst, it.k_bits, kk));
+    }
+    reinterpret_cast<uint64_t*>(it.out)[t] = acc;
+  } else {
+    constexpr int leaves = (kLLeaf ? 1 : 0) + (kRLeaf ? 1 : 0);
+    uint32_t acc[TSG_MAX_PRIMES] = {0, 0, 0, 0};
+    uint64_t part[TSG_MAX_PRIMES] = {0, 0, 0, 0};
+    const uint64_t lp = it.op[0].plane, rp = it.op[1].plane;
+    for (uint32_t kk = 0; kk < nk; ++kk) {
+      const uint64_t lko = lo + pack_offset(it.op[0].kdst, it.k_bits, kk);
+      const uint64_t rko = ro + pack_offset(it.op[1].kdst, it.k_bits, kk);
+#pragma unroll
+      for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
+        if (p < ring.np) {
+          const uint32_t l = load_elem<kLLeaf, uint32_t>(lhs, lko + (kLLeaf ? 0 : p * lp));
+          const uint32_t r = load_elem<kRLeaf, uint32_t>(rhs, rko + (kRLeaf ? 0 : p * rp));
+          part[p] += (uint64_t)l * r;
+          if (leaves == 0 ? (kk & 1) : ((kk & 15) == 15)) {
+            acc[p] = add_mod(acc[p], mont_finish(part[p], leaves, ring, p), ring.p[p]);
+            part[p] = 0;
+          }
+        }
+      }
+    }
+    uint32_t* out = reinterpret_cast<uint32_t*>(it.out);
+#pragma unroll
+    for (int p = 0; p < TSG_MAX_PRIMES; ++p) {
+      if (p < ring.np)
+        out[t + p * it.o_plane] = add_mod(acc[p], mont_finish(part[p], leaves, ring, p), ring.p[p]);
+    }
+  }
+}
+
+// The steps of a packed launch: warp w belongs to the last step whose warp0 <= w.
+template <int kRing>
+__global__ void __launch_bounds__(kThreads) tree_pack_kernel(const __grid_constant__ PackArgs a,
+                                                             RingArgs ring) {
+  const uint32_t warp = blockIdx.x * (kThreads / 32) + threadIdx.x / 32;
+  if (warp >= a.n_warps) return;
+  int lo = 0, hi = a.n_items - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (a.items[mid].warp0 <= warp) lo = mid;
+    else hi = mid - 1;
+  }
+  const PackItem& it = a.items[lo];
+  const uint64_t t = (uint64_t)(warp - it.warp0) * 32 + (threadIdx.x & 31);
+  if (t >= (1ull << it.t_bits)) return;
+  if constexpr (kRing == TSG_RING_OR_AND) {
+    pack_entry<kRing, true, true>(it, t, ring);  // every OR-AND operand is uint8
+  } else {
+    switch (it.leaves) {
+      case 0: pack_entry<kRing, false, false>(it, t, ring); break;
+      case 1: pack_entry<kRing, true, false>(it, t, ring); break;
+      case 2: pack_entry<kRing, false, true>(it, t, ring); break;
+      default: pack_entry<kRing, true, true>(it, t, ring); break;
+    }
+  }
+}
+
+// Launcher of the packed kernel (tsg_pack.cu).
+tsg_status launch_pack(int ring, const PackArgs& a, const RingArgs& ra, cudaStream_t st);
+
 }  // namespace dev
 }  // namespace tsg

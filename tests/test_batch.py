@@ -83,6 +83,56 @@ def test_lane_workspace_holds_every_lane_region():
             ctypes.byref(out)) == _native.TSG_ERR_INVALID_ARGUMENT
 
 
+def test_packed_workspace_regions():
+    """Packed batches: a lane's region holds its largest instance (level-order placement
+    for instances run in one group of all their slices, step order otherwise), so one lane
+    needs the largest single-instance requirement and one lane per instance the sum; bad
+    lane counts and group sizes are rejected on the host."""
+    plans = _plans(ragged_instances(6, 10, 20), target_bits=8)
+    lib = _native.lib()
+    full = [1 << p.num_sliced for p in plans]
+    groups = [full[0], max(1, full[1] // 2), full[2], full[3], full[4], full[5]]
+    handles = (ctypes.c_void_p * len(plans))(*[p.handle.value for p in plans])
+    ring, planes = _native.TSG_RING_MODP, 3
+
+    def size(hs, gs, lanes):
+        out = ctypes.c_int64()
+        _native.check(lib.tsg_batch_packed_workspace_bytes(
+            len(gs), hs, ring, planes, _native.i64_array(gs), lanes, ctypes.byref(out)))
+        return out.value
+
+    each = [size((ctypes.c_void_p * 1)(p.handle.value), [g], 1) for p, g in zip(plans, groups)]
+    assert all(e % 256 == 0 and e >= 256 for e in each)
+    assert size(handles, groups, 1) == max(each)
+    assert size(handles, groups, 6) == size(handles, groups, 32) == sum(each)
+    # the step-order placement for the instance run in several groups
+    assert each[1] == (plans[1].workspace_bytes(ring, planes, groups[1]) + 255) // 256 * 256
+    out = ctypes.c_int64()
+    for bad in (0, 33):
+        assert lib.tsg_batch_packed_workspace_bytes(
+            len(plans), handles, ring, planes, _native.i64_array(groups), bad,
+            ctypes.byref(out)) == _native.TSG_ERR_INVALID_ARGUMENT
+    assert lib.tsg_batch_packed_workspace_bytes(
+        len(plans), handles, ring, planes, _native.i64_array([3] + groups[1:]), 2,
+        ctypes.byref(out)) == _native.TSG_ERR_INVALID_ARGUMENT
+
+
+def test_packed_batch_rejects_a_bad_instance_before_launching():
+    plans = _plans(ragged_instances(4, 10, 16, seed=1), target_bits=6)
+    lib = _native.lib()
+    n = len(plans)
+    handles = (ctypes.c_void_p * n)(*[p.handle.value for p in plans])
+    fake = (ctypes.c_void_p * n)(*([256] * n))
+    launches = ctypes.c_int64(5)
+    st = lib.tsg_batch_run_packed(n, handles, _native.TSG_RING_OR_AND, 0, None, fake,
+                                  _native.i64_array([1, 1, 3, 1]), 2, None, 0, fake, None,
+                                  ctypes.byref(launches))
+    assert st == _native.TSG_ERR_INVALID_ARGUMENT and launches.value == 0
+    assert lib.tsg_batch_run_packed(n, handles, _native.TSG_RING_OR_AND, 0, None, fake,
+                                    _native.i64_array([1] * n), 0, None, 0, fake, None,
+                                    None) == _native.TSG_ERR_INVALID_ARGUMENT
+
+
 def test_batch_rejects_a_bad_instance_before_launching():
     """Instance 2 has a group size that is not a power of two: the call fails in the host
     checks (the pointers are never dereferenced, so placeholders suffice)."""
@@ -132,10 +182,43 @@ def test_ragged_batch_counts_and_sat_bits_match_brute_force(cuda):
 
 
 @pytest.mark.gpu
-def test_batch_graph_replay_matches_uncaptured_run(cuda):
+def test_packed_batch_equals_lanes_and_the_checkers(cuda):
+    """Packed runs (small steps of a tree level across instances in shared launches) give
+    the per-step runs' results bit for bit in every ring, with fewer launches: small
+    sliced instances (one group of all slices, or several groups), and unsliced n = 28-32
+    instances whose large steps run as their own launches between the packed ones."""
+    small = ragged_instances(10, 12, 20, seed=7)
+    large = ragged_instances(4, 28, 32, seed=8)
+    instances = small + large
+    diagrams = [cnf.clause_diagram() for cnf in instances]
+    trees = [plan_tree(d.wiring, target_bits=9 if i < len(small) else None, trials=1)
+             for i, d in enumerate(diagrams)]
+    packed = BatchContraction(CudaRel, diagrams, trees=trees, lanes=3)
+    lanes = BatchContraction(CudaRel, diagrams, trees=trees, lanes=3, packed=False)
+    assert any(c.num_slices > 1 for c in packed.contractions)
+    groups = [c.num_slices for c in packed.contractions]
+    j = next(i for i, c in enumerate(packed.contractions) if c.num_slices >= 4)
+    groups[j] = packed.contractions[j].num_slices // 4  # this one runs in four groups
+    primes = PRIMES_31[:3]
+    for ring, pr in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_U64, ()),
+                     (_native.TSG_RING_OR_AND, ())):
+        a = [r.cpu() for r in packed.run(ring, pr, groups=groups)]
+        n_packed = packed.last_launches
+        b = [r.cpu() for r in lanes.run(ring, pr, groups=groups)]
+        assert all(torch.equal(x, y) for x, y in zip(a, b)), ring
+        assert 0 < n_packed < lanes.last_launches
+    expected = [orc.brute_force_count(c.num_vars, c.clauses) for c in small] + \
+               [orc.dpll_count(c.num_vars, c.clauses)[0] for c in large]
+    assert packed.count(num_primes=3, groups=groups) == expected
+    assert [bool(x) for x in packed.contract(groups=groups)] == [e > 0 for e in expected]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("packed", [True, False])
+def test_batch_graph_replay_matches_uncaptured_run(cuda, packed):
     instances = ragged_instances(8, 14, 24, seed=3)
     batch = BatchContraction(CudaRel, [cnf.clause_diagram() for cnf in instances],
-                             target_bits=10, trials=1)
+                             target_bits=10, trials=1, packed=packed)
     primes = PRIMES_31[:3]
     direct = [r.clone() for r in batch.run(_native.TSG_RING_MODP, primes)]
     sat_direct = [r.clone() for r in batch.run(_native.TSG_RING_OR_AND)]
