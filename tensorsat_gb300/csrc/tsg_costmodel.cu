@@ -23,6 +23,7 @@ constexpr int kTileM = 128;  // rows of one CTA tile = TMEM lanes
 constexpr int kTileK = 64;   // K staged per round (4 MMAs of K = 16)
 constexpr int kThreads = 128;
 constexpr unsigned long long kWaitNs = 2000000000ull;
+constexpr int kStagePerWarp = 32 * (32 * 4 + 16);  // epilogue stage: 32 rows of 32 FP32 + pad
 
 __device__ int g_cm_error = 0;  // set when a bounded wait for the MMAs gives up
 
@@ -56,6 +57,11 @@ __device__ __forceinline__ uint32_t tile_offset(int r, int k) {
   return (uint32_t)((r >> 3) * (kTileK / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
 
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&p);
+}
+
 __device__ __forceinline__ bool wait_mbar(uint64_t* bar, uint32_t parity) {
   const uint32_t addr = smem_u32(bar);
   uint64_t t0;
@@ -83,8 +89,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     gemm_bf16_tn_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B,
                         const float* __restrict__ bias, void* out, int K, int ldo, int relu,
                         int out_f32) {
-  __shared__ __align__(128) uint8_t sa[kTileM * kTileK * 2];
-  __shared__ __align__(128) uint8_t sb[N * kTileK * 2];
+  // the A and B tiles; after the last MMA the same bytes stage the epilogue's rows
+  __shared__ __align__(1024) uint8_t smem[(kTileM + N) * kTileK * 2];
+  static_assert((kTileM + N) * kTileK * 2 >= 4 * kStagePerWarp, "epilogue stage does not fit");
+  uint8_t* sa = smem;
+  uint8_t* sb = smem + kTileM * kTileK * 2;
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x;
@@ -109,15 +118,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int ktiles = K / kTileK;
   bool ok = true;
   for (int kt = 0; kt < ktiles && ok; ++kt) {
-    // stage the A and B tiles: 16-byte chunks (8 consecutive K values) per thread
+    // stage the A and B tiles: 16-byte chunks (8 consecutive K values) per thread. Each
+    // group of 8 threads takes the 8 rows of one core matrix (distinct shared-memory
+    // banks); a warp reads 64 contiguous bytes of each of 8 rows.
     const int k0 = kt * kTileK;
     for (int c = tid; c < kTileM * (kTileK / 8); c += kThreads) {
-      const int r = c / (kTileK / 8), kc = (c % (kTileK / 8)) * 8;
+      const int q = c >> 3;
+      const int r = (q / (kTileK / 8)) * 8 + (c & 7), kc = (q % (kTileK / 8)) * 8;
       const uint4 v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * K + k0 + kc);
       *reinterpret_cast<uint4*>(sa + tile_offset(r, kc)) = v;
     }
     for (int c = tid; c < N * (kTileK / 8); c += kThreads) {
-      const int r = c / (kTileK / 8), kc = (c % (kTileK / 8)) * 8;
+      const int q = c >> 3;
+      const int r = (q / (kTileK / 8)) * 8 + (c & 7), kc = (q % (kTileK / 8)) * 8;
       const uint4 v = *reinterpret_cast<const uint4*>(B + (size_t)r * K + k0 + kc);
       *reinterpret_cast<uint4*>(sb + tile_offset(r, kc)) = v;
     }
@@ -152,8 +165,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    // epilogue: warp w reads TMEM lanes 32w..32w+31 (rows), 32 columns per load
-    const int row = m0 + warp * 32 + (tid & 31);
+    // epilogue: warp w reads TMEM lanes 32w..32w+31 (rows), 32 columns per load; each
+    // thread puts its row's 32 results (bias, ReLU, conversion applied) into the warp's
+    // stage, then the warp writes the 32 x 32 block out in 16-byte pieces, whole rows
+    // per group of lanes
+    const int lane = tid & 31;
+    const int eb = out_f32 ? 4 : 2;
+    const int pitch = 32 * eb + 16;  // bytes per staged row (16-byte groups spread over banks)
+    uint8_t* stage = smem + warp * kStagePerWarp;
+    const int lpr = 2 * eb;          // lanes per row of 32 results
+    const int rpi = 32 / lpr;        // rows per warp-wide copy
 #pragma unroll 1
     for (int c0 = 0; c0 < N; c0 += 32) {
       uint32_t v[32];
@@ -169,16 +190,37 @@ __global__ void __launch_bounds__(kThreads, 1)
             "=r"(v[30]), "=r"(v[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      float x[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
-        float x = __uint_as_float(v[j]);
-        if (bias) x += bias[c0 + j];
-        if (relu) x = fmaxf(x, 0.f);
-        if (out_f32)
-          reinterpret_cast<float*>(out)[(size_t)row * ldo + c0 + j] = x;
-        else
-          reinterpret_cast<__nv_bfloat16*>(out)[(size_t)row * ldo + c0 + j] = __float2bfloat16(x);
+        x[j] = __uint_as_float(v[j]) + (bias ? bias[c0 + j] : 0.f);
+        if (relu) x[j] = fmaxf(x[j], 0.f);
       }
+      uint8_t* my = stage + lane * pitch;
+      if (out_f32) {
+#pragma unroll
+        for (int j = 0; j < 32; j += 4)
+          *reinterpret_cast<float4*>(my + j * 4) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 32; j += 8) {
+          uint4 u;
+          u.x = pack_bf16x2(x[j], x[j + 1]);
+          u.y = pack_bf16x2(x[j + 2], x[j + 3]);
+          u.z = pack_bf16x2(x[j + 4], x[j + 5]);
+          u.w = pack_bf16x2(x[j + 6], x[j + 7]);
+          *reinterpret_cast<uint4*>(my + j * 2) = u;
+        }
+      }
+      __syncwarp();
+      for (int r0 = 0; r0 < 32; r0 += rpi) {
+        const int r = r0 + lane / lpr, part = lane % lpr;
+        const uint4 u = *reinterpret_cast<const uint4*>(stage + r * pitch + part * 16);
+        uint8_t* dst = reinterpret_cast<uint8_t*>(out) +
+                       ((size_t)(m0 + warp * 32 + r) * ldo + c0) * eb + part * 16;
+        *reinterpret_cast<uint4*>(dst) = u;
+      }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -278,8 +320,10 @@ tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void* a_dev,
       ldo < n || m / cm::kTileM > 0x7fffffff)
     return fail(TSG_ERR_INVALID_ARGUMENT,
                 "cm_gemm: M must be a multiple of 128, K of 64, N 64 or 128, ldo >= N");
-  if (((uintptr_t)a_dev | (uintptr_t)b_dev) & 15)
-    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: operands must be 16-byte aligned");
+  if (((uintptr_t)a_dev | (uintptr_t)b_dev | (uintptr_t)out_dev) & 15)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: operands and output must be 16-byte aligned");
+  if ((ldo * (out_f32 ? 4 : 2)) % 16 != 0)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: output rows must be a multiple of 16 bytes apart");
   const dim3 grid((unsigned)(m / cm::kTileM));
   cudaStream_t st = (cudaStream_t)stream;
   const auto* a = (const __nv_bfloat16*)a_dev;
