@@ -51,8 +51,12 @@ UNIT = "instances/s"
 N_VARS, N_CLAUSES = 60, 256
 TARGET_BITS = 26
 NUM_PRIMES = 3
-PLAN_FILE = ROOT / "plans" / "3sat_n60_m256_rng0_t26.json"
-TUNE_FILE = ROOT / "plans" / "3sat_n60_m256_rng0_t26.tune.json"
+# committed plans of the headline instance: the planner's tree (8 trials) and the learned
+# path's tree (the committed cost model's pick among 64 planner candidates,
+# plans/make_plan.py), each with its autotuner entries
+PLAN_FILES = {"planner": ROOT / "plans" / "3sat_n60_m256_rng0_t26.json",
+              "learned": ROOT / "plans" / "3sat_n60_m256_rng0_learned.json"}
+TUNE_FILES = {k: v.with_name(v.stem + ".tune.json") for k, v in PLAN_FILES.items()}
 
 
 def parse_args():
@@ -90,8 +94,12 @@ def parse_args():
     p.add_argument("--tune", action="store_true",
                    help="run the autotuner for the n=60 plan when its tuning file has no "
                         "entry for this GPU, and store the entry")
-    p.add_argument("--tune-file", default=str(TUNE_FILE),
-                   help="tuning file of the n=60 plan (read, and written by --tune)")
+    p.add_argument("--tree", choices=["learned", "planner"], default=None,
+                   help="committed n=60 tree: the learned path's pick (default when its plan "
+                        "file exists) or the planner's own")
+    p.add_argument("--tune-file", default=None,
+                   help="tuning file of the n=60 plan (read, and written by --tune; default: "
+                        "the one beside the chosen plan)")
     p.add_argument("--no-tuning", action="store_true",
                    help="ignore the committed tuning (the executor's own kernel choices)")
     p.add_argument("--no-instance", action="store_true",
@@ -168,11 +176,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def tree_choice(args) -> str:
+    if args.tree is not None:
+        return args.tree
+    return "learned" if PLAN_FILES["learned"].exists() else "planner"
+
+
 def committed_plan(args) -> dict | None:
     """The committed plan of the headline workload (seed 0, 8 trials), unless replanning."""
-    if args.replan or args.seed != 0 or args.trials != 8 or not PLAN_FILE.exists():
+    path = PLAN_FILES[tree_choice(args)]
+    if args.replan or args.seed != 0 or args.trials != 8 or not path.exists():
         return None
-    return json.loads(PLAN_FILE.read_text())
+    return json.loads(path.read_text())
 
 
 def build_workload(args):
@@ -285,14 +300,21 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def dominant_traffic(ring: str, step: int, group: int):
+DRAM_PROFILES = {"planner": ROOT / "profiles" / "tree_steps_n60_dram.txt",
+                 "learned": ROOT / "profiles" / "tree_steps_n60_learned_dram.txt"}
+
+
+def dominant_traffic(ring: str, step: int, group: int, tree: str, plan_sha: str):
     """DRAM bytes (read + write) of one launch of tree step `step` in `ring`, from the ncu
-    launch list committed under profiles/ for this workload, or None when that capture
-    does not hold this step at this group size."""
-    path = ROOT / "profiles" / "tree_steps_n60_dram.txt"
-    if not path.exists():
+    launch list committed under profiles/ for this plan (its "# plan <sha256>" line), or
+    None when no capture of this plan holds this step at this group size."""
+    path = DRAM_PROFILES.get(tree)
+    if path is None or not path.exists():
         return None
-    for line in path.read_text().splitlines():
+    text = path.read_text()
+    if f"# plan {plan_sha}" not in text:
+        return None
+    for line in text.splitlines():
         parts = line.split("#")[0].split()
         if len(parts) == 5 and parts[0] == ring and parts[1] == str(step) and parts[2] == str(group):
             try:
@@ -312,6 +334,11 @@ def workload_config(args, contraction, group: int) -> dict:
         "sliced_wires": st["num_sliced"],
         "log2_index_space_per_slice": round(st["log2_index_space_per_slice"], 3),
         "slices_per_step": group,
+        "tree": ("replanned by the planner" if committed_plan(args) is None else
+                 {"learned": "learned path: the committed cost model's pick among 64 planner "
+                             "candidates (plans/3sat_n60_m256_rng0_learned.json)",
+                  "planner": "the planner's tree, 8 trials "
+                             "(plans/3sat_n60_m256_rng0_t26.json)"}[tree_choice(args)]),
         "count_ring": f"mod {NUM_PRIMES} primes < 2^31 (CRT)",
         "l2": "inputs larger than L2 (intermediates up to 2^26 entries x slices)",
     }
@@ -367,7 +394,7 @@ def run_gb300(args) -> None:
     if committed_plan(args) is not None and not args.no_tuning:
         from tensorsat_gb300 import autotune
 
-        tune_file = Path(args.tune_file)
+        tune_file = Path(args.tune_file or TUNE_FILES[tree_choice(args)])
         entries = {r: autotune.load(tune_file, contraction, r, p)
                    for r, p in ((_native.TSG_RING_MODP, primes), (_native.TSG_RING_OR_AND, ()))}
         if args.tune and any(e is None for e in entries.values()):
@@ -480,7 +507,10 @@ def run_gb300(args) -> None:
     dom_bytes = step_bytes[ring_name][dom] * group
     achieved = dom_bytes / (dom_ms / 1e3) / 1e9
     step_total_ms = sum(sum(v) for v in acc_ms.values()) / timing_passes
-    traffic = dominant_traffic(ring_name, dom, g_modp if ring_name == "modp" else g_or)
+    from tensorsat_gb300 import autotune
+
+    traffic = dominant_traffic(ring_name, dom, g_modp if ring_name == "modp" else g_or,
+                               tree_choice(args), autotune.plan_key(contraction))
     step_roofline = (sum(step_bytes["modp"]) + sum(step_bytes["or_and"])) * group / step_s / 1e9
 
     # end to end through the public API: host leaves in, host results out, every step
@@ -920,17 +950,7 @@ def candidates_parallel(pool, instances, count: int, parts: int = 8):
     ``parts`` workers (the planner's usual choice stays first)."""
     from tensorsat_gb300 import costmodel
 
-    settings = costmodel.candidate_settings(count)
-    jobs = [(c.num_vars, c.clauses, count, settings[p::parts])
-            for c in instances for p in range(parts)]
-    res = pool.map(_candidates_job, jobs, chunksize=1)
-    out = []
-    for i in range(len(instances)):
-        share = res[i * parts:(i + 1) * parts]
-        merged = [t for k in range(max(len(x) for x in share))
-                  for x in share if k < len(x) for t in [x[k]]]
-        out.append(costmodel.distinct(merged))
-    return out
+    return costmodel.cnf_candidates(pool, instances, count, parts)
 
 
 COSTMODEL_FILE = ROOT / "plans" / "costmodel_n60.npz"

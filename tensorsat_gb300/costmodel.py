@@ -341,6 +341,33 @@ def candidate_trees(wiring: Any, count: int, target_bits: int = 26,
     return out
 
 
+def _cnf_candidates(args: tuple) -> list[tuple[Any, tuple]]:
+    """Worker: candidate trees of one CNF instance's clause network for some settings."""
+    from .lib.sat import CNFInstance
+
+    num_vars, clauses, count, settings = args
+    return candidate_trees(CNFInstance(num_vars, clauses).clause_diagram().wiring, count,
+                           settings=settings)
+
+
+def cnf_candidates(pool: Any, instances: Sequence[Any], count: int,
+                   parts: int = 8) -> list[list[tuple[Any, tuple]]]:
+    """The planner candidates (:func:`candidate_trees`) of the clause network of every
+    CNF instance, each instance's settings split over ``parts`` tasks of ``pool`` (a
+    process pool; start it with ``spawn``, or before the first CUDA call). The planner's
+    usual choice stays first."""
+    settings = candidate_settings(count)
+    jobs = [(c.num_vars, [tuple(cl) for cl in c.clauses], count, settings[p::parts])
+            for c in instances for p in range(parts)]
+    res = pool.map(_cnf_candidates, jobs, chunksize=1)
+    out = []
+    for i in range(len(instances)):
+        share = res[i * parts:(i + 1) * parts]
+        merged = [x[k] for k in range(max(len(x) for x in share)) for x in share if k < len(x)]
+        out.append(distinct(merged))
+    return out
+
+
 def distinct(trees: Sequence[tuple[Any, tuple]]) -> list[tuple[Any, tuple]]:
     """The (tree, sliced wires) pairs without repeats, in their first order."""
     out, seen = [], set()
