@@ -304,15 +304,14 @@ DRAM_PROFILES = {"planner": ROOT / "profiles" / "tree_steps_n60_dram.txt",
                  "learned": ROOT / "profiles" / "tree_steps_n60_learned_dram.txt"}
 
 
-def dominant_traffic(ring: str, step: int, group: int, tree: str, plan_sha: str):
+def dominant_traffic(ring: str, step: int, group: int, plan_sha: str):
     """DRAM bytes (read + write) of one launch of tree step `step` in `ring`, from the ncu
-    launch list committed under profiles/ for this plan (its "# plan <sha256>" line), or
-    None when no capture of this plan holds this step at this group size."""
-    path = DRAM_PROFILES.get(tree)
-    if path is None or not path.exists():
-        return None
-    text = path.read_text()
-    if f"# plan {plan_sha}" not in text:
+    launch list committed under profiles/ for this plan (the file whose "# plan <sha256>"
+    line names it), or None when no capture of this plan holds this step at this group
+    size."""
+    text = next((p.read_text() for p in DRAM_PROFILES.values()
+                 if p.exists() and f"# plan {plan_sha}" in p.read_text()), None)
+    if text is None:
         return None
     for line in text.splitlines():
         parts = line.split("#")[0].split()
@@ -322,6 +321,19 @@ def dominant_traffic(ring: str, step: int, group: int, tree: str, plan_sha: str)
             except ValueError:
                 return None
     return None
+
+
+def tree_text(args) -> str:
+    plan = committed_plan(args)
+    if plan is None:
+        return "replanned by the planner"
+    if tree_choice(args) == "planner":
+        return "the planner's tree, 8 trials (plans/3sat_n60_m256_rng0_t26.json)"
+    cb = plan.get("chosen_by", {})
+    picked = cb.get("picked")
+    return (f"learned path: the committed cost model's pick among {cb.get('candidates')} planner "
+            f"candidates (plans/3sat_n60_m256_rng0_learned.json): candidate {picked}"
+            + (", the planner's own tree" if picked == 0 else ""))
 
 
 def workload_config(args, contraction, group: int) -> dict:
@@ -334,11 +346,7 @@ def workload_config(args, contraction, group: int) -> dict:
         "sliced_wires": st["num_sliced"],
         "log2_index_space_per_slice": round(st["log2_index_space_per_slice"], 3),
         "slices_per_step": group,
-        "tree": ("replanned by the planner" if committed_plan(args) is None else
-                 {"learned": "learned path: the committed cost model's pick among 64 planner "
-                             "candidates (plans/3sat_n60_m256_rng0_learned.json)",
-                  "planner": "the planner's tree, 8 trials "
-                             "(plans/3sat_n60_m256_rng0_t26.json)"}[tree_choice(args)]),
+        "tree": tree_text(args),
         "count_ring": f"mod {NUM_PRIMES} primes < 2^31 (CRT)",
         "l2": "inputs larger than L2 (intermediates up to 2^26 entries x slices)",
     }
@@ -510,7 +518,7 @@ def run_gb300(args) -> None:
     from tensorsat_gb300 import autotune
 
     traffic = dominant_traffic(ring_name, dom, g_modp if ring_name == "modp" else g_or,
-                               tree_choice(args), autotune.plan_key(contraction))
+                               autotune.plan_key(contraction))
     step_roofline = (sum(step_bytes["modp"]) + sum(step_bytes["or_and"])) * group / step_s / 1e9
 
     # end to end through the public API: host leaves in, host results out, every step
