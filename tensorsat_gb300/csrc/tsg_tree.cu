@@ -655,10 +655,11 @@ tsg_status fill_tile_operand(TileOperand& op, const int* pos, const OperandDesc&
       op.pair_sel = sel;
     }
   }
-  if (op.mode == kModeGather && v == 4 && !op.leaf && ring != TSG_RING_OR_AND &&
-      op.tab[0] == 0 && op.tab[1] == 1 && op.tab[2] != 0 && op.tab[3] == op.tab[2] + 1 &&
-      (op.tab[2] & 1) == 0 && (op.base & 1) == 0)
-    op.mode = kModeDual;  // alignment of the pairs is proven in check_tile_bounds
+  // positions {0, 1, d, d + 1}: two 2-element vector loads (count rings: intermediates;
+  // OR-AND: any operand, two 2-byte loads), decided once the E and summed offsets are known
+  const bool dual_shape = op.mode == kModeGather && v == 4 &&
+                          (ring == TSG_RING_OR_AND || !op.leaf) && op.tab[0] == 0 &&
+                          op.tab[1] == 1 && op.tab[2] != 0 && op.tab[3] == op.tab[2] + 1;
   if (op.mode == kModeGather && v == 16) {
     // carried fast F bits (F index, operand bit), ascending F index: distinct value d
     // has bit k of d = carried bit k of the position
@@ -691,6 +692,17 @@ tsg_status fill_tile_operand(TileOperand& op, const int* pos, const OperandDesc&
   op.has_e = ep.empty() ? 0 : 1;
   for (int e = 0; e < ne; ++e) op.e_off[e] = (uint32_t)scatter_pairs(ep, e);
   for (int kk = 0; kk < n_k; ++kk) op.k_off[kk] = (uint32_t)scatter_pairs(d.kp, kk);
+  if (dual_shape) {
+    // every offset term but the first position bit even: each pair starts on an even
+    // element (check_tile_bounds proves the same again before the launch)
+    bool even = (op.tab[2] & 1) == 0 && (op.base & 1) == 0 && (op.plane & 1) == 0;
+    for (int i = 0; i < op.g.n; ++i) even = even && op.g.dst[i] >= 1;
+    for (const NarrowMap* m : {&op.f_hi, &op.f_lo})
+      for (int i = 0; i < m->n; ++i) even = even && !(m->dst[i] < 1 && m->src[i] >= 1);
+    for (int e = 0; e < ne; ++e) even = even && (op.e_off[e] & 1) == 0;
+    for (int kk = 0; kk < n_k; ++kk) even = even && (op.k_off[kk] & 1) == 0;
+    if (even) op.mode = kModeDual;
+  }
   return TSG_OK;
 }
 
@@ -701,7 +713,7 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
                       uint64_t cnt, int ring, TileArgs* t, TileShape* shape, bool* ok,
                       TileBits* bits_out = nullptr, bool allow_v16 = true) {
   std::memset(t, 0, sizeof(*t));
-  *ok = st.out_bits <= 30 && st.k_bits <= 4 && cnt <= 65535;
+  *ok = st.out_bits <= 30 && st.k_bits <= 6 && cnt <= 65535;
   if (!*ok) return TSG_OK;
   // E: output bits the larger operand does not carry (at most 2, highest first)
   int carried[2] = {0, 0};
@@ -1083,6 +1095,10 @@ tsg_status build_fused(const RunCtx& c, int s, int64_t base, const TileBits& tb,
       extra.push_back(off);
       extra_max = std::max(extra_max, off);
     }
+    // paired loads need even producer offsets too; otherwise the operand is gathered
+    if (f.op[o].mode == kModeDual)
+      for (uint32_t x : extra)
+        if (x & 1) f.op[o].mode = kModeGather;
     const int v = ps.op[o];
     const uint64_t lo_ext = dp.leaf ? (uint64_t)plan->leaves[v].offset : 0;
     const uint64_t hi_ext = dp.leaf ? lo_ext + (1ull << plan->leaves[v].rank) + c.leaf_extra

@@ -252,7 +252,7 @@ constexpr int kModePerm = 4;
 // two 2-element vector loads
 constexpr int kModeDual = 5;
 constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
-constexpr int kMaxK = 16;  // summed combinations kept in tables (k <= 4)
+constexpr int kMaxK = 64;  // summed combinations kept in tables (k <= 6)
 
 struct NarrowMap {
   int32_t n;
@@ -405,6 +405,11 @@ __device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t
     const uint32_t x = (uint32_t)base[off] * 0x01010101u;
 #pragma unroll
     for (int i = 0; i < V / 4; ++i) w[i] = x;
+  } else if (V == 4 && op.mode == kModeDual) {
+    // positions {0, 1, d, d + 1}: two 2-byte loads (even offsets, proven on the host)
+    const uint32_t lo = *reinterpret_cast<const uint16_t*>(base + off);
+    const uint32_t hi = *reinterpret_cast<const uint16_t*>(base + off + op.tab[2]);
+    w[0] = lo | (hi << 16);
   } else if (V == 4 && op.mode == kModePair) {
     const uint32_t x0 = base[off], x1 = base[off + op.tab[3]];
     uint32_t r = 0;
@@ -594,11 +599,12 @@ __device__ __forceinline__ void tile_thread(const TileArgs& a, const RingArgs& r
               }
             }
             if constexpr (kRing == TSG_RING_MODP && kPairs) {
-              // two Montgomery products stay below p 2^32: reduce every pair of sums
-              if (leaves == 0 && (kk & 1) && kk + 1 < nk) {
+              // two Montgomery products stay below p 2^32: reduce every pair of sums; sums
+              // with a leaf factor are reduced every 16 terms (small_mod's range)
+              if (leaves == 0 ? ((kk & 1) && kk + 1 < nk) : ((kk & 15) == 15 && kk + 1 < nk)) {
 #pragma unroll
                 for (int j = 0; j < V; ++j) {
-                  done[j] = add_mod(done[j], mont_redc(acc[j], pc.p, pc.pinv), pc.p);
+                  done[j] = add_mod(done[j], mont_finish_c(acc[j], leaves, pc), pc.p);
                   acc[j] = 0;
                 }
               }
