@@ -1181,20 +1181,30 @@ def run_costmodel_gemm(args) -> None:
         return e0.elapsed_time(e1) / steps
 
     steps = max(args.steps, 20)
-    ms = timed(ours, steps)
-    _native.check(lib.tsg_cm_take_error(stream))
     want = torch.relu(a.float() @ w.float().T + bias)
-    err = float((out.float() - want).abs().max() / want.abs().max())
+    forms = {}
+    for mode, name in ((1, "staged"), (0, "tma")):
+        _native.check(lib.tsg_cm_set_gemm_mode(mode))
+        out.zero_()
+        t = timed(ours, steps)
+        _native.check(lib.tsg_cm_take_error(stream))
+        forms[name] = {"ms_per_launch": t,
+                       "max_rel_error_vs_fp32": float((out.float() - want).abs().max()
+                                                      / want.abs().max())}
+    _native.check(lib.tsg_cm_set_gemm_mode(1))
+    ms = forms["tma"]["ms_per_launch"]
+    err = forms["tma"]["max_rel_error_vs_fp32"]
     ms_cublas = timed(cublas, steps)
     flops = 2.0 * m * n * k
     nbytes = 2.0 * (m * k + n * k + m * n) + 4 * n
     peak, kind = measured_peaks()
     line = {
-        "metric": "cost-model layer GEMM (tcgen05.mma kind::f16, TMEM accumulator, bias+ReLU "
-                  "epilogue), node rows x 128 x 128",
+        "metric": "cost-model layer GEMM (TMA tensor loads, tcgen05.mma kind::f16, TMEM "
+                  "accumulator, bias+ReLU epilogue), node rows x 128 x 128",
         "value": nbytes / ms / 1e6, "unit": "GB/s", "higher_is_better": True,
         "ms_per_launch": ms, "steps": steps, "warmup": max(3, args.warmup),
         "tflops": flops / ms / 1e9, "cublas_ms_per_launch": ms_cublas,
+        "forms": forms,
         "over_cublas": ms_cublas / ms, "max_rel_error_vs_fp32": err,
         "roofline": {"bound": "hbm", "achieved": nbytes / ms / 1e6, "peak": peak,
                      "unit": "GB/s", "frac": nbytes / ms / 1e6 / peak, "peak_source": kind,

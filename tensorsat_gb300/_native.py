@@ -78,6 +78,7 @@ EXPORTED_SYMBOLS = (
     "tsg_plan_run_variants",
     "tsg_cm_gemm_bf16",
     "tsg_cm_take_error",
+    "tsg_cm_set_gemm_mode",
     "tsg_cm_child_sum",
     "tsg_cm_parent_add",
     "tsg_cm_gemm_at_b",
@@ -179,6 +180,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_batch_run_packed.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
                                          POINTER(c_uint32), POINTER(c_void_p), _i64p, c_int32,
                                          c_void_p, c_int64, POINTER(c_void_p), c_void_p, _i64p]
+    lib.tsg_cm_set_gemm_mode.restype = c_int32
+    lib.tsg_cm_set_gemm_mode.argtypes = [c_int32]
     lib.tsg_plan_variants_workspace_bytes.restype = c_int32
     lib.tsg_plan_variants_workspace_bytes.argtypes = [c_void_p, c_int32, c_int32, c_int64,
                                                       c_int64, _i64p]

@@ -8,11 +8,16 @@
 // swizzling (8-row x 16-byte core matrices), the accumulator read back with tcgen05.ld
 // for a fused epilogue (bias, ReLU, BF16 or FP32 store). The remaining training kernels
 // (child aggregation and its transpose, weight gradients, Adam) are plain CUDA.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <atomic>
+#include <mutex>
+#include <string>
 
 #include "tsg_common.cuh"
 
@@ -78,6 +83,70 @@ __device__ __forceinline__ bool wait_mbar(uint64_t* bar, uint32_t parity) {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     if (t - t0 > kWaitNs) return false;
+  }
+}
+
+// Epilogue of a 128-row tile: warp w reads TMEM lanes 32w..32w+31 (rows), 32 columns per
+// load; each thread puts its row's 32 results (bias, ReLU, conversion applied) into the
+// warp's stage in shared memory (`smem`, free once the MMAs are done), then the warp writes
+// the 32 x 32 block out in 16-byte pieces, whole rows per group of lanes.
+template <int N>
+__device__ __forceinline__ void epilogue(uint32_t tmem, uint8_t* smem, void* out, int m0, int ldo,
+                                         const float* __restrict__ bias, int relu, int out_f32) {
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+  const int eb = out_f32 ? 4 : 2;
+  const int pitch = 32 * eb + 16;  // bytes per staged row (16-byte groups spread over banks)
+  uint8_t* stage = smem + warp * kStagePerWarp;
+  const int lpr = 2 * eb;          // lanes per row of 32 results
+  const int rpi = 32 / lpr;        // rows per warp-wide copy
+#pragma unroll 1
+  for (int c0 = 0; c0 < N; c0 += 32) {
+    uint32_t v[32];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+        "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+          "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
+          "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
+          "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+          "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    float x[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      x[j] = __uint_as_float(v[j]) + (bias ? bias[c0 + j] : 0.f);
+      if (relu) x[j] = fmaxf(x[j], 0.f);
+    }
+    uint8_t* my = stage + lane * pitch;
+    if (out_f32) {
+#pragma unroll
+      for (int j = 0; j < 32; j += 4)
+        *reinterpret_cast<float4*>(my + j * 4) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; j += 8) {
+        uint4 u;
+        u.x = pack_bf16x2(x[j], x[j + 1]);
+        u.y = pack_bf16x2(x[j + 2], x[j + 3]);
+        u.z = pack_bf16x2(x[j + 4], x[j + 5]);
+        u.w = pack_bf16x2(x[j + 6], x[j + 7]);
+        *reinterpret_cast<uint4*>(my + j * 2) = u;
+      }
+    }
+    __syncwarp();
+    for (int r0 = 0; r0 < 32; r0 += rpi) {
+      const int r = r0 + lane / lpr, part = lane % lpr;
+      const uint4 u = *reinterpret_cast<const uint4*>(stage + r * pitch + part * 16);
+      uint8_t* dst = reinterpret_cast<uint8_t*>(out) +
+                     ((size_t)(m0 + warp * 32 + r) * ldo + c0) * eb + part * 16;
+      *reinterpret_cast<uint4*>(dst) = u;
+    }
+    __syncwarp();
   }
 }
 
@@ -164,65 +233,143 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
   }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
-    // epilogue: warp w reads TMEM lanes 32w..32w+31 (rows), 32 columns per load; each
-    // thread puts its row's 32 results (bias, ReLU, conversion applied) into the warp's
-    // stage, then the warp writes the 32 x 32 block out in 16-byte pieces, whole rows
-    // per group of lanes
-    const int lane = tid & 31;
-    const int eb = out_f32 ? 4 : 2;
-    const int pitch = 32 * eb + 16;  // bytes per staged row (16-byte groups spread over banks)
-    uint8_t* stage = smem + warp * kStagePerWarp;
-    const int lpr = 2 * eb;          // lanes per row of 32 results
-    const int rpi = 32 / lpr;        // rows per warp-wide copy
-#pragma unroll 1
-    for (int c0 = 0; c0 < N; c0 += 32) {
-      uint32_t v[32];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-          "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
-            "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]),
-            "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]),
-            "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-            "=r"(v[30]), "=r"(v[31])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      float x[32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        x[j] = __uint_as_float(v[j]) + (bias ? bias[c0 + j] : 0.f);
-        if (relu) x[j] = fmaxf(x[j], 0.f);
-      }
-      uint8_t* my = stage + lane * pitch;
-      if (out_f32) {
-#pragma unroll
-        for (int j = 0; j < 32; j += 4)
-          *reinterpret_cast<float4*>(my + j * 4) = make_float4(x[j], x[j + 1], x[j + 2], x[j + 3]);
-      } else {
-#pragma unroll
-        for (int j = 0; j < 32; j += 8) {
-          uint4 u;
-          u.x = pack_bf16x2(x[j], x[j + 1]);
-          u.y = pack_bf16x2(x[j + 2], x[j + 3]);
-          u.z = pack_bf16x2(x[j + 4], x[j + 5]);
-          u.w = pack_bf16x2(x[j + 6], x[j + 7]);
-          *reinterpret_cast<uint4*>(my + j * 2) = u;
-        }
-      }
-      __syncwarp();
-      for (int r0 = 0; r0 < 32; r0 += rpi) {
-        const int r = r0 + lane / lpr, part = lane % lpr;
-        const uint4 u = *reinterpret_cast<const uint4*>(stage + r * pitch + part * 16);
-        uint8_t* dst = reinterpret_cast<uint8_t*>(out) +
-                       ((size_t)(m0 + warp * 32 + r) * ldo + c0) * eb + part * 16;
-        *reinterpret_cast<uint4*>(dst) = u;
-      }
-      __syncwarp();
-    }
+  if (ok) epilogue<N>(tmem, smem, out, m0, ldo, bias, relu, out_f32);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)N)
+                 : "memory");
+}
+
+// The same product with the operand tiles loaded by the tensor memory accelerator:
+// cp.async.bulk.tensor 2D boxes of 64 K x rows (128 bytes per row) written into shared
+// memory in the 128-byte swizzled K-major layout, completion counted in bytes on an
+// mbarrier; one thread issues the copies and the MMAs. K is staged 128 at a time (two
+// boxes per operand).
+constexpr int kTmaBoxK = 64;     // K per box: one 128-byte line per row
+constexpr int kTmaRoundK = 128;  // K per round (two boxes per operand)
+
+// Shared-memory descriptor of a K-major tile in the 128-byte swizzled layout TMA writes:
+// 8-row groups 1024 bytes apart (SBO), leading offset unused (1), version 1, layout type
+// 2 (128-byte swizzle, bits 61-63). A K step of 16 values moves the start by 32 bytes
+// within the swizzled line; tiles are 1024-byte aligned (base offset 0).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <int N>
+constexpr int tma_smem_bytes() {
+  return 1024 + (kTmaRoundK / kTmaBoxK) * (kTileM + N) * kTmaBoxK * 2;
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThreads, 1)
+    gemm_bf16_tma_kernel(const __grid_constant__ CUtensorMap tma_a,
+                         const __grid_constant__ CUtensorMap tma_b,
+                         const float* __restrict__ bias, void* out, int K, int ldo, int relu,
+                         int out_f32) {
+  extern __shared__ uint8_t dyn_smem[];
+  // 1024-byte aligned tiles: the round's A boxes, then its B boxes; afterwards the same
+  // bytes stage the epilogue
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(dyn_smem) + 1023) & ~static_cast<uintptr_t>(1023));
+  constexpr int kABox = kTileM * kTmaBoxK * 2;
+  constexpr int kBBox = N * kTmaBoxK * 2;
+  static_assert((kTmaRoundK / kTmaBoxK) * kABox >= 4 * kStagePerWarp, "epilogue stage");
+  uint8_t* sa = smem;
+  uint8_t* sb = smem + (kTmaRoundK / kTmaBoxK) * kABox;
+  __shared__ __align__(8) uint64_t full;
+  __shared__ __align__(8) uint64_t mma_done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int round_ok;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int m0 = blockIdx.x * kTileM;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"((uint32_t)N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&full)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mma_done)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  constexpr uint32_t idesc = instr_desc(N);
+  const int rounds = (K + kTmaRoundK - 1) / kTmaRoundK;
+  bool ok = true;
+  for (int r = 0; r < rounds && ok; ++r) {
+    const int k0 = r * kTmaRoundK;
+    const int boxes = min(kTmaRoundK, K - k0) / kTmaBoxK;
+    if (tid == 0) {
+      const uint32_t bytes = (uint32_t)boxes * (kABox + kBBox);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                       smem_u32(&full)),
+                   "r"(bytes)
+                   : "memory");
+      for (int c = 0; c < boxes; ++c) {
+        tma_load_2d(sa + c * kABox, &tma_a, k0 + c * kTmaBoxK, m0, &full);
+        tma_load_2d(sb + c * kBBox, &tma_b, k0 + c * kTmaBoxK, 0, &full);
+      }
+      int good = wait_mbar(&full, (uint32_t)(r & 1)) ? 1 : 0;
+      if (good) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int c = 0; c < boxes; ++c) {
+#pragma unroll
+          for (int kk = 0; kk < kTmaBoxK / 16; ++kk) {
+            const uint64_t ad = smem_desc_sw128(smem_u32(sa + c * kABox) + kk * 32);
+            const uint64_t bd = smem_desc_sw128(smem_u32(sb + c * kBBox) + kk * 32);
+            const uint32_t acc = (r > 0 || c > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_u32(&mma_done))
+            : "memory");
+      } else {
+        atomicExch(&g_cm_error, TSG_ERR_TIMEOUT);
+        wait_mbar(&full, (uint32_t)(r & 1));  // the copies in flight, once more (bounded)
+      }
+      round_ok = good;
+    }
+    __syncthreads();
+    ok = round_ok != 0;
+    // the MMAs read this round's tiles: wait before the next round or the epilogue
+    if (ok && !wait_mbar(&mma_done, (uint32_t)(r & 1))) {
+      if (tid == 0) atomicExch(&g_cm_error, TSG_ERR_TIMEOUT);
+      ok = false;
+    }
+    __syncthreads();
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) epilogue<N>(tmem, smem, out, m0, ldo, bias, relu, out_f32);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
@@ -305,6 +452,65 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
   w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
+// Host side of the TMA form: the driver's tensor-map encoder, reached through the
+// runtime's entry-point query (the library links only the runtime), and the maps of the
+// two operands.
+std::atomic<int> g_gemm_mode{1};  // 0: TMA-loaded tiles, 1: thread-staged tiles
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// Map of a row-major BF16 matrix (rows x k, k contiguous) read in boxes of 64 K x box_rows
+// rows, 128-byte swizzle.
+tsg_status operand_map(CUtensorMap* map, const void* ptr, uint64_t rows, uint64_t k,
+                       uint32_t box_rows) {
+  auto encode = tensor_map_encoder();
+  if (!encode) return fail(TSG_ERR_UNSUPPORTED, "cm_gemm: cuTensorMapEncodeTiled unavailable");
+  const cuuint64_t dims[2] = {k, rows};
+  const cuuint64_t strides[1] = {k * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kTmaBoxK, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims,
+                            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: tensor map rejected (" + std::to_string((int)r) + ")");
+  return TSG_OK;
+}
+
+template <int N>
+tsg_status launch_gemm_tma(const void* a, const void* b, int64_t m, int64_t k, const float* bias,
+                           int32_t relu, void* out, int64_t ldo, int32_t out_f32,
+                           cudaStream_t st) {
+  CUtensorMap ma, mb;
+  TSG_TRY(operand_map(&ma, a, (uint64_t)m, (uint64_t)k, kTileM));
+  TSG_TRY(operand_map(&mb, b, (uint64_t)N, (uint64_t)k, N));
+  constexpr int smem = tma_smem_bytes<N>();
+  static std::once_flag attr;
+  cudaError_t aerr = cudaSuccess;
+  std::call_once(attr, [&] {
+    aerr = cudaFuncSetAttribute(gemm_bf16_tma_kernel<N>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  });
+  TSG_CUDA_TRY(aerr);
+  gemm_bf16_tma_kernel<N><<<(unsigned)(m / kTileM), kThreads, smem, st>>>(
+      ma, mb, bias, out, (int)k, (int)ldo, relu, out_f32);
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
 }  // namespace cm
 }  // namespace tsg
 
@@ -326,6 +532,11 @@ tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void* a_dev,
     return fail(TSG_ERR_INVALID_ARGUMENT, "cm_gemm: output rows must be a multiple of 16 bytes apart");
   const dim3 grid((unsigned)(m / cm::kTileM));
   cudaStream_t st = (cudaStream_t)stream;
+  if (cm::g_gemm_mode.load(std::memory_order_relaxed) == 0) {
+    if (n == 64)
+      return cm::launch_gemm_tma<64>(a_dev, b_dev, m, k, bias_dev, relu, out_dev, ldo, out_f32, st);
+    return cm::launch_gemm_tma<128>(a_dev, b_dev, m, k, bias_dev, relu, out_dev, ldo, out_f32, st);
+  }
   const auto* a = (const __nv_bfloat16*)a_dev;
   const auto* b = (const __nv_bfloat16*)b_dev;
   switch (n) {
@@ -339,6 +550,13 @@ tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void* a_dev,
       break;
   }
   TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
+}
+
+tsg_status tsg_cm_set_gemm_mode(int32_t mode) {
+  if (mode != 0 && mode != 1)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "cm_set_gemm_mode: 0 (TMA) or 1 (thread-staged)");
+  cm::g_gemm_mode.store(mode, std::memory_order_relaxed);
   return TSG_OK;
 }
 

@@ -26,8 +26,20 @@ def _gemm(a, b, bias=None, relu=False, out_f32=True):
     return out
 
 
-@pytest.mark.parametrize("m,n,k", [(128, 64, 64), (128, 128, 64), (256, 128, 256), (1024, 128, 128)])
-def test_gemm_matches_host_product(cuda, m, n, k):
+@pytest.fixture(params=[0, 1], ids=["tma", "staged"])
+def gemm_mode(request):
+    lib = _native.lib()
+    _native.check(lib.tsg_cm_set_gemm_mode(request.param))
+    yield request.param
+    _native.check(lib.tsg_cm_set_gemm_mode(DEFAULT_GEMM_MODE))
+
+
+DEFAULT_GEMM_MODE = 1
+
+
+@pytest.mark.parametrize("m,n,k", [(128, 64, 64), (128, 128, 64), (256, 128, 256), (1024, 128, 128),
+                                   (384, 64, 192)])
+def test_gemm_matches_host_product(cuda, gemm_mode, m, n, k):
     g = torch.Generator().manual_seed(m + n + k)
     a = torch.randn(m, k, generator=g).to(torch.bfloat16)
     b = torch.randn(n, k, generator=g).to(torch.bfloat16)
