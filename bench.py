@@ -1191,7 +1191,7 @@ def run_costmodel_gemm(args) -> None:
         forms[name] = {"ms_per_launch": t,
                        "max_rel_error_vs_fp32": float((out.float() - want).abs().max()
                                                       / want.abs().max())}
-    _native.check(lib.tsg_cm_set_gemm_mode(1))
+    _native.check(lib.tsg_cm_set_gemm_mode(0))
     ms = forms["tma"]["ms_per_launch"]
     err = forms["tma"]["max_rel_error_vs_fp32"]
     ms_cublas = timed(cublas, steps)

@@ -425,9 +425,9 @@ TSG_API tsg_status tsg_cm_gemm_bf16(int64_t m, int64_t n, int64_t k, const void*
 
 /* out[v] = sum of h[u] over the children u of node v (BF16 rows of `width`; children of v
  * are child[cstart[v] .. cstart[v+1]); out row stride ldo). */
-/* Operand staging of tsg_cm_gemm_bf16 for the whole process: 0 loads the A and B tiles
- * with TMA tensor copies (cp.async.bulk.tensor, 128-byte swizzle, one thread issuing
- * copies and MMAs), 1 stages them with the CTA's threads (canonical layout without
+/* Operand staging of tsg_cm_gemm_bf16 for the whole process: 0 (default) loads the A and
+ * B tiles with TMA tensor copies (cp.async.bulk.tensor, 128-byte swizzle, one thread
+ * issuing copies and MMAs), 1 stages them with the CTA's threads (canonical layout without
  * swizzle). Both give the same products. */
 TSG_API tsg_status tsg_cm_set_gemm_mode(int32_t mode);
 TSG_API tsg_status tsg_cm_child_sum(const void* h_dev, const int32_t* cstart_dev,

@@ -455,7 +455,7 @@ __global__ void adam_kernel(float* __restrict__ w, const float* __restrict__ g,
 // Host side of the TMA form: the driver's tensor-map encoder, reached through the
 // runtime's entry-point query (the library links only the runtime), and the maps of the
 // two operands.
-std::atomic<int> g_gemm_mode{1};  // 0: TMA-loaded tiles, 1: thread-staged tiles
+std::atomic<int> g_gemm_mode{0};  // 0: TMA-loaded tiles (default), 1: thread-staged tiles
 
 PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static std::once_flag once;

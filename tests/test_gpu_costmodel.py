@@ -34,7 +34,7 @@ def gemm_mode(request):
     _native.check(lib.tsg_cm_set_gemm_mode(DEFAULT_GEMM_MODE))
 
 
-DEFAULT_GEMM_MODE = 1
+DEFAULT_GEMM_MODE = 0
 
 
 @pytest.mark.parametrize("m,n,k", [(128, 64, 64), (128, 128, 64), (256, 128, 256), (1024, 128, 128),
