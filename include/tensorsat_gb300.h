@@ -17,7 +17,8 @@
  *
  * Reference interfaces replaced (paths are relative to the tensorsat project root):
  *   tsg_contract2_or_and     FinRel._contract2            tensorsat/lang/fin_rel.py:255-288
- *   tsg_contract2_count_u64  the unclamped einsum of the #SAT prototype
+ *   tsg_contract2_count_u64, tsg_contract2_modp
+ *                            the unclamped einsum of the #SAT prototype
  *                            notebooks/prototypes/2025-02-13-#sat-tensor-contraction.ipynb
  *                            (cells 11-12); the count semantics FinRel itself never offers
  *   tsg_rewire_or_and        FinRel._rewire                tensorsat/lang/fin_rel.py:379-393
@@ -96,6 +97,20 @@ TSG_API tsg_status tsg_contract2_count_u64(const uint64_t* lhs_dev, int32_t lhs_
                                    const int64_t* rhs_wires, const int64_t* rhs_dims,
                                    int32_t out_rank, const int64_t* out_wires,
                                    uint64_t* out_dev, void* stream);
+
+/* The same index semantics over residues: num_primes (1..4) planes of uint32 residues
+ * (plain, 0 <= x < p) lie back to back in lhs, rhs and out (plane q of a tensor at
+ * q * its entry count); plane q of out is sum(lhs * rhs) mod primes[q] (any moduli >= 2),
+ * each product reduced, so no intermediate overflows. The per-step form of exact model
+ * counting modulo several primes, recombined by CRT on the host; counterpart of
+ * tsg_contract2_count_u64 beyond 2^64 (FinRel._contract2's einsum,
+ * tensorsat/lang/fin_rel.py:255-288, without the clamp). */
+TSG_API tsg_status tsg_contract2_modp(const uint32_t* lhs_dev, int32_t lhs_rank,
+                              const int64_t* lhs_wires, const int64_t* lhs_dims,
+                              const uint32_t* rhs_dev, int32_t rhs_rank,
+                              const int64_t* rhs_wires, const int64_t* rhs_dims,
+                              int32_t out_rank, const int64_t* out_wires, int32_t num_primes,
+                              const uint32_t* primes, uint32_t* out_dev, void* stream);
 
 /* out = sign(rewire(in, out_ports)): permute / duplicate (diagonal) / discard (sum)
  * ports of a uint8 {0,1} tensor. Replaces FinRel._rewire. */

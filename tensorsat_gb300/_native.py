@@ -45,6 +45,7 @@ EXPORTED_SYMBOLS = (
     "tsg_abi_version",
     "tsg_contract2_or_and",
     "tsg_contract2_count_u64",
+    "tsg_contract2_modp",
     "tsg_rewire_or_and",
     "tsg_union_or",
     "tsg_spider_fill",
@@ -120,6 +121,10 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_contract2_or_and.argtypes = c2
     lib.tsg_contract2_count_u64.restype = c_int32
     lib.tsg_contract2_count_u64.argtypes = c2
+    lib.tsg_contract2_modp.restype = c_int32
+    lib.tsg_contract2_modp.argtypes = [c_void_p, c_int32, _i64p, _i64p, c_void_p, c_int32, _i64p,
+                                       _i64p, c_int32, _i64p, c_int32, POINTER(c_uint32),
+                                       c_void_p, c_void_p]
     lib.tsg_rewire_or_and.restype = c_int32
     lib.tsg_rewire_or_and.argtypes = [c_void_p, c_int32, _i64p, c_int32, _i32p, c_void_p,
                                       c_void_p]

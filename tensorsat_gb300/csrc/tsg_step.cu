@@ -63,7 +63,123 @@ struct GenericArgs {
   int64_t sum_dim[kMaxWires];
   int64_t sum_ls[kMaxWires];
   int64_t sum_rs[kMaxWires];
+  int64_t lhs_numel, rhs_numel;  // plane strides of the modular form
+  uint32_t mod[TSG_MAX_PRIMES];  // moduli of the modular form, one per plane
 };
+
+// lhs / rhs offsets of output entry t; false off the diagonal of repeated output wires
+// (the entry is then zero).
+__device__ __forceinline__ bool decode_output(const GenericArgs& a, int64_t t, int64_t* lo_out,
+                                              int64_t* ro_out) {
+  int64_t coord[kMaxWires];
+  for (int w = 0; w < a.n_wires; ++w) coord[w] = -1;
+  int64_t rem = t, lo = 0, ro = 0;
+  bool on_diagonal = true;
+  for (int p = a.n_out - 1; p >= 0; --p) {
+    const int64_t d = a.out_dim[p];
+    const int64_t c = rem % d;
+    rem /= d;
+    const int w = a.out_wire[p];
+    if (coord[w] < 0) {
+      coord[w] = c;
+      lo += c * a.wire_ls[w];
+      ro += c * a.wire_rs[w];
+    } else if (coord[w] != c) {
+      on_diagonal = false;
+    }
+  }
+  *lo_out = lo;
+  *ro_out = ro;
+  return on_diagonal;
+}
+
+// Modulus of plane q, selected without dynamic indexing of the parameter block.
+__device__ __forceinline__ uint32_t plane_mod(const GenericArgs& a, int q) {
+  uint32_t m = a.mod[0];
+#pragma unroll
+  for (int i = 1; i < TSG_MAX_PRIMES; ++i)
+    if (q == i) m = a.mod[i];
+  return m;
+}
+
+// Residues mod p (plain, 0 <= x < p) of every plane (blockIdx.y): out = sum of lhs * rhs
+// over the summed wires, each product reduced mod p and the sum once more at the end.
+__global__ void generic_modp_kernel(const uint32_t* __restrict__ lhs,
+                                    const uint32_t* __restrict__ rhs, uint32_t* __restrict__ out,
+                                    GenericArgs a) {
+  const int q = blockIdx.y;
+  const uint64_t p = plane_mod(a, q);
+  const uint32_t* L = lhs + q * a.lhs_numel;
+  const uint32_t* R = rhs + q * a.rhs_numel;
+  uint32_t* O = out + q * a.total;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.total; t += stride) {
+    int64_t lo, ro;
+    uint64_t acc = 0;
+    if (decode_output(a, t, &lo, &ro)) {
+      int64_t kc[kMaxWires];
+      for (int i = 0; i < a.n_sum; ++i) kc[i] = 0;
+      int64_t klo = 0, kro = 0;
+      int64_t terms = 0;
+      while (true) {
+        acc += ((uint64_t)L[lo + klo] * R[ro + kro]) % p;
+        if (++terms == (int64_t(1) << 30)) {  // sums of reduced products stay below 2^62
+          acc %= p;
+          terms = 0;
+        }
+        int i = a.n_sum - 1;
+        for (; i >= 0; --i) {
+          if (++kc[i] < a.sum_dim[i]) {
+            klo += a.sum_ls[i];
+            kro += a.sum_rs[i];
+            break;
+          }
+          klo -= (a.sum_dim[i] - 1) * a.sum_ls[i];
+          kro -= (a.sum_dim[i] - 1) * a.sum_rs[i];
+          kc[i] = 0;
+        }
+        if (i < 0) break;
+      }
+    }
+    O[t] = (uint32_t)(acc % p);
+  }
+}
+
+// Split-K form of the modular contraction: one block per output entry and plane.
+__global__ void generic_modp_splitk_kernel(const uint32_t* __restrict__ lhs,
+                                           const uint32_t* __restrict__ rhs,
+                                           uint32_t* __restrict__ out, GenericArgs a) {
+  __shared__ uint64_t red[128];
+  const int q = blockIdx.y;
+  const uint64_t p = plane_mod(a, q);
+  const uint32_t* L = lhs + q * a.lhs_numel;
+  const uint32_t* R = rhs + q * a.rhs_numel;
+  uint32_t* O = out + q * a.total;
+  for (int64_t t = blockIdx.x; t < a.total; t += gridDim.x) {
+    int64_t lo, ro;
+    uint64_t acc = 0;
+    if (decode_output(a, t, &lo, &ro)) {
+      for (int64_t kk = threadIdx.x; kk < a.ksize; kk += blockDim.x) {
+        int64_t r2 = kk, klo = 0, kro = 0;
+        for (int i = a.n_sum - 1; i >= 0; --i) {
+          const int64_t c = r2 % a.sum_dim[i];
+          r2 /= a.sum_dim[i];
+          klo += c * a.sum_ls[i];
+          kro += c * a.sum_rs[i];
+        }
+        acc = (acc + ((uint64_t)L[lo + klo] * R[ro + kro]) % p) % p;
+      }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) red[threadIdx.x] = (red[threadIdx.x] + red[threadIdx.x + s]) % p;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) O[t] = (uint32_t)red[0];
+    __syncthreads();
+  }
+}
 
 template <typename T, bool kOrAnd>
 __global__ void generic_contract_kernel(const T* __restrict__ lhs, const T* __restrict__ rhs,
@@ -236,6 +352,13 @@ tsg_status build_generic(int32_t lhs_rank, const int64_t* lhs_wires, const int64
   std::memset(a, 0, sizeof(*a));
   a->n_out = out_rank;
   a->rhs_is_one = rhs_one ? 1 : 0;
+  a->lhs_numel = a->rhs_numel = 1;
+  for (int i = 0; i < lhs_rank; ++i)
+    if (mul_overflows(a->lhs_numel, lhs_dims[i], &a->lhs_numel))
+      return fail(TSG_ERR_TOO_LARGE, "contract2: operand size overflows int64");
+  for (int i = 0; i < rhs_rank; ++i)
+    if (mul_overflows(a->rhs_numel, rhs_dims[i], &a->rhs_numel))
+      return fail(TSG_ERR_TOO_LARGE, "contract2: operand size overflows int64");
   std::map<int64_t, int> out_id;
   int64_t total = 1;
   for (int p = 0; p < out_rank; ++p) {
@@ -344,6 +467,39 @@ tsg_status tsg_contract2_count_u64(const uint64_t* lhs_dev, int32_t lhs_rank,
   TSG_TRY(build_generic(lhs_rank, lhs_wires, lhs_dims, rhs_rank, rhs_wires, rhs_dims, out_rank,
                         out_wires, &a));
   return launch_generic<uint64_t, false>(lhs_dev, rhs_dev, out_dev, a, (cudaStream_t)stream);
+}
+
+tsg_status tsg_contract2_modp(const uint32_t* lhs_dev, int32_t lhs_rank,
+                              const int64_t* lhs_wires, const int64_t* lhs_dims,
+                              const uint32_t* rhs_dev, int32_t rhs_rank,
+                              const int64_t* rhs_wires, const int64_t* rhs_dims,
+                              int32_t out_rank, const int64_t* out_wires, int32_t num_primes,
+                              const uint32_t* primes, uint32_t* out_dev, void* stream) {
+  if (!lhs_dev || !rhs_dev || !out_dev)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "contract2: null tensor pointer");
+  if (rhs_rank < 0) return fail(TSG_ERR_INVALID_ARGUMENT, "contract2: negative rhs rank");
+  if (num_primes < 1 || num_primes > TSG_MAX_PRIMES || !primes)
+    return fail(TSG_ERR_INVALID_ARGUMENT, "contract2_modp: 1..4 moduli expected");
+  GenericArgs a;
+  TSG_TRY(build_generic(lhs_rank, lhs_wires, lhs_dims, rhs_rank, rhs_wires, rhs_dims, out_rank,
+                        out_wires, &a));
+  for (int q = 0; q < num_primes; ++q) {
+    if (primes[q] < 2) return fail(TSG_ERR_INVALID_ARGUMENT, "contract2_modp: moduli must be >= 2");
+    a.mod[q] = primes[q];
+  }
+  if (a.total == 0) return TSG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const unsigned threads = 128;
+  if (a.ksize > 256 && a.total < 4096) {
+    const unsigned blocks = (unsigned)std::min<int64_t>(a.total, (int64_t)device_sm_count() * 8);
+    generic_modp_splitk_kernel<<<dim3(blocks, (unsigned)num_primes), threads, 0, st>>>(
+        lhs_dev, rhs_dev, out_dev, a);
+  } else {
+    generic_modp_kernel<<<dim3(grid_for((uint64_t)a.total, threads, 8), (unsigned)num_primes),
+                          threads, 0, st>>>(lhs_dev, rhs_dev, out_dev, a);
+  }
+  TSG_CUDA_TRY(cudaGetLastError());
+  return TSG_OK;
 }
 
 tsg_status tsg_rewire_or_and(const uint8_t* in_dev, int32_t rank, const int64_t* dims,

@@ -104,6 +104,49 @@ def test_count_u64_per_step_matches_oracle(cuda):
         np.testing.assert_array_equal(out.cpu().numpy().view(np.uint64), exp)
 
 
+def test_modp_per_step_matches_oracle(cuda):
+    """tsg_contract2_modp: per plane, the residues of the exact einsum (the oracle's integer
+    count of the same contraction) modulo each prime; 3 planes, repeated and summed wires,
+    and sums long enough for the split-K form."""
+    rng = np.random.default_rng(11)
+    lib = _native.lib()
+    primes = [2147483647, 2147483629, 2147483587]
+    arr = (_native.c_uint32 * 3)(*primes)
+    for case in range(40):
+        if case >= 34:  # at most 2 outputs over 2^10 or more summed entries (split-K form)
+            lw = [int(x) for x in rng.choice(12, size=10, replace=False)]
+            rw = [int(x) for x in rng.choice(12, size=10, replace=False)]
+            dims = {w: 2 for w in range(12)}
+            ow = [int(x) for x in rng.choice(sorted(set(lw) | set(rw)),
+                                             size=int(rng.integers(0, 2)), replace=False)]
+        else:
+            lw = [int(x) for x in rng.integers(0, 5, size=int(rng.integers(1, 5)))]
+            rw = [int(x) for x in rng.integers(0, 5, size=int(rng.integers(1, 5)))]
+            dims = {w: int(rng.integers(1, 4)) for w in range(5)}
+            present = sorted(set(lw) | set(rw))
+            ow = [int(x) for x in rng.choice(present, size=int(rng.integers(0, len(present) + 1)),
+                                             replace=False)]
+        a = rng.integers(0, 1 << 31, size=[3] + [dims[w] for w in lw], dtype=np.int64)
+        b = rng.integers(0, 1 << 31, size=[3] + [dims[w] for w in rw], dtype=np.int64)
+        for q, p in enumerate(primes):
+            a[q] %= p
+            b[q] %= p
+        ta = torch.from_numpy(a.astype(np.uint32).view(np.int32)).to(cuda)
+        tb = torch.from_numpy(b.astype(np.uint32).view(np.int32)).to(cuda)
+        out = torch.empty([3] + [dims[w] for w in ow], dtype=torch.int32, device=cuda)
+        _native.check(lib.tsg_contract2_modp(
+            ta.data_ptr(), len(lw), _native.i64_array(lw), _native.i64_array(a.shape[1:]),
+            tb.data_ptr(), len(rw), _native.i64_array(rw), _native.i64_array(b.shape[1:]),
+            len(ow), _native.i64_array(ow), 3, arr, out.data_ptr(), 0))
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().view(np.uint32)
+        for q, p in enumerate(primes):
+            exact = orc.contract2_count(a[q].astype(object), lw, b[q].astype(object), rw, ow)
+            want = np.vectorize(lambda x: int(x) % p, otypes=[object])(np.asarray(exact, dtype=object))
+            np.testing.assert_array_equal(got[q].astype(np.int64), want.astype(np.int64),
+                                          err_msg=str((case, q, lw, rw, ow)))
+
+
 def test_union_spider_scalar_stack(cuda):
     a = CudaRel(np.array([[0, 1], [0, 0]], dtype=np.uint8))
     b = CudaRel(np.array([[0, 0], [1, 0]], dtype=np.uint8))
