@@ -666,27 +666,67 @@ tsg_status fill_tile_operand(TileOperand& op, const int* pos, const OperandDesc&
     std::vector<std::pair<int, int>> cb;
     for (const auto& pr : lo)
       if (pr.first < 4) cb.push_back(pr);
-    if (cb.empty() || cb.size() > 3) {
-      *ok = false;  // excluded by the choice of V
-      return TSG_OK;
-    }
-    op.mode = kModePerm;
-    op.pn = 1 << cb.size();
-    for (int dd = 0; dd < op.pn; ++dd) {
-      uint32_t off = 0;
-      for (size_t k = 0; k < cb.size(); ++k)
-        if ((dd >> k) & 1) off |= 1u << cb[k].second;
-      op.dtab[dd] = off;
-    }
-    for (int i = 0; i < 4; ++i) {
-      uint32_t sel = 0;
-      for (int t = 0; t < 4; ++t) {
-        const int j = 4 * i + t;
-        uint32_t dd = 0;
-        for (size_t k = 0; k < cb.size(); ++k) dd |= (uint32_t)((j >> cb[k].first) & 1) << k;
-        sel |= dd << (4 * t);
+    if (cb.size() == 4) {
+      // kModeQuad (quad_operand admitted it): F bits fa, fb are operand bits 0, 1; fc, fd
+      // select one of four words
+      int fbyte[2] = {-1, -1};
+      std::vector<std::pair<int, int>> word;  // (F bit, operand bit) of the word-selecting bits
+      for (const auto& pr : cb) {
+        if (pr.second <= 1) fbyte[pr.second] = pr.first;
+        else word.push_back(pr);
       }
-      op.psel[i] = sel;
+      if (fbyte[0] < 0 || fbyte[1] < 0 || word.size() != 2) {
+        *ok = false;
+        return TSG_OK;
+      }
+      op.mode = kModeQuad;
+      for (int q = 0; q < 4; ++q)
+        op.dtab[q] = ((q & 1) ? (1u << word[0].second) : 0u) + ((q & 2) ? (1u << word[1].second) : 0u);
+      for (int i = 0; i < 4; ++i) {
+        int src[2] = {-1, -1};
+        uint32_t sel = 0;
+        for (int t = 0; t < 4; ++t) {
+          const int j = 4 * i + t;
+          const int q = ((j >> word[0].first) & 1) | (((j >> word[1].first) & 1) << 1);
+          const int byte = ((j >> fbyte[0]) & 1) | (((j >> fbyte[1]) & 1) << 1);
+          int slot = q == src[0] ? 0 : (q == src[1] ? 1 : -1);
+          if (slot < 0) {
+            slot = src[0] < 0 ? 0 : 1;
+            if (src[slot] >= 0) {
+              *ok = false;  // three source words: excluded by quad_operand
+              return TSG_OK;
+            }
+            src[slot] = q;
+          }
+          sel |= (uint32_t)(slot * 4 + byte) << (4 * t);
+        }
+        if (src[1] < 0) src[1] = src[0];
+        op.qsrc[i] = (uint32_t)src[0] | ((uint32_t)src[1] << 2);
+        op.psel[i] = sel;
+      }
+    } else {
+      if (cb.empty() || cb.size() > 3) {
+        *ok = false;  // excluded by the choice of V
+        return TSG_OK;
+      }
+      op.mode = kModePerm;
+      op.pn = 1 << cb.size();
+      for (int dd = 0; dd < op.pn; ++dd) {
+        uint32_t off = 0;
+        for (size_t k = 0; k < cb.size(); ++k)
+          if ((dd >> k) & 1) off |= 1u << cb[k].second;
+        op.dtab[dd] = off;
+      }
+      for (int i = 0; i < 4; ++i) {
+        uint32_t sel = 0;
+        for (int t = 0; t < 4; ++t) {
+          const int j = 4 * i + t;
+          uint32_t dd = 0;
+          for (size_t k = 0; k < cb.size(); ++k) dd |= (uint32_t)((j >> cb[k].first) & 1) << k;
+          sel |= dd << (4 * t);
+        }
+        op.psel[i] = sel;
+      }
     }
   }
   op.has_e = ep.empty() ? 0 : 1;
@@ -704,6 +744,29 @@ tsg_status fill_tile_operand(TileOperand& op, const int* pos, const OperandDesc&
     if (even) op.mode = kModeDual;
   }
   return TSG_OK;
+}
+
+// OR-AND, V = 16, an operand carrying all four fastest output bits (F bits 0-3): readable
+// as four aligned 4-byte words when two of those bits are its own bits 0 and 1, at most
+// one of the other two is an F bit below 2 (so each output word draws on at most two
+// words), and every other term of its offsets is a multiple of 4 (its constant offset,
+// output bits above 3, summed and slot bits).
+bool quad_operand(const StepInfo& st, const OperandDesc& d, int o) {
+  int low = 0, hi_small = 0;
+  for (int b = 0; b < 4; ++b) {
+    const int p = st.pos[o][b];
+    if (p < 0) return false;
+    if (p <= 1) low++;
+    else if (b < 2) hi_small++;
+  }
+  if (low != 2 || hi_small > 1 || (d.base & 3) != 0) return false;
+  for (int i = 4; i < st.out_bits; ++i)
+    if (st.pos[o][i] >= 0 && st.pos[o][i] < 2) return false;
+  for (const auto& pr : d.kp)
+    if (pr.second < 2) return false;
+  for (const auto& pr : d.gp)
+    if (pr.second < 2) return false;
+  return true;
 }
 
 // Builds the tile form of step s from the operand descriptions; sets *ok = false when the
@@ -750,7 +813,8 @@ tsg_status build_tile(const StepInfo& st, const OperandDesc d[2], const StepArgs
           ident = ident && p == b;
         }
       }
-      if (carried == 4) ok16 = ident && (d[o].base & 15) == 0;
+      if (carried == 4 && !(ident && (d[o].base & 15) == 0))
+        ok16 = quad_operand(st, d[o], o);
     }
     if (ok16) v = 16;
   }
@@ -861,6 +925,22 @@ tsg_status check_tile_bounds(const RunCtx& c, int s, const LaunchArgs& la) {
     for (int e = 0; e < sh.ne; ++e) ok = ok && (op.e_off[e] & vmask) == 0;
     for (int kk = 0; kk < t.n_k; ++kk) ok = ok && (op.k_off[kk] & vmask) == 0;
     if (!ok) return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: vector load not aligned");
+  }
+  // Word loads of kModeQuad: every offset term but the four fastest positions, and every
+  // word offset, must be a multiple of 4 bytes.
+  for (int o = 0; o < 2 && sh.v == 16; ++o) {
+    const TileOperand& op = t.op[o];
+    if (op.mode != kModeQuad) continue;
+    bool ok = (op.base & 3) == 0 && (op.plane & 3) == 0;
+    for (int i = 0; i < op.g.n; ++i) ok = ok && op.g.dst[i] >= 2;
+    for (int i = 0; i < op.f_hi.n; ++i) ok = ok && op.f_hi.dst[i] >= 2;
+    for (int i = 0; i < op.f_lo.n; ++i)
+      for (int b = 0; b < op.f_lo.len[i]; ++b)
+        if (op.f_lo.src[i] + b >= 4) ok = ok && op.f_lo.dst[i] + b >= 2;
+    for (int q = 0; q < 4; ++q) ok = ok && (op.dtab[q] & 3) == 0;
+    for (int e = 0; e < sh.ne; ++e) ok = ok && (op.e_off[e] & 3) == 0;
+    for (int kk = 0; kk < t.n_k; ++kk) ok = ok && (op.k_off[kk] & 3) == 0;
+    if (!ok) return fail(TSG_ERR_INVALID_ARGUMENT, "tile bounds: word loads not aligned");
   }
   // Two-element vector loads (kModeDual): every offset term but the first position bit
   // must be even.

@@ -251,6 +251,11 @@ constexpr int kModePerm = 4;
 // V = 4, count rings: positions at offsets {0, 1, d, d + 1} (two adjacent pairs), read as
 // two 2-element vector loads
 constexpr int kModeDual = 5;
+// OR-AND, V = 16: the operand carries all four fastest positions, two of them as its own
+// bits 0 and 1 (one aligned 4-byte word) and two elsewhere; four word loads at dtab[0..3]
+// and, per output word i, one __byte_perm of words qsrc[i] & 3 and qsrc[i] >> 2 with
+// selector psel[i]
+constexpr int kModeQuad = 6;
 constexpr int kMaxE = 4;   // enumerated output combinations per thread (|E| <= 2)
 constexpr int kMaxK = 64;  // summed combinations kept in tables (k <= 6)
 
@@ -276,7 +281,8 @@ struct TileOperand {
   int32_t leaf;           // uint8 leaf (widened on load)
   int32_t pn;             // kModePerm: distinct values (2, 4 or 8)
   uint32_t dtab[8];       // kModePerm: their offsets
-  uint32_t psel[4];       // kModePerm: __byte_perm selector of each output word
+  uint32_t psel[4];       // kModePerm / kModeQuad: __byte_perm selector of each output word
+  uint32_t qsrc[4];       // kModeQuad: source words of each output word (2 bits each)
 };
 
 struct TileArgs {
@@ -416,6 +422,16 @@ __device__ __forceinline__ void tile_load_packed(const TileOperand& op, uint64_t
 #pragma unroll
     for (int j = 0; j < 4; ++j) r |= (((op.pair_sel >> j) & 1) ? x1 : x0) << (8 * j);
     w[0] = r;
+  } else if (V == 16 && op.mode == kModeQuad) {
+    // four aligned words (alignment proven on the host); selects, not an indexed array
+    const uint32_t q0 = *reinterpret_cast<const uint32_t*>(base + off);
+    const uint32_t q1 = *reinterpret_cast<const uint32_t*>(base + off + op.dtab[1]);
+    const uint32_t q2 = *reinterpret_cast<const uint32_t*>(base + off + op.dtab[2]);
+    const uint32_t q3 = *reinterpret_cast<const uint32_t*>(base + off + op.dtab[3]);
+    auto pick = [&](uint32_t q) { return q == 0 ? q0 : (q == 1 ? q1 : (q == 2 ? q2 : q3)); };
+#pragma unroll
+    for (int i = 0; i < V / 4; ++i)
+      w[i] = __byte_perm(pick(op.qsrc[i] & 3u), pick((op.qsrc[i] >> 2) & 3u), op.psel[i]);
   } else if (V == 16 && op.mode == kModePerm) {
     uint32_t w0 = 0, w1 = 0;
 #pragma unroll
