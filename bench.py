@@ -74,8 +74,8 @@ def parse_args():
                    help="held-out n=60 instances of the learned-path leg of the default run")
     p.add_argument("--learned-candidates", type=int, default=64,
                    help="planner candidate trees the cost model ranks per instance")
-    p.add_argument("--cm-train", type=int, default=160, help="costmodel: training instances")
-    p.add_argument("--cm-heldout", type=int, default=32, help="costmodel: held-out n=60 instances")
+    p.add_argument("--cm-train", type=int, default=320, help="costmodel: training instances")
+    p.add_argument("--cm-heldout", type=int, default=64, help="costmodel: held-out n=60 instances")
     p.add_argument("--cm-epochs", type=int, default=150, help="costmodel: training epochs")
     p.add_argument("--cm-out", default="", help="costmodel: write the trained weights (.npz)")
     p.add_argument("--workload", default="n60",
