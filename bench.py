@@ -79,7 +79,7 @@ def parse_args():
     p.add_argument("--cm-epochs", type=int, default=150, help="costmodel: training epochs")
     p.add_argument("--cm-out", default="", help="costmodel: write the trained weights (.npz)")
     p.add_argument("--workload", default="n60",
-                   choices=["n60", "ragged", "costmodel", "costmodel-gemm"],
+                   choices=["n60", "ragged", "costmodel", "costmodel-eval", "costmodel-gemm"],
                    help="n60: the single-instance headline workload; ragged: a batch of "
                         "random instances of uneven sizes (batched runs, CUDA graphs)")
     p.add_argument("--instances", type=int, default=512, help="ragged: batch size")
@@ -1080,6 +1080,49 @@ def learned_leg(held, cands, dpll_held, group: int = 16) -> dict:
     }
 
 
+def run_costmodel_eval(args) -> None:
+    """Evaluates the committed cost model (no training) on --cm-heldout held-out n=60,
+    m=256 instances (seeds 10000 on), 4 planner candidates each, every candidate measured
+    on the device: prediction error, and the measured device time of the model's pick
+    against the planner's pick and the best candidate."""
+    import numpy as np
+
+    from tensorsat_gb300 import _native
+
+    _native.lib()
+    held = costmodel_heldout(args.cm_heldout)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with cpu_pool(cores) as pool:
+        cand_held = pool.map(_candidates_job, [(c.num_vars, c.clauses, 4) for c in held],
+                             chunksize=4)
+        dpll_held = pool.map(_dpll_instance, [(c.num_vars, c.clauses) for c in held[:4]])
+    plan_s = time.perf_counter() - t0
+
+    import torch
+
+    from tensorsat_gb300 import costmodel
+
+    torch.cuda.set_device(0)
+    group = 16
+    model = costmodel.CostModel(seed=0)
+    model.load_state(dict(np.load(COSTMODEL_FILE)))
+    t0 = time.perf_counter()
+    rows = costmodel_measure(held, cand_held, group)
+    measure_s = time.perf_counter() - t0
+    ev = costmodel_evaluate(model, held, rows, dpll_held, 4)
+    line = {
+        "metric": "committed cost model on held-out 3-SAT n=60 m=256 instances: "
+                  "|log predicted - log measured| device time per slice",
+        "value": ev["mean_abs_log_error"], "unit": "mean abs log error",
+        "higher_is_better": False, **ev,
+        "seconds": {"planning": round(plan_s, 1), "measuring": round(measure_s, 1)},
+        "config": {"weights": "plans/costmodel_n60.npz", "candidates_per_instance": 4,
+                   "measure": f"tsg_plan_run_timed, {group} slices, 3-prime count + OR-AND"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_costmodel(args) -> None:
     """Trains the cost model on measured candidate trees of random 3-SAT instances (n
     uniform in [24, 56]) and evaluates it on held-out n=60, m=256 instances: prediction
@@ -1223,6 +1266,8 @@ def main() -> None:
         run_ragged(args)
     elif args.workload == "costmodel":
         run_costmodel(args)
+    elif args.workload == "costmodel-eval":
+        run_costmodel_eval(args)
     elif args.workload == "costmodel-gemm":
         run_costmodel_gemm(args)
     else:
