@@ -15,6 +15,10 @@ Serving form: :meth:`BatchContraction.count` and :meth:`BatchContraction.contrac
 the captured leaf pools in place, so a stream of inputs pays one host-to-device copy, one
 graph launch and one read-back per batch.
 
+:meth:`BatchContraction.serve` pipelines such a stream: while the GPU contracts one batch
+of inputs, the host packs the next batch's leaves into the other of two pinned staging
+buffers and reads back the previous batch's answers.
+
 Results are the same as running each network through its own
 :class:`~tensorsat_gb300.contractions.gpu.GpuContraction`: SAT bits in the OR-AND
 semiring, exact model counts modulo 31-bit primes recombined by CRT.
@@ -24,7 +28,7 @@ from __future__ import annotations
 
 import ctypes
 import math
-from collections.abc import Sequence
+from collections.abc import Iterable, Iterator, Sequence
 from typing import Any
 
 import numpy as np
@@ -116,6 +120,9 @@ class BatchContraction:
         self.last_launches = 0  # kernel launches of the last run (or capture)
         self._staging: torch.Tensor | None = None    # pinned host copy of the leaf pools
         self._staged: torch.cuda.Event | None = None  # the staging buffer's last copies
+        self._serve_stage: list[torch.Tensor | None] = [None, None]  # serve()'s two buffers
+        self._need: int | None = None                # cached primes_needed()
+        self._need_pool: np.ndarray | None = None    # host leaves it was computed from
 
     @property
     def contractions(self) -> list[GpuContraction]:
@@ -166,6 +173,7 @@ class BatchContraction:
             off += host.size
         self._staged = torch.cuda.Event()
         self._staged.record()
+        self._keep_bound(stage[:total], [dl for _, dl in parts])
         return total
 
     def groups(self, ring: int, planes: int, budget_bytes: int | None = None) -> list[int]:
@@ -283,12 +291,7 @@ class BatchContraction:
         """Replays this batch's cached graph for (ring, primes, groups), capturing it on
         first use (with ``workspace``, which the graph keeps); returns its result buffers,
         which the next replay overwrites."""
-        key = (ring, tuple(primes), None if groups is None else tuple(groups))
-        g = self._graphs.get(key)
-        if g is None:
-            g = self.capture(ring, primes, groups, workspace)
-            self._graphs[key] = g
-        res = g.replay()
+        res = self._replay_graph(ring, primes, groups, workspace).replay()
         GpuContraction.check_device()
         return res
 
@@ -322,11 +325,28 @@ class BatchContraction:
         return bounds
 
     def primes_needed(self) -> int:
-        bound = max(self.count_bounds())
-        n = 1
-        while sum(math.log2(p) for p in PRIMES_31[:n]) <= bound:
-            n += 1
-        return n
+        """31-bit primes whose product exceeds every diagram's count bound. Cached: a new
+        input batch (:meth:`load`, :meth:`serve`) whose leaf entries are all at most the
+        ones the bound was computed from keeps it, since a count only grows with its leaf
+        entries (all non-negative)."""
+        if self._need is None:
+            bound = max(self.count_bounds())
+            n = 1
+            while sum(math.log2(p) for p in PRIMES_31[:n]) <= bound:
+                n += 1
+            self._need = n
+            parts = [c._host_pool(d) for c, d in zip(self._contractions, self._diagrams)]
+            self._need_pool = (None if any(dl for _, dl in parts)
+                               else np.concatenate([h for h, _ in parts]))
+        return self._need
+
+    def _keep_bound(self, staged: np.ndarray, device_leaves: Sequence[Any]) -> None:
+        """Drops the cached prime count unless the staged host leaves of a new input batch
+        are entrywise at most those it was computed from (and no leaf is on the device)."""
+        ref = self._need_pool
+        if ref is None or any(device_leaves) or staged.size != ref.size or \
+                not bool(np.all(staged <= ref)):
+            self._need = None
 
     def count(self, num_primes: int | None = None,
               groups: Sequence[int] | None = None, *, graph: bool = False,
@@ -356,6 +376,124 @@ class BatchContraction:
             counts = crt([planes[p] for p in range(num_primes)], primes)
             out.append(c._counts_from_root(counts))
         return out
+
+    def _stage(self, diagrams: Sequence[Diagram], slot: int) -> list:
+        """Validates ``diagrams`` (this batch's wirings, in order) and packs their host
+        leaves into pinned staging buffer ``slot`` (0 or 1); returns the device leaves
+        that :meth:`GpuContraction._finish_pool` writes."""
+        diagrams = list(diagrams)
+        if len(diagrams) != len(self):
+            raise ValueError(f"expected {len(self)} diagrams, got {len(diagrams)}")
+        for c, d in zip(self._contractions, diagrams):
+            c.validate(d)
+        parts = [c._host_pool(d) for c, d in zip(self._contractions, diagrams)]
+        total = sum(host.size for host, _ in parts)
+        buf = self._serve_stage[slot]
+        if buf is None or buf.numel() < total:
+            buf = torch.empty(max(1, total), dtype=torch.uint8, pin_memory=True)
+            self._serve_stage[slot] = buf
+        stage = buf.numpy()
+        off = 0
+        for pool, (host, _) in zip(self.pools(), parts):
+            if pool.numel() != host.size:
+                raise RuntimeError("leaf pool size changed")
+            stage[off: off + host.size] = host
+            off += host.size
+        return [dl for _, dl in parts]
+
+    def serve(self, batches: Iterable[Sequence[Diagram]], num_primes: int | None = None, *,
+              groups: Sequence[int] | None = None, sat_groups: Sequence[int] | None = None,
+              workspace: torch.Tensor | None = None) -> Iterator[tuple[list[Any], list[CudaRel]]]:
+        """Serves a stream of input batches (each a list of diagrams with this batch's
+        wirings, in order) and yields, per batch, its exact model counts and OR-AND result
+        boxes (as :meth:`count` and :meth:`contract` give them; ``bool(box)`` is a closed
+        network's SAT bit). One graph per ring is captured on
+        the first batch and replayed for every batch; while the GPU contracts batch k, the
+        host packs batch k+1's leaves into the other of two pinned staging buffers and
+        reads back batch k-1's answers, so a pass costs about the larger of the host and
+        the device time instead of their sum."""
+        need = self.primes_needed()
+        if num_primes is None:
+            num_primes = need
+        if num_primes < need or num_primes > _native.TSG_MAX_PRIMES:
+            raise OverflowError(f"the batch's count bounds need {need} 31-bit primes "
+                                f"(at most {_native.TSG_MAX_PRIMES} per run)")
+        primes = PRIMES_31[:num_primes]
+        dev = _device.require_cuda()
+        stream = torch.cuda.current_stream(dev)
+        if self._pools is None:
+            self.pools()
+        copied = [torch.cuda.Event(), torch.cuda.Event()]  # staging buffer free again
+        for ev in copied:
+            ev.record(stream)
+        g_count = g_sat = None
+        pending = None  # (done event, pinned results, sizes) of the batch in flight
+        slot = 0
+        for diagrams in batches:
+            copied[slot].synchronize()  # the copies out of this buffer (two batches ago) ran
+            diagrams = list(diagrams)
+            device_leaves = self._stage(diagrams, slot)
+            buf = self._serve_stage[slot]
+            self._diagrams = diagrams
+            self._keep_bound(buf.numpy()[:sum(p.numel() for p in self._pools)],
+                             device_leaves)
+            if self.primes_needed() > num_primes:
+                raise OverflowError(f"a served batch needs {self._need} 31-bit primes; the "
+                                    f"stream was started with {num_primes}")
+            off = 0
+            for c, pool, dl in zip(self._contractions, self._pools, device_leaves):
+                n = pool.numel()
+                pool.copy_(buf[off: off + n], non_blocking=True)
+                c._finish_pool(pool, dl)
+                off += n
+            copied[slot].record(stream)
+            if g_count is None:
+                g_count = self._replay_graph(_native.TSG_RING_MODP, primes, groups, workspace)
+                g_sat = self._replay_graph(_native.TSG_RING_OR_AND, (), sat_groups, workspace)
+            g_count.replay()
+            g_sat.replay()
+            res = g_count.results + g_sat.results
+            flat = torch.cat([r.reshape(-1).view(torch.uint8) for r in res])
+            host = torch.empty(flat.numel(), dtype=torch.uint8, pin_memory=True)
+            host.copy_(flat, non_blocking=True)
+            done = torch.cuda.Event()
+            done.record(stream)
+            if pending is not None:
+                yield self._serve_answers(*pending, primes)
+            pending = (done, host, [(r.dtype, tuple(r.shape), r.numel() * r.element_size())
+                                    for r in res])
+            slot ^= 1
+        if pending is not None:
+            yield self._serve_answers(*pending, primes)
+
+    def _replay_graph(self, ring: int, primes: Sequence[int], groups: Sequence[int] | None,
+                      workspace: torch.Tensor | None) -> BatchGraph:
+        key = (ring, tuple(primes), None if groups is None else tuple(groups))
+        g = self._graphs.get(key)
+        if g is None:
+            g = self.capture(ring, primes, groups, workspace)
+            self._graphs[key] = g
+        return g
+
+    def _serve_answers(self, done: torch.cuda.Event, host: torch.Tensor, sizes: list,
+                       primes: Sequence[int]) -> tuple[list[Any], list[CudaRel]]:
+        done.synchronize()
+        GpuContraction.check_device()
+        raw = host.numpy()
+        arrays, off = [], 0
+        for dtype, shape, nbytes in sizes:
+            dt = {torch.uint8: np.uint8, torch.int32: np.int32, torch.int64: np.int64}[dtype]
+            arrays.append(raw[off: off + nbytes].view(dt).reshape(shape))
+            off += nbytes
+        n = len(self)
+        counts = []
+        for c, h in zip(self._contractions, arrays[:n]):
+            planes = h.view(np.uint32).reshape(len(primes), -1)
+            counts.append(c._counts_from_root(crt([planes[p] for p in range(len(primes))],
+                                                  primes)))
+        boxes = [c._box_from_root(torch.from_numpy(h.copy()))
+                 for c, h in zip(self._contractions, arrays[n:])]
+        return counts, boxes
 
     def __repr__(self) -> str:
         return f"<BatchContraction of {len(self)} networks>"

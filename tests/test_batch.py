@@ -261,6 +261,48 @@ def test_batch_serving_graphs_follow_loaded_leaves(cuda):
         batch.load(one[:-1])
 
 
+@pytest.mark.gpu
+def test_batch_serve_pipelines_input_batches(cuda):
+    """serve() yields, per input batch, the counts and SAT bits that load() + count() /
+    contract() give, while it packs the next batch during the current one's replays; the
+    batches alternate between inputs with variable 1 fixed to 1 and to 0."""
+    instances = ragged_instances(6, 12, 18, seed=9)
+    one = [cnf.clause_diagram("1" + "?" * (cnf.num_vars - 1)) for cnf in instances]
+    zero = [cnf.clause_diagram("0" + "?" * (cnf.num_vars - 1)) for cnf in instances]
+    exp1 = [orc.brute_force_count(c.num_vars, list(c.clauses) + [(1,)]) for c in instances]
+    exp0 = [orc.brute_force_count(c.num_vars, list(c.clauses) + [(-1,)]) for c in instances]
+    batch = BatchContraction(CudaRel, one, target_bits=8, trials=1)
+    stream = [one, zero, one, zero, zero]
+    want = [exp1, exp0, exp1, exp0, exp0]
+    got = list(batch.serve(stream, num_primes=3))
+    assert len(got) == len(stream)
+    for (counts, boxes), exp in zip(got, want):
+        assert counts == exp
+        assert [bool(b) for b in boxes] == [e > 0 for e in exp]
+    assert len(batch._graphs) == 2  # one capture per ring
+
+
+def test_batch_prime_count_is_cached_while_leaves_shrink():
+    """primes_needed() is computed once; a new input batch whose leaf entries are all at
+    most the first ones keeps it (counts only shrink), any larger entry drops it."""
+    instances = ragged_instances(3, 10, 14, seed=6)
+    free = [cnf.clause_diagram() for cnf in instances]
+    fixed = [cnf.clause_diagram("1" + "?" * (cnf.num_vars - 1)) for cnf in instances]
+    batch = BatchContraction(CudaRel, free, target_bits=8, trials=1)
+    need = batch.primes_needed()
+    assert batch._need == need and batch._need_pool is not None
+    parts = [c._host_pool(d) for c, d in zip(batch.contractions, fixed)]
+    staged = np.concatenate([h for h, _ in parts])
+    assert np.all(staged <= batch._need_pool)
+    batch._keep_bound(staged, [dl for _, dl in parts])
+    assert batch._need == need
+    bigger = staged.copy()
+    bigger[np.argmin(batch._need_pool)] = 1 if batch._need_pool.min() == 0 else 255
+    batch._keep_bound(bigger, [])
+    assert batch._need is None
+    assert batch.primes_needed() == need
+
+
 def test_ragged_plan_only_report_runs_on_the_host():
     """bench.py --workload ragged --plan-only plans a batch on the host cores and reports
     its algorithmic bytes per n without touching a GPU."""
