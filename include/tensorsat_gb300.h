@@ -374,6 +374,12 @@ TSG_API tsg_status tsg_plan_subset_dp(int32_t n, int32_t words, const uint64_t* 
  * record is cleared. Runs launched before the failure are invalid. */
 TSG_API tsg_status tsg_take_device_error(void* stream);
 
+/* Enqueues on `stream` a copy of the device-side failure record (0: none) into *host_dst
+ * (4 bytes; pinned host memory keeps the copy asynchronous) without synchronizing or
+ * clearing it, so a pipelined caller can check a finished run after waiting on its own
+ * event; when the copy reads non-zero, tsg_take_device_error reports and clears it. */
+TSG_API tsg_status tsg_peek_device_error_async(int32_t* host_dst, void* stream);
+
 /* Limit of every bounded wait inside the streaming kernel (a consumer waiting for staged
  * data, the producer waiting for a free stage), in nanoseconds of the GPU's global timer;
  * between 1 us and the default 2 s. A wait that runs out makes the kernel record

@@ -73,6 +73,7 @@ EXPORTED_SYMBOLS = (
     "tsg_batch_lanes_workspace_bytes",
     "tsg_batch_run_lanes",
     "tsg_batch_packed_workspace_bytes",
+    "tsg_peek_device_error_async",
     "tsg_batch_run_packed",
     "tsg_plan_set_step_options",
     "tsg_plan_variants_workspace_bytes",
@@ -178,6 +179,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.tsg_batch_run_lanes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
                                         POINTER(c_uint32), POINTER(c_void_p), _i64p, c_int32,
                                         c_void_p, c_int64, POINTER(c_void_p), c_void_p]
+    lib.tsg_peek_device_error_async.restype = c_int32
+    lib.tsg_peek_device_error_async.argtypes = [c_void_p, c_void_p]
     lib.tsg_batch_packed_workspace_bytes.restype = c_int32
     lib.tsg_batch_packed_workspace_bytes.argtypes = [c_int32, POINTER(c_void_p), c_int32, c_int32,
                                                      _i64p, c_int32, _i64p]

@@ -456,12 +456,16 @@ class BatchContraction:
             flat = torch.cat([r.reshape(-1).view(torch.uint8) for r in res])
             host = torch.empty(flat.numel(), dtype=torch.uint8, pin_memory=True)
             host.copy_(flat, non_blocking=True)
+            # the failure record as of this batch, read with the results (no stream sync)
+            flag = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+            _native.check(_native.lib().tsg_peek_device_error_async(flag.data_ptr(),
+                                                                    stream.cuda_stream))
             done = torch.cuda.Event()
             done.record(stream)
             if pending is not None:
                 yield self._serve_answers(*pending, primes)
-            pending = (done, host, [(r.dtype, tuple(r.shape), r.numel() * r.element_size())
-                                    for r in res])
+            pending = (done, host, flag, [(r.dtype, tuple(r.shape),
+                                           r.numel() * r.element_size()) for r in res])
             slot ^= 1
         if pending is not None:
             yield self._serve_answers(*pending, primes)
@@ -475,10 +479,11 @@ class BatchContraction:
             self._graphs[key] = g
         return g
 
-    def _serve_answers(self, done: torch.cuda.Event, host: torch.Tensor, sizes: list,
-                       primes: Sequence[int]) -> tuple[list[Any], list[CudaRel]]:
+    def _serve_answers(self, done: torch.cuda.Event, host: torch.Tensor, flag: torch.Tensor,
+                       sizes: list, primes: Sequence[int]) -> tuple[list[Any], list[CudaRel]]:
         done.synchronize()
-        GpuContraction.check_device()
+        if int(flag[0]) != 0:
+            GpuContraction.check_device()  # synchronizes, clears and raises the failure
         raw = host.numpy()
         arrays, off = [], 0
         for dtype, shape, nbytes in sizes:

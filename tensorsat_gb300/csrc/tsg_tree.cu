@@ -2421,6 +2421,13 @@ tsg_status tsg_take_device_error(void* stream) {
                                "complete); results of the affected runs are invalid");
 }
 
+tsg_status tsg_peek_device_error_async(int32_t* host_dst, void* stream) {
+  if (!host_dst) return fail(TSG_ERR_INVALID_ARGUMENT, "peek_device_error: null destination");
+  TSG_CUDA_TRY(cudaMemcpyFromSymbolAsync(host_dst, g_device_error, sizeof(int), 0,
+                                         cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  return TSG_OK;
+}
+
 tsg_status tsg_plan_run_static(const tsg_plan* plan, int32_t ring, int32_t num_primes,
                                const uint32_t* primes, const uint8_t* leaf_pool_dev,
                                int64_t slice_begin, int64_t slice_end, int64_t group_size,
