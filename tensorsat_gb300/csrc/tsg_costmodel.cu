@@ -498,13 +498,16 @@ tsg_status launch_gemm_tma(const void* a, const void* b, int64_t m, int64_t k, c
   TSG_TRY(operand_map(&ma, a, (uint64_t)m, (uint64_t)k, kTileM));
   TSG_TRY(operand_map(&mb, b, (uint64_t)N, (uint64_t)k, N));
   constexpr int smem = tma_smem_bytes<N>();
-  static std::once_flag attr;
-  cudaError_t aerr = cudaSuccess;
-  std::call_once(attr, [&] {
-    aerr = cudaFuncSetAttribute(gemm_bf16_tma_kernel<N>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  });
-  TSG_CUDA_TRY(aerr);
+  // the shared-memory opt-in is per device: set it once on each device that launches
+  static std::atomic<uint64_t> attr_set{0};
+  int dev = 0;
+  TSG_CUDA_TRY(cudaGetDevice(&dev));
+  const uint64_t bit = dev < 64 ? (uint64_t(1) << dev) : 0;
+  if (!bit || !(attr_set.load(std::memory_order_acquire) & bit)) {
+    TSG_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16_tma_kernel<N>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    attr_set.fetch_or(bit, std::memory_order_release);
+  }
   gemm_bf16_tma_kernel<N><<<(unsigned)(m / kTileM), kThreads, smem, st>>>(
       ma, mb, bias, out, (int)k, (int)ldo, relu, out_f32);
   TSG_CUDA_TRY(cudaGetLastError());
