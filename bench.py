@@ -16,12 +16,25 @@ The tree is the committed plan ``plans/3sat_n60_m256_rng0_t26.json`` (the projec
 planner with ``target_bits=26, trials=8, seed=0``; ``--replan`` plans again), so both arms
 contract the same tree and the reference arm loads no native code.
 
+The autotuner's committed entries for that plan and GPU (``plans/*.tune.json``) set the
+slice group per ring and the per-step kernel options (``--no-tuning`` runs the executor's
+own choices).
+
 ``batched`` (default run, one GPU): a bounded ragged batch of random 3-SAT instances (n
 uniform in [30, 40], clause ratio uniform in [3.5, 5.0], seeded per instance), planned on
-the host cores before the first CUDA call, timed as captured-graph replays, in the plain
-per-instance form (``GpuContraction.count`` + ``.contract``) and in the serving form
-(``BatchContraction.load`` + ``graph=True``), with every count and SAT bit checked against
-the oracle's DPLL counts.
+the host cores before the first CUDA call, timed as captured-graph replays (small steps of
+a tree level packed across instances, and one launch per step for comparison), in the
+plain per-instance form (``GpuContraction.count`` + ``.contract``) and in the serving forms
+(``BatchContraction.serve`` pipelined over a stream of input batches; ``load`` +
+``graph=True`` one call after the other), with every count and SAT bit checked against the
+oracle's DPLL counts.
+
+``learned`` (default run): the committed cost model ranks 64 planner candidates of each of
+8 held-out n=60 instances; its picks and the planner's trees are timed on the device.
+
+Other workloads: ``--workload ragged`` (the batch alone), ``costmodel`` (train and
+evaluate the cost model), ``costmodel-eval`` (evaluate the committed weights on held-out
+instances), ``costmodel-gemm`` (the cost model's tensor-core layer against cuBLAS).
 
 ``--impl reference`` times the reference's CPU path for the same workload (the oracle's
 restatement of the upstream numpy contraction: per-slice einsum in the OR-AND semiring and
