@@ -55,3 +55,18 @@ def test_candidate_settings_split_and_merge():
     key = lambda ts: [(tuple(t.steps), s) for t, s in ts]
     assert key(merged)[0] == key(whole)[0]
     assert sorted(key(merged)) == sorted(key(whole))
+
+
+def test_cnf_candidates_in_spawned_workers():
+    """cnf_candidates splits each instance's planner settings over spawned workers and
+    merges them back: the same candidate set as one process, the planner's usual choice
+    first."""
+    import multiprocessing as mp
+
+    cnf = CNFInstance.random(3, 18, 76, rng=4)
+    whole = costmodel.candidate_trees(cnf.clause_diagram().wiring, 6)
+    with mp.get_context("spawn").Pool(2) as pool:
+        got = costmodel.cnf_candidates(pool, [cnf], 6, parts=3)[0]
+    key = lambda ts: [(tuple(t.steps), tuple(s)) for t, s in ts]
+    assert key(got)[0] == key(whole)[0]
+    assert sorted(key(got)) == sorted(key(whole))
