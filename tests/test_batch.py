@@ -329,3 +329,23 @@ def test_batch_load_checks_its_diagrams_before_any_device_work():
         batch.load(one[:-1])  # wrong count
     with pytest.raises(ValueError):
         batch.load(list(reversed(one)))  # other wirings
+
+
+def test_reference_arm_prints_its_line_on_the_host():
+    """bench.py --impl reference times the oracle's restatement of the reference's numpy
+    path on the host cores, loading the committed plan without the native library, and
+    prints one JSON line with the reference arm's keys."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    out = subprocess.run([sys.executable, str(root / "bench.py"), "--impl", "reference",
+                          "--steps", "1", "--warmup", "0"],
+                         capture_output=True, text=True, timeout=900, check=True)
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    assert line["config"]["slices_per_instance"] == 8192
