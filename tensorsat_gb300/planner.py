@@ -466,43 +466,94 @@ def reconfigure(tree: ContractionTree, subtree_size: int = 10, passes: int = 4,
     return ContractionTree(L, steps, node_wires, tree.out_wires)
 
 
+class _WireMatrix:
+    """The steps' wire sets of a tree as 0/1 matrices over its wires (rows: steps), for
+    evaluating many candidate slicings at once. Sums over steps run in step order
+    (sequential accumulation), so every value equals :meth:`ContractionTree.cost`'s."""
+
+    def __init__(self, tree: ContractionTree) -> None:
+        L = tree.num_leaves
+        self.wires = sorted(set().union(*tree.node_wires)) if tree.node_wires else []
+        col = {w: i for i, w in enumerate(self.wires)}
+        n = len(tree.steps)
+        self.union = np.zeros((n, len(self.wires)), dtype=np.int64)
+        self.out = np.zeros((n, len(self.wires)), dtype=np.int64)
+        for s in range(n):
+            for w in tree.step_union(s):
+                self.union[s, col[w]] = 1
+            for w in tree.node_wires[L + s]:
+                self.out[s, col[w]] = 1
+        self.col = col
+
+    def sizes(self, sliced: Sequence[int]) -> tuple[np.ndarray, np.ndarray]:
+        """Per step: unsliced wires of the step's index space and of its result."""
+        u = self.union.sum(axis=1)
+        o = self.out.sum(axis=1)
+        for w in sliced:
+            if w in self.col:
+                u = u - self.union[:, self.col[w]]
+                o = o - self.out[:, self.col[w]]
+        return u, o
+
+
+def _log2_total(u: np.ndarray) -> np.ndarray:
+    """log2 of the sum over steps (axis 0, in step order) of 2^u, per column; 0 for an
+    empty sum, like :meth:`ContractionTree.cost`."""
+    if u.shape[0] == 0:
+        return np.zeros(u.shape[1:])
+    tot = np.add.accumulate(np.ldexp(1.0, u), axis=0)[-1]  # exact powers, summed in order
+    return np.array([math.log2(t) if t > 0 else 0.0 for t in np.atleast_1d(tot)]).reshape(
+        np.shape(tot))
+
+
 def slice_tree(tree: ContractionTree, target_bits: int, forbid: frozenset[int] = frozenset()
                ) -> frozenset[int]:
     """Greedy slicing: repeatedly slice the wire of a largest intermediate that lowers the
-    peak most, breaking ties by the smallest total (all-slices) cost."""
-    sliced: set[int] = set()
-    L = tree.num_leaves
+    peak most, breaking ties by the smallest total (all-slices) cost (then the smallest
+    wire). All candidate wires of a round are evaluated at once on the steps' wire
+    matrices."""
+    m = _WireMatrix(tree)
+    sliced: list[int] = []
+    u, o = m.sizes(())
     while True:
-        tot, peak, _ = tree.cost(frozenset(sliced))
+        peak = int(o.max()) if o.size else 0
         if peak <= target_bits:
             return frozenset(sliced)
-        cands: set[int] = set()
-        for s in range(len(tree.steps)):
-            ws = tree.node_wires[L + s] - sliced
-            if len(ws) == peak:
-                cands |= ws
-        cands -= forbid
+        at_peak = o == peak
+        cands = sorted(w for w in m.wires
+                       if w not in forbid and w not in sliced and
+                       bool(m.out[at_peak, m.col[w]].any()))
         if not cands:
             raise ValueError(
                 f"cannot slice below 2^{peak} entries: the largest intermediates only carry"
                 " output wires"
             )
+        cols = [m.col[w] for w in cands]
+        u2 = u[:, None] - m.union[:, cols]
+        p2 = (o[:, None] - m.out[:, cols]).max(axis=0)
+        t2 = _log2_total(u2)
         best = None
-        for w in sorted(cands):
-            t2, p2, _ = tree.cost(frozenset(sliced | {w}))
-            key = (p2, t2 + len(sliced) + 1)
+        for i, w in enumerate(cands):
+            key = (int(p2[i]), float(t2[i]) + len(sliced) + 1)
             if best is None or key < best[0]:
                 best = (key, w)
-        sliced.add(best[1])
+        w = best[1]
+        sliced.append(w)
+        u = u - m.union[:, m.col[w]]
+        o = o - m.out[:, m.col[w]]
 
 
 def unslice(tree: ContractionTree, sliced: frozenset[int], target_bits: int) -> frozenset[int]:
     """Drops sliced wires that are no longer needed to keep every intermediate within
     2^target_bits entries (each dropped wire halves the number of slices)."""
+    m = _WireMatrix(tree)
     sl = set(sliced)
+    _, o = m.sizes(sorted(sl))
     for w in sorted(sliced):
-        if tree.cost(frozenset(sl - {w}))[1] <= target_bits:
+        back = o + (m.out[:, m.col[w]] if w in m.col else 0)
+        if (int(back.max()) if back.size else 0) <= target_bits:
             sl.discard(w)
+            o = back
     return frozenset(sl)
 
 

@@ -44,3 +44,37 @@ def subset_dp_reference(n: int, bits: Sequence[int], keep: int, live: int,
             sub = (sub - 1) & rest
         best[m] = top
     return best[full], split, kept
+
+
+def slice_tree_reference(tree, target_bits: int, forbid=frozenset()):
+    """Set-based restatement of the planner's greedy slicing (one full cost evaluation
+    per candidate wire): the vectorised ``planner.slice_tree`` must pick the same wires."""
+    sliced = set()
+    L = tree.num_leaves
+    while True:
+        tot, peak, _ = tree.cost(frozenset(sliced))
+        if peak <= target_bits:
+            return frozenset(sliced)
+        cands = set()
+        for s in range(len(tree.steps)):
+            ws = tree.node_wires[L + s] - sliced
+            if len(ws) == peak:
+                cands |= ws
+        cands -= forbid
+        if not cands:
+            raise ValueError("cannot slice")
+        best = None
+        for w in sorted(cands):
+            t2, p2, _ = tree.cost(frozenset(sliced | {w}))
+            key = (p2, t2 + len(sliced) + 1)
+            if best is None or key < best[0]:
+                best = (key, w)
+        sliced.add(best[1])
+
+
+def unslice_reference(tree, sliced, target_bits: int):
+    sl = set(sliced)
+    for w in sorted(sliced):
+        if tree.cost(frozenset(sl - {w}))[1] <= target_bits:
+            sl.discard(w)
+    return frozenset(sl)

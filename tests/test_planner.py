@@ -4,6 +4,8 @@ executor's index semantics against brute force)."""
 
 from __future__ import annotations
 
+import random
+
 import numpy as np
 import pytest
 
@@ -329,3 +331,31 @@ def test_checkpointed_count_argument_errors(tmp_path):
     (tmp_path / "c.json").write_text('{"format": "something else"}')
     with pytest.raises(ValueError):
         c.count_checkpointed(closed, tmp_path / "c.json", chunk_slices=4, group=1)
+
+
+def test_vectorised_slicing_matches_the_set_based_restatement():
+    """planner.slice_tree / unslice evaluate all candidate wires of a round at once; they
+    pick exactly the wires the one-cost-per-candidate restatement picks (same sums in the
+    same order), on min-fill trees of random 3-, 4- and 5-SAT networks at several caps."""
+    from plan_dp_reference import slice_tree_reference, unslice_reference
+
+    from tensorsat_gb300.contractions.gpu import _network, _prepare
+
+    cases = [(3, 30, 128, 1), (3, 44, 187, 2), (3, 60, 256, 0), (4, 26, 250, 3), (5, 22, 300, 4)]
+    for k, n, m, seed in cases:
+        net = _network(_prepare(CNFInstance.random(k, n, m, rng=seed).clause_diagram().wiring))
+        rng = random.Random(seed)
+        tree = planner.build_tree(net, planner.minfill_order(net, rng,
+                                                             planner.simplify_order(net)))
+        forbid = frozenset(net.out_wires)
+        peak = tree.cost(frozenset())[1]
+        for cap in (peak - 1, peak - 4, max(6, peak - 10), 22):
+            if cap >= peak or cap < 1:
+                continue
+            try:
+                want = slice_tree_reference(tree, cap, forbid)
+            except ValueError:
+                continue
+            got = planner.slice_tree(tree, cap, forbid)
+            assert got == want, (k, n, seed, cap)
+            assert planner.unslice(tree, got, cap + 2) == unslice_reference(tree, got, cap + 2)
